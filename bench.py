@@ -1,0 +1,331 @@
+"""Benchmark of the GB300 PBD step: particle-steps/s on the 1M-particle fluid workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+
+Our arm (default): 100^3 = 1,000,000 fluid particles in a 128^3-cell domain (seed 2),
+4 solver iterations, vorticity 5e-4, XSPH viscosity 0.01, FP32.  `value` is particle-steps/s
+with the state resident in HBM (K frames replayed as CUDA graphs, CUDA events on the
+launching stream); `e2e` drives the reference-facing C ABI with host buffers each frame
+(pbd_clear + pbd_add_particles from pinned memory, pbd_step, pbd_get_state), copies inside
+the timed region.  The roofline entry is for the dominant kernel, timed with CUDA event
+pairs around each launch (pbd_profile_frames) over the same number of frames.
+
+Reference arm (--impl reference): the reference step has no CPU implementation and its CUDA
+code does not build with CUDA 13, so the arm times the oracle's FP32 OpenMP C
+transliteration of the reference kernels on the host cores, same workload and metric.
+
+Under torchrun (N > 1) every rank steps its own replica of the workload ("replicas only":
+the step has no exchange); value = particles x frames of all ranks / max rank time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "pbd-simulation-framework-cuda_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s (plain 1M-particle PBD step)"
+UNIT = "particle-steps/s"
+REST_DENSITY = 1000.0
+LAMBDA_EPS = 0.1
+L2_BYTES = 129 * 2 ** 20
+
+
+def algorithmic_bytes_per_particle_step(iterations=4, passes=3, vort_visc=True):
+    """B = 328 + 16 P + 88 I (vorticity and XSPH on) or 200 + 16 P + 88 I (off):
+    each per-particle array read or written once per data-dependent pass, FP32 float4 state."""
+    return (328 if vort_visc else 200) + 16 * passes + 88 * iterations
+
+
+# per-particle algorithmic bytes of one launch of each kernel
+KERNEL_BYTES = {
+    "predict_key": 84,      # read x, v, f_ext (48), write v, p*, key (36)
+    "onesweep_pass": 16,    # read key + value, write key + value
+    "reorder_cells": 112,   # read perm, key (8), gather x, p*, v (48), write (48), cell writes (8)
+    "lambda": 20,           # read p* (16), write lambda (4)
+    "delta": 68,            # read p*, lambda, x (36), write p*, x (32); +16 for v on the last pass
+    "omega": 48,            # read p*, v (32), write omega (16)
+    "vort_visc": 80,        # read p*, v, omega (48), write f_ext, v (32)
+    "update": 64,
+}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def build_workload(pbd, scenes, name):
+    w = scenes.WORKLOADS[name]
+    params = scenes.workload_params(pbd, w["box"], REST_DENSITY, vorticity=w["vorticity"], viscosity=w["viscosity"])
+    params.lambda_epsilon = LAMBDA_EPS
+    pos, vel = scenes.lattice(*w["shape"], seed=w["seed"])
+    return params, pos, vel, w
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [t.strip() for t in line.split(",")]
+                if len(f) < 7:
+                    continue
+                try:
+                    sms.append(float(f[0]))
+                    mx = float(f[1])
+                except ValueError:
+                    continue
+                for k, nm in enumerate(names):
+                    if f[3 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        except OSError:
+            pass
+        return {"sm_mhz": float(np.median(sms)) if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def cpu_baseline(name, max_seconds, threads=None):
+    """FP32 OpenMP transliteration of the reference step (oracle build), timed on host cores."""
+    import pbd
+    import scenes
+    from oracle import oracle as orc_mod
+    params, pos, vel, w = build_workload(pbd, scenes, name)
+    if threads:
+        orc_mod.set_threads(threads)
+    cores = orc_mod.max_threads()
+    o = orc_mod.Oracle(params, len(pos), "f32")
+    o.add_particles(pos, vel)
+    o.step(1)   # first frame (page faults of the list) outside the sample
+    frames, t0 = 0, time.perf_counter()
+    while True:
+        o.step(1)
+        frames += 1
+        el = time.perf_counter() - t0
+        if el >= max_seconds or frames >= 1000:
+            break
+    o.close()
+    rate = len(pos) * frames / el
+    return {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{name}: {len(pos)} particles x {frames} frames (after 1 untimed), {el:.1f} s, FP32 OpenMP"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    budget = max(5.0, min(120.0, 3.0 * (args.steps + args.warmup)))
+    cb = cpu_baseline(args.workload, budget)
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice)",
+            "config": {"workload": args.workload, "particles": 1000000 if args.workload == "fluid_1m" else None},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import pbd
+    import scenes
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    params, pos, vel, w = build_workload(pbd, scenes, args.workload)
+    n = len(pos)
+    sim = pbd.Sim(params, n)
+    sim.add_particles(pos, vel)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    # ---- warm-up (also records the CUDA graphs)
+    sim.step(args.warmup, stream=sh)
+    stream.synchronize()
+    sim.sync()
+    launches_per_step = sim.launches_per_step()
+
+    # ---- device-resident timing
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        sim.step(args.steps, stream=sh)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    sim.sync()
+    ms = ev0.elapsed_time(ev1)
+    t_rank = ms / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_rank], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_rank = float(t.item())
+    value = n * args.steps * world / t_rank
+
+    # ---- per-kernel device time over the same number of frames (direct launches)
+    prof = sim.profile(args.steps, stream=sh)
+    stream.synchronize()
+    sim.sync()
+    share = {k: v[1] for k, v in prof.items()}
+    top = max(share, key=share.get)
+    launches, total_ms = prof[top]
+    per_launch_s = total_ms / launches / 1e3
+    bytes_per = KERNEL_BYTES.get(top, 0) * n
+    if top == "delta":
+        # one of I delta launches also writes v: average the extra 16 B over the I launches
+        bytes_per += 16 * n / params.solver_iterations
+    achieved = bytes_per / per_launch_s / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        try:
+            traffic = json.load(open(tfile)).get(top)
+        except Exception:
+            traffic = None
+
+    # ---- end to end through the reference-facing ABI with host buffers
+    e2e_steps = max(3, min(args.steps, 50))
+    hx = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
+    hv = torch.empty((n, 4), dtype=torch.float32, pin_memory=True).numpy()
+    st = sim.state()
+    hx[:] = st["x"]
+    hv[:] = st["v"]
+    xp = hx.ctypes.data_as(pbd.C.POINTER(pbd.C.c_float))
+    vp = hv.ctypes.data_as(pbd.C.POINTER(pbd.C.c_float))
+    L = pbd.lib()
+
+    def e2e_frame():
+        pbd.check(L.pbd_clear(sim.h))
+        pbd.check(L.pbd_add_particles(sim.h, n, xp, vp, None))
+        pbd.check(L.pbd_step(sim.h, 1, pbd.C.c_void_p(sh)))
+        pbd.check(L.pbd_get_state(sim.h, xp, vp, None, None))
+
+    e2e_frame()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_frame()
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([t_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e_value = n * e2e_steps * world / t_e2e
+    sim.sync()
+
+    working_set = n * (16 * 3 + 16 * 3 + 4 + 16 + 16 * 2) + 2 * params.max_grid * 4
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded jittered lattice, SplitMix64)",
+        "config": {"workload": args.workload, "particles": n, "domain_cells": w["box"], "solver_iterations": 4,
+                   "vorticity": w["vorticity"], "xsph_viscosity": w["viscosity"], "rest_density": REST_DENSITY,
+                   "lambda_epsilon": LAMBDA_EPS, "parallelism": f"replicas x{world}",
+                   "l2": f"working set {working_set / 2**20:.0f} MiB > L2 {L2_BYTES / 2**20:.0f} MiB (no flush)"},
+        "clocks": clocks.summary(),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
+                "frames": e2e_steps},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": bytes_per, "launch_ms": per_launch_s * 1e3},
+        "step_roofline": {"bytes_per_particle_step": algorithmic_bytes_per_particle_step(),
+                          "achieved_gbs": algorithmic_bytes_per_particle_step() * value / world / 1e9,
+                          "frac": algorithmic_bytes_per_particle_step() * value / world / 1e9 / peak},
+        "kernel_ms_per_frame": {k: v[1] / args.steps for k, v in prof.items()},
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="fluid_1m")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,202 @@
+/*
+ * pbd.h -- C ABI of the GB300-native unified-particle PBD step.
+ *
+ * This library replaces the per-frame step of niklasandersson/PBD-Simulation-Framework-CUDA:
+ * `Fluid::compute()` (src/app/simulation/Fluid.cu:14-97) and the kernels it drives
+ * (src/app/simulation/kernel/{Forces,Hash,SortReorder,Collision,Density,Update}.h).
+ * The reference exposes that step as a C++ class behind `Cuda_Computable::compute()`
+ * (src/cuda/Cuda_Computable.h:8-23) plus parameterless launchers (kernel/Kernels.h:18-43)
+ * that read a global `__constant__ SimulationParameters params` (kernel/Globals.h:50-77)
+ * filled from config.txt every frame (kernel/Initialize.h:20-86).  Here the same step is
+ * one handle-based C API: plain pointers and sizes, no CUDA or torch types in the
+ * signatures (streams are passed as `void*` holding a cudaStream_t).
+ *
+ * Conventions
+ *  - Every function returns an int status (PBD_OK == 0) and never throws; the text of the
+ *    last error on the calling thread is returned by pbd_last_error().
+ *  - Particle state is float4 per particle (x, y, z, w), stored as 4 consecutive floats.
+ *  - A pbd_sim handle is externally synchronised: one host thread at a time.  Separate
+ *    handles are independent.  All GPU work of a call is queued on the stream passed to
+ *    it (NULL = the legacy default stream) and is asynchronous unless stated otherwise.
+ *  - Particles are kept in Morton-sorted order, exactly as the reference re-orders its
+ *    textures every frame (kernel/SortReorder.h:86-129); pbd_get_state returns that order.
+ */
+#ifndef PBD_H
+#define PBD_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBD_ABI_VERSION 1u
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define PBD_OK                0
+#define PBD_ERR_INVALID_ARG   1  /* null pointer, bad size, bad enum */
+#define PBD_ERR_CAPACITY      2  /* N + n would exceed the capacity given to pbd_create */
+#define PBD_ERR_CUDA          3  /* a CUDA runtime call failed (text in pbd_last_error) */
+#define PBD_ERR_CONFIG        4  /* config.txt could not be read or parsed */
+#define PBD_ERR_TIMEOUT       5  /* a bounded device-side wait gave up (no hang, no trap) */
+#define PBD_ERR_UNSUPPORTED   6  /* a valid reference option this build does not implement */
+#define PBD_ERR_ALLOC         7  /* device or host allocation failed */
+#define PBD_ERR_RANGE         8  /* a parameter is outside the range the reference's setters accept */
+
+/* ---- Active flags: Application.Simulation.Active.* (config.txt:40-52, Fluid.cu:21-96) ---- */
+#define PBD_ACTIVE_APPLY_FORCES            (1u << 0)
+#define PBD_ACTIVE_FIND_CONTACTS           (1u << 1)
+#define PBD_ACTIVE_FIND_NEIGHBOURS         (1u << 2)
+#define PBD_ACTIVE_COMPUTE_LAMBDA          (1u << 3)
+#define PBD_ACTIVE_COMPUTE_DELTA_POSITIONS (1u << 4)
+#define PBD_ACTIVE_APPLY_DELTA_POSITIONS   (1u << 5)
+#define PBD_ACTIVE_UPDATE_POSITIONS        (1u << 6)
+#define PBD_ACTIVE_COMPUTE_OMEGAS          (1u << 7)
+#define PBD_ACTIVE_COMPUTE_VORTICITY       (1u << 8)
+#define PBD_ACTIVE_COMPUTE_VISCOSITY       (1u << 9)
+#define PBD_ACTIVE_ALL                     0x3FFu
+
+/* ---- behaviour flags (pbd_params.flags) ------------------------------------------- */
+/* Reproduce kernel/SortReorder.h:183-184: at i == N-1 the reference writes
+ * cellEndings[N-1] = N (indexing by particle, not by cell).  When cell number N-1 is
+ * occupied and is not the last cell, its range then runs to N.  On by default. */
+#define PBD_FLAG_CELL_END_QUIRK  (1u << 0)
+/* Carry a uint32 particle id through every re-order so callers can follow particles. */
+#define PBD_FLAG_TRACK_IDS       (1u << 1)
+/* Carry the per-particle colour array through every re-order (kernel/SortReorder.h:106-107)
+ * and write colour = neighbourCount / maxNeighbours as findNeighbours does
+ * (kernel/Collision.h:118-120).  Off by default: colours are cosmetic. */
+#define PBD_FLAG_COLORS          (1u << 2)
+
+/* ---- parameters: mirrors SimulationParameters (kernel/Globals.h:50-75) plus the
+ *      config keys Fluid::compute reads directly (Fluid.cu:35-67).  Field comments give
+ *      the config.txt key under Application.Simulation unless stated otherwise. -------- */
+typedef struct pbd_params {
+    uint32_t struct_size;                 /* = sizeof(pbd_params); set by pbd_params_default */
+    uint32_t threads_per_block;           /* Application.Cuda.threadsPerBlock (advisory)      */
+    float    particle_radius;             /* Particles.particleRadius; diameter = 2 r          */
+    uint32_t max_neighbours_per_particle; /* Particles.maxNeighboursPerParticle (list cap M)   */
+    float    delta_t;                     /* Forces.deltaT                                      */
+    float    gravity;                     /* Forces.gravity (y component)                       */
+    float    rest_density;                /* Density.restDensity                                */
+    float    kernel_width_spiky;          /* Density.kernelWidthSpiky, x particle diameter      */
+    float    k_scorr;                     /* Density.kSCorr                                     */
+    int32_t  n_scorr;                     /* Density.nSCorr                                     */
+    float    q_scorr;                     /* Density.qSCorr, x spiky width                      */
+    float    c_viscosity;                 /* Viscosity.cViscosity                               */
+    float    kernel_width_poly;           /* Viscosity.kernelWidthPoly (absolute)               */
+    float    e_vorticity;                 /* Vorticity.eVorticity                               */
+    uint32_t collision_type;              /* Collision.collisionType (0 = per-contact Jacobi)   */
+    uint32_t kernel_width_neighbours;     /* Collision.kernelWidthNeighbours (cell shells)      */
+    uint32_t max_collision_batches;       /* Collision.maxCollisionBatches                      */
+    float    stiffness;                   /* Collision.stiffness                                */
+    float    enclosure_position_damping;  /* Enclosure.enclosurePositionDamping                 */
+    float    enclosure_velocity_damping;  /* Enclosure.enclosureVelocityDamping                 */
+    float    bounds_min[3];               /* Enclosure.{X,Y,Z}.min                              */
+    float    bounds_max[3];               /* Enclosure.{X,Y,Z}.max                              */
+    uint32_t solver_iterations;           /* Iterations.solverIterations                        */
+    uint32_t stabilization_iterations;    /* Iterations.stabilizationIterations                 */
+    uint32_t active;                      /* PBD_ACTIVE_* bitmask (Active.*)                    */
+    uint32_t max_grid;                    /* Morton cells addressable; 128^3 (Particles.cc:8)   */
+    float    lambda_epsilon;              /* relaxation eps of lambda = -C/(B+C+eps); 1e-4 (Density.h:90) */
+    uint32_t flags;                       /* PBD_FLAG_* bitmask                                 */
+} pbd_params;
+
+typedef struct pbd_sim pbd_sim;
+
+/* ---- parameters ------------------------------------------------------------------ */
+/* Fill *p with the values of the reference's config.txt (config.txt:9-131). */
+int pbd_params_default(pbd_params* p);
+/* Parse a config file in the reference's grammar (src/parser/ConfigParser.h:265-330 with
+ * comments, #define and #include) and overwrite the fields whose keys it holds.  Replaces
+ * Config::getInstance(file) + the getValue calls of kernel/Initialize.h:33-73. */
+int pbd_load_config(pbd_params* p, const char* path);
+/* Same, from an in-memory text.  `base_dir` resolves #include (may be NULL). */
+int pbd_parse_config(pbd_params* p, const char* text, const char* base_dir);
+/* Write *p as a config file in the reference's layout (ConfigParser.h:241-247). */
+int pbd_write_config(const pbd_params* p, const char* path);
+/* Check every field against the ranges of the reference's setters
+ * (kernel/Communication.h:440-624); PBD_ERR_RANGE names the first bad field. */
+int pbd_validate_params(const pbd_params* p);
+
+/* ---- lifecycle ------------------------------------------------------------------- */
+/* Replaces Fluid::Fluid() -> cudaInitializeKernels() (kernel/Initialize.h:122-130).
+ * `capacity` plays the role of maxParticles = textureWidth^2 (Particles.cc:12).
+ * Allocates every device buffer once; the step itself never allocates. */
+int pbd_create(const pbd_params* p, uint32_t capacity, pbd_sim** out);
+/* Replaces Fluid::~Fluid() -> cudaCleanupKernels() (kernel/Initialize.h:136-140). */
+int pbd_destroy(pbd_sim* sim);
+int pbd_set_params(pbd_sim* sim, const pbd_params* p);   /* validated like pbd_validate_params */
+int pbd_get_params(const pbd_sim* sim, pbd_params* p);
+int pbd_num_particles(const pbd_sim* sim, uint32_t* n);
+int pbd_capacity(const pbd_sim* sim, uint32_t* cap);
+
+/* ---- particle injection (kernel/Communication.h:22-67, 626-660) ------------------- */
+/* addParticlesCallback: append n particles at index N from host arrays of n float4
+ * (col may be NULL).  Rejected with PBD_ERR_CAPACITY when N + n > capacity (the reference
+ * returns silently).  Synchronous with respect to the host arrays. */
+int pbd_add_particles(pbd_sim* sim, uint32_t n, const float* pos4, const float* vel4,
+                      const float* col4);
+/* Same, from device pointers (no host copy); queued on `stream`. */
+int pbd_add_particles_device(pbd_sim* sim, uint32_t n, const float* d_pos4,
+                             const float* d_vel4, const float* d_col4, void* stream);
+/* addParticleCallback: one particle at pos with velocity 50*dir, w = 0. */
+int pbd_add_particle(pbd_sim* sim, const float pos[3], const float dir[3]);
+/* clearParticlesCallback: N = 0. */
+int pbd_clear(pbd_sim* sim);
+
+/* ---- the step -------------------------------------------------------------------- */
+/* Run `nsteps` frames of Fluid::compute() (Fluid.cu:14-97) on `stream` (a cudaStream_t,
+ * NULL = legacy default stream).  The whole frame is one CUDA graph launch; nothing is
+ * synchronised.  Simulation::step's cudaDeviceSynchronize (Simulation.cu:16-19) is
+ * pbd_sync(). */
+int pbd_step(pbd_sim* sim, int nsteps, void* stream);
+/* Wait for the sim's queued work and report device-side error words
+ * (PBD_ERR_TIMEOUT if a bounded wait gave up). */
+int pbd_sync(pbd_sim* sim);
+
+/* ---- state out (synchronous; host pointers, any may be NULL) ------------------------ */
+int pbd_get_state(pbd_sim* sim, float* pos4, float* vel4, float* pred4, uint32_t* ids);
+/* Device pointers of the current state buffers (valid until the next pbd_step/add/clear). */
+int pbd_get_device_state(pbd_sim* sim, const float** d_pos4, const float** d_vel4,
+                         const float** d_pred4);
+
+/* ---- introspection for tests and tools -------------------------------------------- */
+/* After a step: the sorted Morton keys, the sort permutation (index before the sort of
+ * the particle now at i), cellStart/cellEnd for the first `ncells` cells, per-particle
+ * lambda and f_ext (float4).  Any pointer may be NULL. */
+int pbd_debug_dump(pbd_sim* sim, uint32_t* keys, uint32_t* perm, uint32_t* cell_start,
+                   uint32_t* cell_end, uint32_t ncells, float* lambda, float* fext4,
+                   float* omega4);
+/* Materialise the neighbour list the reference would build this frame (findContacts +
+ * findNeighbours, kernel/Collision.h:11-160): `list` is N x max_entries uint32, `count`
+ * and `contacts` are N uint32.  Entries beyond max_entries are counted but not stored. */
+int pbd_debug_neighbours(pbd_sim* sim, uint32_t max_entries, uint32_t* list,
+                         uint32_t* count, uint32_t* contacts);
+/* Run only the front of a frame: applyForces, initializeCellIds, sortIds, reorder,
+ * resetCellInfo/computeCellInfo (Fluid.cu:21-33).  For bit-exact tests of keys,
+ * permutation and cell ranges. */
+int pbd_debug_front(pbd_sim* sim, void* stream);
+/* Number of kernels one pbd_step frame launches (for launch accounting). */
+int pbd_launches_per_step(pbd_sim* sim, uint32_t* n);
+/* Run `nsteps` frames with direct launches (no graph) and a CUDA event pair around every
+ * kernel; per kernel name, the launches and their summed device time.  For profiling only
+ * (the reference has no counterpart: its only timer is an FPS counter,
+ * src/glfw/GLFW_Window.cc:63-86). */
+typedef struct pbd_kernel_stat {
+    char     name[32];
+    uint32_t launches;
+    float    total_ms;
+} pbd_kernel_stat;
+int pbd_profile_frames(pbd_sim* sim, int nsteps, void* stream, pbd_kernel_stat* stats,
+                       uint32_t max_stats, uint32_t* n_stats);
+
+/* Text of the last error on this thread ("" if none). */
+const char* pbd_last_error(void);
+uint32_t pbd_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PBD_H */

@@ -1,0 +1,92 @@
+// pbd_device.cuh -- device-side parameter block and the per-pair arithmetic of the step.
+//
+// Everything here restates the reference's device helpers in our own code:
+//   Morton hashing          kernel/Hash.h:10-34
+//   poly6 / spiky kernels   kernel/Density.h:14-42
+//   wall confinement        kernel/Forces.h:19-59
+// The parameter block replaces `__constant__ SimulationParameters params`
+// (kernel/Globals.h:50-77): it is passed by value to every kernel (kernel parameters live
+// in the constant bank), so separate simulations never share a global.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pbd {
+
+constexpr uint32_t kEmptyCell = 0xFFFFFFFFu;   // UINT_MAX start = empty cell (SortReorder.h:146)
+
+struct DevParams {
+    uint32_t N;            // numberOfParticles this frame
+    uint32_t G;            // maxGrid (cells addressable by the tables)
+    uint32_t M;            // maxNeighboursPerParticle (list cap)
+    uint32_t K;            // kernelWidthNeighbours (cell shells)
+    uint32_t active;       // PBD_ACTIVE_* bits
+    uint32_t flags;        // PBD_FLAG_* bits
+    int32_t  n_scorr;
+    uint32_t far_pairs_zero;  // 1 when pairs beyond every kernel support contribute exactly 0
+    float d;               // particleDiameter = 2 r
+    float dt, gravity;
+    float rho0;
+    float hs, hp;          // spiky width (x diameter already applied), poly width
+    float hp2;             // hp*hp
+    float k_scorr;
+    float c_visc, e_vort;
+    float stiffness, one_minus_stiffness;
+    float pos_damp, vel_damp;
+    float lambda_eps;
+    float bmin[3], bmax[3];
+    float poly_inv_den;    // 1 / (0.001 + 64 pi hp^9)   (Density.h:21, double there)
+    float spiky_den;       // pi * hs^6                  (Density.h:37)
+    float wq;              // poly6(q), the s_corr reference value (Density.h:138)
+    float cut2;            // max(hp, hs, d)^2: beyond it no kernel and no contact is non-zero
+};
+
+// ---------------------------------------------------------------- Morton (Hash.h) -----
+__device__ __forceinline__ uint32_t expand_bits(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+// Per-axis part of mortonCode: clamp to [0, 1023], truncate, spread.
+__device__ __forceinline__ uint32_t morton_axis(float c) {
+    c = fminf(fmaxf(c, 0.0f), 1023.0f);
+    return expand_bits((uint32_t)c);
+}
+
+__device__ __forceinline__ uint32_t morton(float x, float y, float z) {
+    return (morton_axis(x) << 2) + (morton_axis(y) << 1) + morton_axis(z);
+}
+
+// ---------------------------------------------------------- pair kernels (Density.h) --
+// poly6Viscosity: W = 315 t^3 t^3 / den, t = hp^2 - d^2, for 0.001 < d < hp - 0.001.
+__device__ __forceinline__ float poly6(const DevParams& P, float dist) {
+    if (dist > 0.001f && dist < P.hp - 0.001f) {
+        float t = __fsub_rn(P.hp2, __fmul_rn(dist, dist));
+        float t3 = t * t * t;
+        return (315.0f * t3 * t3) * P.poly_inv_den;
+    }
+    return 0.0f;
+}
+
+// Scalar part of spiky: 15 (hs - d)^2 / (pi hs^6) / |r|_4, so that grad = s * r (r = pi - pj,
+// normalised over all four lanes as the float4 normalize of the reference does).
+__device__ __forceinline__ float spiky_scale(const DevParams& P, float dist, float r2w) {
+    if (dist > 0.0001f && (P.hs - dist) > 0.0001f) {
+        float a = P.hs - dist;
+        return 15.0f * __fdiv_rn(a * a, P.spiky_den) * rsqrtf(r2w);
+    }
+    return 0.0f;
+}
+
+// Integer power by repeated multiplication (the reference's pow(float, int)).
+__device__ __forceinline__ float powi(float x, int n) {
+    int m = n < 0 ? -n : n;
+    float r = 1.0f;
+    for (int k = 0; k < m; ++k) r *= x;
+    return n < 0 ? 1.0f / r : r;
+}
+
+}  // namespace pbd

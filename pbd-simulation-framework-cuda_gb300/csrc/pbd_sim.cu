@@ -1,0 +1,660 @@
+// pbd_sim.cu -- the simulation handle, the frame schedule, CUDA-graph replay and the C ABI.
+//
+// Host-side counterpart of the reference's Fluid (src/app/simulation/Fluid.{h,cu}) and of
+// the kernel module's host globals (kernel/Globals.h:15-37, kernel/Initialize.h):
+//  - every device buffer is allocated once in pbd_create (one arena) -- the frame never
+//    allocates, unlike the per-frame parameter upload of Initialize.h:71;
+//  - a frame is recorded once into a CUDA graph and replayed per pbd_step call; the graph is
+//    re-recorded only when N or the parameters change;
+//  - double-buffered arrays are addressed through a small "which buffer is current" record
+//    (Cur).  A frame flips some of them; when the flips do not cancel, two graphs are kept,
+//    one per starting parity, and replayed alternately.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pbd_internal.h"
+#include "pbd_kernels.cuh"
+
+namespace pbd {
+thread_local std::string g_last_error;
+void set_error(const std::string& m) { g_last_error = m; }
+void clear_error() { g_last_error.clear(); }
+}  // namespace pbd
+
+using namespace pbd;
+
+namespace {
+
+struct Cur {
+    int x = 0, p = 0, v = 0;   // current buffer of positions (also colours, ids), predictions, velocities
+    bool operator==(const Cur& o) const { return x == o.x && p == o.p && v == o.v; }
+    bool operator!=(const Cur& o) const { return !(*this == o); }
+};
+
+constexpr int kThreadsParticle = 256;
+constexpr int kThreadsNeighbour = 128;
+
+inline uint32_t div_up(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+}  // namespace
+
+struct pbd_sim {
+    pbd_params prm{};
+    uint32_t cap = 0, N = 0;
+    int device = 0, num_sms = 0;
+    void* arena = nullptr;
+    float4 *x[2]{}, *p[2]{}, *v[2]{}, *col[2]{};
+    uint32_t* ids[2]{};
+    float4 *fext = nullptr, *omega = nullptr, *delta = nullptr;
+    float* lambda = nullptr;
+    uint32_t *keys[2]{}, *vals[2]{};
+    uint32_t *cell_start = nullptr, *cell_end = nullptr;
+    uint32_t *hist = nullptr, *status = nullptr, *tile_counter = nullptr, *err = nullptr, *table_n = nullptr;
+    uint32_t max_tiles = 0;
+    Cur cur;
+    int table_passes = -1;        // passes of the sort whose keys the cell tables hold (-1: none)
+    uint32_t table_hint = 0;      // host upper bound of the device word table_n
+    cudaStream_t last_stream = nullptr;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t exec[2]{};
+    Cur exec_start[2];
+    int nexec = 0;
+    Cur flips;
+    uint32_t graph_n = 0xFFFFFFFFu;
+    bool dirty = true;
+    uint32_t launches = 0;
+};
+
+namespace {
+
+int cuda_fail(const char* what, cudaError_t e) {
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return PBD_ERR_CUDA;
+}
+#define CK(call)                                         \
+    do {                                                 \
+        cudaError_t _e = (call);                         \
+        if (_e != cudaSuccess) return cuda_fail(#call, _e); \
+    } while (0)
+
+int sort_passes(const pbd_params& p) {
+    // With applyForces on, every key comes from a position clamped inside the enclosure, whose
+    // limits are at most 126.5 (Communication.h:573-598): keys < 2^21, three 8-bit digits.
+    return (p.active & PBD_ACTIVE_APPLY_FORCES) ? 3 : 4;
+}
+
+float powi_host(float x, int n) {
+    float r = 1.0f;
+    for (int k = 0; k < n; ++k) r *= x;
+    return r;
+}
+
+DevParams make_dev_params(const pbd_sim* s) {
+    const pbd_params& p = s->prm;
+    DevParams P{};
+    P.N = s->N;
+    P.G = p.max_grid;
+    P.M = p.max_neighbours_per_particle;
+    P.K = p.kernel_width_neighbours;
+    P.active = p.active;
+    P.flags = p.flags;
+    P.n_scorr = p.n_scorr;
+    P.d = 2.0f * p.particle_radius;                       // Initialize.h:43
+    P.dt = p.delta_t;
+    P.gravity = p.gravity;
+    P.rho0 = p.rest_density;
+    P.hs = P.d * p.kernel_width_spiky;                    // Initialize.h:45
+    P.hp = p.kernel_width_poly;                           // Initialize.h:53
+    P.hp2 = P.hp * P.hp;
+    P.k_scorr = p.k_scorr;
+    P.c_visc = p.c_viscosity;
+    P.e_vort = p.e_vorticity;
+    P.stiffness = p.stiffness;
+    P.one_minus_stiffness = 1.0f - p.stiffness;
+    P.pos_damp = p.enclosure_position_damping;
+    P.vel_damp = p.enclosure_velocity_damping;
+    P.lambda_eps = p.lambda_epsilon;
+    for (int a = 0; a < 3; ++a) { P.bmin[a] = p.bounds_min[a]; P.bmax[a] = p.bounds_max[a]; }
+    const double kPi = 3.14159265359;                     // Globals.h:122
+    P.poly_inv_den = (float)(1.0 / ((double)0.001f + 64.0 * kPi * (double)powi_host(P.hp, 9)));
+    P.spiky_den = (float)(kPi * (double)powi_host(P.hs, 6));
+    // s_corr reference value: poly6 at distance |q|, q = spiky width x qSCorr (Initialize.h:49)
+    const float q = P.hs * p.q_scorr;
+    const float qd = std::sqrt(q * q + 0.0f + 0.0f);
+    float wq = 0.0f;
+    if (qd > 0.001f && qd < P.hp - 0.001f) {
+        float t = P.hp2 - qd * qd;
+        float t3 = t * t * t;
+        wq = (315.0f * t3 * t3) * P.poly_inv_den;
+    }
+    P.wq = wq;
+    P.far_pairs_zero = (wq > 0.0f && std::isfinite(wq) && p.n_scorr >= 0) ? 1u : 0u;
+    const float c = std::max(P.hp, std::max(P.hs, P.d));
+    P.cut2 = c * c * 1.0001f;
+    return P;
+}
+
+// Optional per-launch timing: a pair of events around every kernel of a frame.
+struct Profiler {
+    struct Rec { const char* name; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    cudaStream_t st = nullptr;
+    const char* pending = nullptr;
+    void begin(const char* name) {
+        Rec r{name, nullptr, nullptr};
+        cudaEventCreate(&r.a);
+        cudaEventCreate(&r.b);
+        cudaEventRecord(r.a, st);
+        recs.push_back(r);
+    }
+    void end() { cudaEventRecord(recs.back().b, st); }
+    ~Profiler() {
+        for (auto& r : recs) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+    }
+};
+#define PROF_BEGIN(name) do { if (prof) prof->begin(name); } while (0)
+#define PROF_END() do { if (prof) prof->end(); } while (0)
+
+// Record (or run) one frame of Fluid::compute (Fluid.cu:14-97) on `st`.
+cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only, uint32_t& nl,
+                          Profiler* prof = nullptr) {
+    const DevParams P = make_dev_params(s);
+    const pbd_params& prm = s->prm;
+    const uint32_t N = s->N;
+    const int np = sort_passes(prm);
+    const uint32_t G = prm.max_grid;
+    SortScratch S{s->hist, s->status, s->tile_counter, s->err, s->max_tiles};
+    nl = 0;
+
+    // applyForces + initializeCellIds (+ histograms, + clearing last frame's cells)
+    const uint32_t total = std::max(N, s->table_hint);
+    const uint32_t gpred = std::max(1u, std::min(div_up(total, kThreadsParticle), (uint32_t)s->num_sms * 8u));
+    PROF_BEGIN("predict_key");
+    predict_key_kernel<<<gpred, kThreadsParticle, 0, st>>>(P, s->x[cur.x], s->v[cur.v], s->p[cur.p], s->fext,
+                                                           s->keys[0], s->keys[np % 2], s->table_n, s->cell_start,
+                                                           s->hist, np, s->err);
+    PROF_END();
+    ++nl;
+    // sortIds
+    const uint32_t ntiles = div_up(N, kSortTile);
+    for (int pass = 0; pass < np; ++pass) {
+        const int in = pass % 2, out = (pass + 1) % 2;
+        PROF_BEGIN("onesweep_pass");
+        if (pass == 0)
+            onesweep_pass<true><<<ntiles, kSortThreads, 0, st>>>(s->keys[in], s->vals[in], s->keys[out], s->vals[out], N, pass, S);
+        else
+            onesweep_pass<false><<<ntiles, kSortThreads, 0, st>>>(s->keys[in], s->vals[in], s->keys[out], s->vals[out], N, pass, S);
+        PROF_END();
+        ++nl;
+    }
+    // copy + reorder + computeCellInfo
+    const int fin = np % 2;
+    const bool cols = (prm.flags & PBD_FLAG_COLORS) != 0, ids = (prm.flags & PBD_FLAG_TRACK_IDS) != 0;
+    ReorderArgs A{s->keys[fin], s->vals[fin], s->x[cur.x], s->p[cur.p], s->v[cur.v], s->col[cur.x],
+                  s->x[cur.x ^ 1], s->p[cur.p ^ 1], s->v[cur.v ^ 1], cols ? s->col[cur.x ^ 1] : nullptr,
+                  s->ids[cur.x], ids ? s->ids[cur.x ^ 1] : nullptr, s->cell_start, s->cell_end, s->table_n};
+    const uint32_t greo = std::max(div_up(N, kThreadsParticle), div_up((uint64_t)ntiles * kRadix, kThreadsParticle));
+    PROF_BEGIN("reorder_cells");
+    reorder_cells_kernel<<<std::max(1u, greo), kThreadsParticle, 0, st>>>(P, A, S, np, ntiles);
+    PROF_END();
+    ++nl;
+    cur.x ^= 1; cur.p ^= 1; cur.v ^= 1;
+    if (front_only) return cudaGetLastError();
+
+    const uint32_t gn = div_up(N, kThreadsNeighbour);
+    const uint32_t act = prm.active;
+    const uint32_t I = prm.solver_iterations, Sx = prm.stabilization_iterations;
+    const bool do_delta = act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS, do_apply = act & PBD_ACTIVE_APPLY_DELTA_POSITIONS;
+    const bool do_update = act & PBD_ACTIVE_UPDATE_POSITIONS;
+    const bool collide = prm.collision_type == 0;
+    bool last_was_delta = false;
+    for (uint32_t it = 0; it < I; ++it) {
+        if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
+            PROF_BEGIN("lambda");
+            lambda_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->cell_start, s->cell_end, s->lambda);
+            PROF_END();
+            ++nl;
+            last_was_delta = false;
+        }
+        // passes of this iteration: pass 0 carries computeDeltaPositions and the first
+        // solveCollisions; pass k carries solveCollisions k; applyDeltaPositions rides on the
+        // last pass.
+        const uint32_t ncoll = collide ? Sx : 0u;
+        const uint32_t npass = std::max(1u, ncoll);
+        for (uint32_t k = 0; k < npass; ++k) {
+            uint32_t mode = 0;
+            if (k == 0 && do_delta) mode |= kDoDelta;
+            if (k < ncoll) mode |= kDoCollide;
+            const bool last = (k + 1 == npass);
+            if (last && do_apply) {
+                mode |= kDoApply;
+                if (!(mode & kDoDelta)) mode |= kLoadDelta;
+            }
+            if ((mode & kDoDelta) && (!last || !do_apply)) mode |= kStoreDelta;
+            if (mode == 0) continue;
+            const bool final_pass = last && (it + 1 == I);
+            if (final_pass && do_update) mode |= kDoUpdate;
+            PROF_BEGIN("delta");
+            delta_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, mode, s->p[cur.p], s->p[cur.p ^ 1], s->x[cur.x],
+                                                            s->v[cur.v], s->lambda, s->delta, s->cell_start, s->cell_end);
+            PROF_END();
+            ++nl;
+            cur.p ^= 1;
+            last_was_delta = (mode & kDoUpdate) != 0;
+        }
+    }
+    if (do_update && !last_was_delta) {
+        PROF_BEGIN("update");
+        update_kernel<<<div_up(N, kThreadsParticle), kThreadsParticle, 0, st>>>(P, s->p[cur.p], s->x[cur.x], s->v[cur.v]);
+        PROF_END();
+        ++nl;
+    }
+    if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
+        PROF_BEGIN("omega");
+        omega_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->cell_start, s->cell_end, s->omega);
+        PROF_END();
+        ++nl;
+    }
+    const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
+    if (vort || visc) {
+        PROF_BEGIN("vort_visc");
+        vort_visc_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->v[cur.v ^ 1], s->omega,
+                                                            s->fext, s->cell_start, s->cell_end, vort, visc);
+        PROF_END();
+        ++nl;
+        if (visc) cur.v ^= 1;
+    }
+    (void)G;
+    return cudaGetLastError();
+}
+
+void destroy_graphs(pbd_sim* s) {
+    for (int k = 0; k < 2; ++k)
+        if (s->exec[k]) { cudaGraphExecDestroy(s->exec[k]); s->exec[k] = nullptr; }
+    s->nexec = 0;
+}
+
+int capture_one(pbd_sim* s, Cur& c, cudaGraphExec_t* out, uint32_t& nl) {
+    CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = enqueue_frame(s, s->cap_stream, c, false, nl);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(s->cap_stream, &g);
+    if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail("frame capture", e); }
+    if (e2 != cudaSuccess) return cuda_fail("cudaStreamEndCapture", e2);
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail("cudaGraphInstantiate", e);
+    return PBD_OK;
+}
+
+// The sort's final buffer depends on the pass count; if it moved, clear the old cells now.
+int settle_tables(pbd_sim* s, cudaStream_t st) {
+    const int np = sort_passes(s->prm);
+    if (s->table_passes >= 0 && (s->table_passes % 2) != (np % 2)) {
+        clear_cells_kernel<<<std::max(1u, std::min(div_up(s->table_hint, 256), (uint32_t)s->num_sms * 8u)), 256, 0, st>>>(
+            s->keys[s->table_passes % 2], s->table_n, s->cell_start, s->prm.max_grid);
+        CK(cudaGetLastError());
+        CK(cudaMemsetAsync(s->table_n, 0, sizeof(uint32_t), st));
+        s->table_hint = 0;
+    }
+    s->table_passes = np;
+    return PBD_OK;
+}
+
+int build_graphs(pbd_sim* s) {
+    destroy_graphs(s);
+    Cur c0 = s->cur, c = c0;
+    uint32_t nl = 0;
+    int rc = capture_one(s, c, &s->exec[0], nl);
+    if (rc) return rc;
+    s->exec_start[0] = c0;
+    s->nexec = 1;
+    s->flips.x = c.x ^ c0.x; s->flips.p = c.p ^ c0.p; s->flips.v = c.v ^ c0.v;
+    if (c != c0) {
+        Cur c1 = c;
+        uint32_t nl1 = 0;
+        rc = capture_one(s, c, &s->exec[1], nl1);
+        if (rc) return rc;
+        s->exec_start[1] = c1;
+        s->nexec = 2;
+        if (c != c0) { set_error("internal: frame buffer flips do not return to the start"); return PBD_ERR_CUDA; }
+    }
+    s->launches = nl;
+    s->graph_n = s->N;
+    s->dirty = false;
+    return PBD_OK;
+}
+
+int check_sim(const pbd_sim* s, const char* fn) {
+    if (!s) { set_error(std::string(fn) + ": null handle"); return PBD_ERR_INVALID_ARG; }
+    return PBD_OK;
+}
+
+int sync_last(pbd_sim* s) {
+    CK(cudaStreamSynchronize(s->last_stream));
+    return PBD_OK;
+}
+
+}  // namespace
+
+// ======================================================================================
+// C ABI
+// ======================================================================================
+extern "C" {
+
+const char* pbd_last_error(void) { return g_last_error.c_str(); }
+uint32_t pbd_abi_version(void) { return PBD_ABI_VERSION; }
+
+int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
+    clear_error();
+    if (!prm || !out) { set_error("pbd_create: null argument"); return PBD_ERR_INVALID_ARG; }
+    *out = nullptr;
+    int rc = pbd_validate_params(prm);
+    if (rc) return rc;
+    if (prm->collision_type != 0) { set_error("collisionType 1 (batched contact claims) is not implemented"); return PBD_ERR_UNSUPPORTED; }
+    if (capacity == 0 || capacity > (1u << 30) - 1u) { set_error("pbd_create: capacity must be in [1, 2^30)"); return PBD_ERR_INVALID_ARG; }
+    pbd_sim* s = new (std::nothrow) pbd_sim();
+    if (!s) { set_error("pbd_create: host allocation"); return PBD_ERR_ALLOC; }
+    s->prm = *prm;
+    s->cap = capacity;
+    cudaError_t e = cudaGetDevice(&s->device);
+    if (e != cudaSuccess) { delete s; return cuda_fail("cudaGetDevice", e); }
+    e = cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device);
+    if (e != cudaSuccess) { delete s; return cuda_fail("cudaDeviceGetAttribute", e); }
+    s->max_tiles = div_up(capacity, kSortTile);
+    // ---- one arena, 256-byte aligned slices
+    const size_t C = capacity, G = prm->max_grid;
+    std::vector<std::pair<void**, size_t>> parts;
+    for (int b = 0; b < 2; ++b) {
+        parts.push_back({(void**)&s->x[b], C * 16}); parts.push_back({(void**)&s->p[b], C * 16});
+        parts.push_back({(void**)&s->v[b], C * 16}); parts.push_back({(void**)&s->col[b], C * 16});
+        parts.push_back({(void**)&s->ids[b], C * 4});
+        parts.push_back({(void**)&s->keys[b], C * 4}); parts.push_back({(void**)&s->vals[b], C * 4});
+    }
+    parts.push_back({(void**)&s->fext, C * 16}); parts.push_back({(void**)&s->omega, C * 16});
+    parts.push_back({(void**)&s->delta, C * 16}); parts.push_back({(void**)&s->lambda, C * 4});
+    parts.push_back({(void**)&s->cell_start, G * 4}); parts.push_back({(void**)&s->cell_end, G * 4});
+    parts.push_back({(void**)&s->hist, (size_t)kMaxPasses * kRadix * 4});
+    parts.push_back({(void**)&s->status, (size_t)kMaxPasses * s->max_tiles * kRadix * 4});
+    parts.push_back({(void**)&s->tile_counter, kMaxPasses * 4}); parts.push_back({(void**)&s->err, 4});
+    parts.push_back({(void**)&s->table_n, 4});
+    size_t total = 0;
+    for (auto& pt : parts) total += (pt.second + 255) & ~size_t(255);
+    e = cudaMalloc(&s->arena, total);
+    if (e != cudaSuccess) { delete s; set_error(std::string("cudaMalloc arena: ") + cudaGetErrorString(e)); return PBD_ERR_ALLOC; }
+    char* cur = static_cast<char*>(s->arena);
+    for (auto& pt : parts) { *pt.first = cur; cur += (pt.second + 255) & ~size_t(255); }
+    e = cudaMemset(s->arena, 0, total);
+    if (e == cudaSuccess) e = cudaMemset(s->cell_start, 0xFF, G * 4);   // all cells empty
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { cudaFree(s->arena); delete s; return cuda_fail("pbd_create init", e); }
+    *out = s;
+    return PBD_OK;
+}
+
+int pbd_destroy(pbd_sim* s) {
+    clear_error();
+    if (!s) return PBD_OK;
+    cudaDeviceSynchronize();
+    destroy_graphs(s);
+    if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+    cudaError_t e = cudaFree(s->arena);
+    delete s;
+    if (e != cudaSuccess) return cuda_fail("cudaFree", e);
+    return PBD_OK;
+}
+
+int pbd_set_params(pbd_sim* s, const pbd_params* prm) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_set_params")) return rc;
+    if (!prm) { set_error("pbd_set_params: null"); return PBD_ERR_INVALID_ARG; }
+    if (int rc = pbd_validate_params(prm)) return rc;
+    if (prm->collision_type != 0) { set_error("collisionType 1 (batched contact claims) is not implemented"); return PBD_ERR_UNSUPPORTED; }
+    if (prm->max_grid != s->prm.max_grid) { set_error("max_grid is fixed at pbd_create"); return PBD_ERR_UNSUPPORTED; }
+    s->prm = *prm;
+    s->dirty = true;
+    return PBD_OK;
+}
+
+int pbd_get_params(const pbd_sim* s, pbd_params* prm) {
+    if (!s || !prm) { set_error("pbd_get_params: null"); return PBD_ERR_INVALID_ARG; }
+    *prm = s->prm;
+    return PBD_OK;
+}
+
+int pbd_num_particles(const pbd_sim* s, uint32_t* n) {
+    if (!s || !n) { set_error("pbd_num_particles: null"); return PBD_ERR_INVALID_ARG; }
+    *n = s->N;
+    return PBD_OK;
+}
+
+int pbd_capacity(const pbd_sim* s, uint32_t* c) {
+    if (!s || !c) { set_error("pbd_capacity: null"); return PBD_ERR_INVALID_ARG; }
+    *c = s->cap;
+    return PBD_OK;
+}
+
+static int add_common(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4,
+                      cudaMemcpyKind kind, cudaStream_t st, bool sync) {
+    if (int rc = check_sim(s, "pbd_add_particles")) return rc;
+    if (n == 0) return PBD_OK;
+    if (!pos4 || !vel4) { set_error("pbd_add_particles: null position or velocity array"); return PBD_ERR_INVALID_ARG; }
+    if ((uint64_t)s->N + n > s->cap) {
+        set_error("pbd_add_particles: " + std::to_string(s->N) + " + " + std::to_string(n) + " exceeds capacity " + std::to_string(s->cap));
+        return PBD_ERR_CAPACITY;
+    }
+    const size_t off = s->N, bytes = (size_t)n * 16;
+    CK(cudaMemcpyAsync(s->x[s->cur.x] + off, pos4, bytes, kind, st));
+    CK(cudaMemcpyAsync(s->v[s->cur.v] + off, vel4, bytes, kind, st));
+    if (col4) CK(cudaMemcpyAsync(s->col[s->cur.x] + off, col4, bytes, kind, st));
+    fill_ids_kernel<<<div_up(n, 256), 256, 0, st>>>(s->ids[s->cur.x], s->N, n);
+    CK(cudaGetLastError());
+    if (sync) CK(cudaStreamSynchronize(st));
+    s->N += n;
+    s->last_stream = st;
+    return PBD_OK;
+}
+
+int pbd_add_particles(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_add_particles")) return rc;
+    return add_common(s, n, pos4, vel4, col4, cudaMemcpyHostToDevice, s->last_stream, true);
+}
+
+int pbd_add_particles_device(pbd_sim* s, uint32_t n, const float* d_pos4, const float* d_vel4, const float* d_col4, void* stream) {
+    clear_error();
+    return add_common(s, n, d_pos4, d_vel4, d_col4, cudaMemcpyDeviceToDevice, (cudaStream_t)stream, false);
+}
+
+int pbd_add_particle(pbd_sim* s, const float pos[3], const float dir[3]) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_add_particle")) return rc;
+    if (!pos || !dir) { set_error("pbd_add_particle: null"); return PBD_ERR_INVALID_ARG; }
+    if ((uint64_t)s->N + 1 > s->cap) { set_error("pbd_add_particle: capacity reached"); return PBD_ERR_CAPACITY; }
+    add_one_kernel<<<1, 1, 0, s->last_stream>>>(s->x[s->cur.x], s->v[s->cur.v], s->col[s->cur.x], s->ids[s->cur.x], s->N,
+                                                 pos[0], pos[1], pos[2], dir[0], dir[1], dir[2]);
+    CK(cudaGetLastError());
+    s->N += 1;
+    return PBD_OK;
+}
+
+int pbd_clear(pbd_sim* s) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_clear")) return rc;
+    s->N = 0;   // Communication.h:657-660
+    return PBD_OK;
+}
+
+int pbd_step(pbd_sim* s, int nsteps, void* stream) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_step")) return rc;
+    if (nsteps < 0) { set_error("pbd_step: nsteps < 0"); return PBD_ERR_INVALID_ARG; }
+    if (s->N == 0 || nsteps == 0) return PBD_OK;   // Fluid.cu:19
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->dirty || s->graph_n != s->N || s->table_passes != sort_passes(s->prm)) {
+        if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
+        if (int rc = settle_tables(s, st)) return rc;
+        if (int rc = build_graphs(s)) return rc;
+    }
+    for (int k = 0; k < nsteps; ++k) {
+        const int g = (s->nexec == 2 && s->cur == s->exec_start[1]) ? 1 : 0;
+        CK(cudaGraphLaunch(s->exec[g], st));
+        s->cur.x ^= s->flips.x; s->cur.p ^= s->flips.p; s->cur.v ^= s->flips.v;
+    }
+    s->table_hint = s->N;
+    s->last_stream = st;
+    return PBD_OK;
+}
+
+int pbd_sync(pbd_sim* s) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_sync")) return rc;
+    if (int rc = sync_last(s)) return rc;
+    uint32_t err = 0;
+    CK(cudaMemcpy(&err, s->err, 4, cudaMemcpyDeviceToHost));
+    if (err) {
+        CK(cudaMemset(s->err, 0, 4));
+        if (err & kErrSortTimeout) { set_error("radix sort: a bounded look-back wait gave up"); return PBD_ERR_TIMEOUT; }
+        set_error("Morton keys exceed the sorted bit range");
+        return PBD_ERR_RANGE;
+    }
+    return PBD_OK;
+}
+
+int pbd_get_state(pbd_sim* s, float* pos4, float* vel4, float* pred4, uint32_t* ids) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_get_state")) return rc;
+    if (int rc = sync_last(s)) return rc;
+    const size_t b = (size_t)s->N * 16;
+    if (pos4) CK(cudaMemcpy(pos4, s->x[s->cur.x], b, cudaMemcpyDeviceToHost));
+    if (vel4) CK(cudaMemcpy(vel4, s->v[s->cur.v], b, cudaMemcpyDeviceToHost));
+    if (pred4) CK(cudaMemcpy(pred4, s->p[s->cur.p], b, cudaMemcpyDeviceToHost));
+    if (ids) CK(cudaMemcpy(ids, s->ids[s->cur.x], (size_t)s->N * 4, cudaMemcpyDeviceToHost));
+    return PBD_OK;
+}
+
+int pbd_get_device_state(pbd_sim* s, const float** d_pos4, const float** d_vel4, const float** d_pred4) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_get_device_state")) return rc;
+    if (d_pos4) *d_pos4 = reinterpret_cast<const float*>(s->x[s->cur.x]);
+    if (d_vel4) *d_vel4 = reinterpret_cast<const float*>(s->v[s->cur.v]);
+    if (d_pred4) *d_pred4 = reinterpret_cast<const float*>(s->p[s->cur.p]);
+    return PBD_OK;
+}
+
+int pbd_debug_dump(pbd_sim* s, uint32_t* keys, uint32_t* perm, uint32_t* cell_start, uint32_t* cell_end,
+                   uint32_t ncells, float* lambda, float* fext4, float* omega4) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_debug_dump")) return rc;
+    if (int rc = sync_last(s)) return rc;
+    const int fin = (s->table_passes >= 0 ? s->table_passes : sort_passes(s->prm)) % 2;
+    const size_t n = s->N;
+    if (keys) CK(cudaMemcpy(keys, s->keys[fin], n * 4, cudaMemcpyDeviceToHost));
+    if (perm) CK(cudaMemcpy(perm, s->vals[fin], n * 4, cudaMemcpyDeviceToHost));
+    if (ncells > s->prm.max_grid) ncells = s->prm.max_grid;
+    if (cell_start) CK(cudaMemcpy(cell_start, s->cell_start, (size_t)ncells * 4, cudaMemcpyDeviceToHost));
+    if (cell_end) CK(cudaMemcpy(cell_end, s->cell_end, (size_t)ncells * 4, cudaMemcpyDeviceToHost));
+    if (lambda) CK(cudaMemcpy(lambda, s->lambda, n * 4, cudaMemcpyDeviceToHost));
+    if (fext4) CK(cudaMemcpy(fext4, s->fext, n * 16, cudaMemcpyDeviceToHost));
+    if (omega4) CK(cudaMemcpy(omega4, s->omega, n * 16, cudaMemcpyDeviceToHost));
+    return PBD_OK;
+}
+
+int pbd_debug_neighbours(pbd_sim* s, uint32_t max_entries, uint32_t* list, uint32_t* count, uint32_t* contacts) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_debug_neighbours")) return rc;
+    if (int rc = sync_last(s)) return rc;
+    const size_t n = s->N;
+    if (n == 0) return PBD_OK;
+    uint32_t *dl = nullptr, *dc = nullptr, *dk = nullptr;
+    const size_t lb = std::max<size_t>(1, n * (size_t)max_entries) * 4;
+    CK(cudaMalloc(&dl, lb));
+    CK(cudaMalloc(&dc, n * 4));
+    CK(cudaMalloc(&dk, n * 4));
+    const DevParams P = make_dev_params(s);
+    const bool cols = (s->prm.flags & PBD_FLAG_COLORS) && (s->prm.active & PBD_ACTIVE_FIND_NEIGHBOURS);
+    list_kernel<<<div_up(n, 128), 128, 0, s->last_stream>>>(P, s->p[s->cur.p], s->cell_start, s->cell_end, max_entries,
+                                                            dl, dc, dk, cols ? s->col[s->cur.x] : nullptr);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->last_stream);
+    if (e == cudaSuccess && list) e = cudaMemcpy(list, dl, n * (size_t)max_entries * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && count) e = cudaMemcpy(count, dc, n * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && contacts) e = cudaMemcpy(contacts, dk, n * 4, cudaMemcpyDeviceToHost);
+    cudaFree(dl); cudaFree(dc); cudaFree(dk);
+    if (e != cudaSuccess) return cuda_fail("pbd_debug_neighbours", e);
+    return PBD_OK;
+}
+
+int pbd_debug_front(pbd_sim* s, void* stream) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_debug_front")) return rc;
+    if (s->N == 0) return PBD_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
+    if (int rc = settle_tables(s, st)) return rc;
+    uint32_t nl = 0;
+    cudaError_t e = enqueue_frame(s, st, s->cur, true, nl);
+    if (e != cudaSuccess) return cuda_fail("pbd_debug_front", e);
+    CK(cudaStreamSynchronize(st));
+    s->table_hint = s->N;
+    s->last_stream = st;
+    return PBD_OK;
+}
+
+int pbd_profile_frames(pbd_sim* s, int nsteps, void* stream, pbd_kernel_stat* stats, uint32_t max_stats,
+                       uint32_t* n_stats) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_profile_frames")) return rc;
+    if (!stats || !n_stats || nsteps < 0) { set_error("pbd_profile_frames: bad argument"); return PBD_ERR_INVALID_ARG; }
+    *n_stats = 0;
+    if (s->N == 0 || nsteps == 0) return PBD_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
+    if (int rc = settle_tables(s, st)) return rc;
+    Profiler prof;
+    prof.st = st;
+    for (int k = 0; k < nsteps; ++k) {
+        uint32_t nl = 0;
+        cudaError_t e = enqueue_frame(s, st, s->cur, false, nl, &prof);
+        if (e != cudaSuccess) return cuda_fail("pbd_profile_frames", e);
+        s->table_hint = s->N;
+    }
+    s->last_stream = st;
+    CK(cudaStreamSynchronize(st));
+    uint32_t n = 0;
+    for (auto& r : prof.recs) {
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, r.a, r.b));
+        uint32_t k = 0;
+        while (k < n && std::strncmp(stats[k].name, r.name, sizeof(stats[k].name)) != 0) ++k;
+        if (k == n) {
+            if (n == max_stats) continue;
+            std::memset(&stats[n], 0, sizeof(stats[n]));
+            std::strncpy(stats[n].name, r.name, sizeof(stats[n].name) - 1);
+            ++n;
+        }
+        stats[k].launches += 1;
+        stats[k].total_ms += ms;
+    }
+    *n_stats = n;
+    return PBD_OK;
+}
+
+int pbd_launches_per_step(pbd_sim* s, uint32_t* n) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_launches_per_step")) return rc;
+    if (!n) { set_error("pbd_launches_per_step: null"); return PBD_ERR_INVALID_ARG; }
+    if (s->dirty || s->graph_n != s->N) {
+        if (s->N == 0) { *n = 0; return PBD_OK; }
+        if (int rc = build_graphs(s)) return rc;
+    }
+    *n = s->launches;
+    return PBD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,241 @@
+"""ctypes binding of libpbd.so (include/pbd.h) for Python callers, tests and bench.py.
+
+The product is the C ABI; this module only marshals arrays.  It fails loudly when the
+library is missing: there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpbd.so")
+
+# status codes (include/pbd.h)
+OK, ERR_INVALID_ARG, ERR_CAPACITY, ERR_CUDA, ERR_CONFIG, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_ALLOC, ERR_RANGE = range(9)
+
+ACTIVE = {
+    "applyForces": 1 << 0, "findContacts": 1 << 1, "findNeighbours": 1 << 2, "computeLambda": 1 << 3,
+    "computeDeltaPositions": 1 << 4, "applyDeltaPositions": 1 << 5, "updatePositions": 1 << 6,
+    "computeOmegas": 1 << 7, "computeVorticity": 1 << 8, "computeViscosity": 1 << 9,
+}
+ACTIVE_ALL = 0x3FF
+FLAG_CELL_END_QUIRK, FLAG_TRACK_IDS, FLAG_COLORS = 1, 2, 4
+
+EXPORTED = [
+    "pbd_params_default", "pbd_load_config", "pbd_parse_config", "pbd_write_config", "pbd_validate_params",
+    "pbd_create", "pbd_destroy", "pbd_set_params", "pbd_get_params", "pbd_num_particles", "pbd_capacity",
+    "pbd_add_particles", "pbd_add_particles_device", "pbd_add_particle", "pbd_clear", "pbd_step", "pbd_sync",
+    "pbd_get_state", "pbd_get_device_state", "pbd_debug_dump", "pbd_debug_neighbours", "pbd_debug_front",
+    "pbd_launches_per_step", "pbd_profile_frames", "pbd_last_error", "pbd_abi_version",
+]
+
+
+class Params(C.Structure):
+    """pbd_params (include/pbd.h); mirrors SimulationParameters, kernel/Globals.h:50-75."""
+    _fields_ = [
+        ("struct_size", C.c_uint32), ("threads_per_block", C.c_uint32), ("particle_radius", C.c_float),
+        ("max_neighbours_per_particle", C.c_uint32), ("delta_t", C.c_float), ("gravity", C.c_float),
+        ("rest_density", C.c_float), ("kernel_width_spiky", C.c_float), ("k_scorr", C.c_float),
+        ("n_scorr", C.c_int32), ("q_scorr", C.c_float), ("c_viscosity", C.c_float),
+        ("kernel_width_poly", C.c_float), ("e_vorticity", C.c_float), ("collision_type", C.c_uint32),
+        ("kernel_width_neighbours", C.c_uint32), ("max_collision_batches", C.c_uint32), ("stiffness", C.c_float),
+        ("enclosure_position_damping", C.c_float), ("enclosure_velocity_damping", C.c_float),
+        ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3), ("solver_iterations", C.c_uint32),
+        ("stabilization_iterations", C.c_uint32), ("active", C.c_uint32), ("max_grid", C.c_uint32),
+        ("lambda_epsilon", C.c_float), ("flags", C.c_uint32),
+    ]
+
+    def copy(self):
+        p = Params()
+        C.memmove(C.byref(p), C.byref(self), C.sizeof(Params))
+        return p
+
+    def as_dict(self):
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if not isinstance(v, (int, float)) else v
+        return d
+
+
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint32), ("total_ms", C.c_float)]
+
+
+class PBDError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"pbd error {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib():
+    """Load libpbd.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise FileNotFoundError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        L = C.CDLL(LIB_PATH)
+        vp, u32, i32 = C.c_void_p, C.c_uint32, C.c_int
+        fp, u32p = C.POINTER(C.c_float), C.POINTER(C.c_uint32)
+        P = C.POINTER(Params)
+        sig = {
+            "pbd_params_default": [P], "pbd_load_config": [P, C.c_char_p], "pbd_parse_config": [P, C.c_char_p, C.c_char_p],
+            "pbd_write_config": [P, C.c_char_p], "pbd_validate_params": [P],
+            "pbd_create": [P, u32, C.POINTER(vp)], "pbd_destroy": [vp], "pbd_set_params": [vp, P],
+            "pbd_get_params": [vp, P], "pbd_num_particles": [vp, u32p], "pbd_capacity": [vp, u32p],
+            "pbd_add_particles": [vp, u32, fp, fp, fp], "pbd_add_particles_device": [vp, u32, vp, vp, vp, vp],
+            "pbd_add_particle": [vp, fp, fp], "pbd_clear": [vp], "pbd_step": [vp, i32, vp], "pbd_sync": [vp],
+            "pbd_get_state": [vp, fp, fp, fp, u32p], "pbd_get_device_state": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)],
+            "pbd_debug_dump": [vp, u32p, u32p, u32p, u32p, u32, fp, fp, fp],
+            "pbd_debug_neighbours": [vp, u32, u32p, u32p, u32p], "pbd_debug_front": [vp, vp],
+            "pbd_launches_per_step": [vp, u32p],
+            "pbd_profile_frames": [vp, i32, vp, C.POINTER(KernelStat), u32, u32p],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = i32
+        L.pbd_last_error.restype = C.c_char_p
+        L.pbd_last_error.argtypes = []
+        L.pbd_abi_version.restype = u32
+        L.pbd_abi_version.argtypes = []
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != OK:
+        raise PBDError(rc, lib().pbd_last_error().decode(errors="replace"))
+    return rc
+
+
+def default_params():
+    p = Params()
+    check(lib().pbd_params_default(C.byref(p)))
+    return p
+
+
+def load_config(path, params=None):
+    p = default_params() if params is None else params.copy()
+    check(lib().pbd_load_config(C.byref(p), os.fsencode(path)))
+    return p
+
+
+def parse_config(text, params=None, base_dir=None):
+    p = default_params() if params is None else params.copy()
+    check(lib().pbd_parse_config(C.byref(p), text.encode(), None if base_dir is None else os.fsencode(base_dir)))
+    return p
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _up(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_uint32))
+
+
+class Sim:
+    """One pbd_sim handle (the reference's Fluid object plus its injection callbacks)."""
+
+    def __init__(self, params, capacity):
+        self.L = lib()
+        self.h = C.c_void_p()
+        check(self.L.pbd_create(C.byref(params), capacity, C.byref(self.h)))
+        self.capacity = capacity
+
+    def close(self):
+        if self.h:
+            self.L.pbd_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def n(self):
+        v = C.c_uint32()
+        check(self.L.pbd_num_particles(self.h, C.byref(v)))
+        return v.value
+
+    def params(self):
+        p = Params()
+        check(self.L.pbd_get_params(self.h, C.byref(p)))
+        return p
+
+    def set_params(self, p):
+        check(self.L.pbd_set_params(self.h, C.byref(p)))
+
+    def add_particles(self, pos4, vel4, col4=None):
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
+        col4 = None if col4 is None else np.ascontiguousarray(col4, dtype=np.float32)
+        check(self.L.pbd_add_particles(self.h, pos4.shape[0], _fp(pos4), _fp(vel4), _fp(col4)))
+
+    def add_particle(self, pos, direction):
+        p = np.ascontiguousarray(pos, dtype=np.float32)
+        d = np.ascontiguousarray(direction, dtype=np.float32)
+        check(self.L.pbd_add_particle(self.h, _fp(p), _fp(d)))
+
+    def clear(self):
+        check(self.L.pbd_clear(self.h))
+
+    def step(self, nsteps=1, stream=0):
+        check(self.L.pbd_step(self.h, nsteps, C.c_void_p(stream)))
+
+    def sync(self):
+        check(self.L.pbd_sync(self.h))
+
+    def state(self):
+        n = self.n
+        x = np.zeros((n, 4), np.float32); v = np.zeros((n, 4), np.float32)
+        p = np.zeros((n, 4), np.float32); ids = np.zeros(n, np.uint32)
+        check(self.L.pbd_get_state(self.h, _fp(x), _fp(v), _fp(p), _up(ids)))
+        return {"x": x, "v": v, "p": p, "ids": ids}
+
+    def debug(self, ncells=0):
+        n = self.n
+        keys = np.zeros(n, np.uint32); perm = np.zeros(n, np.uint32)
+        cs = np.zeros(ncells, np.uint32); ce = np.zeros(ncells, np.uint32)
+        lam = np.zeros(n, np.float32); fext = np.zeros((n, 4), np.float32); om = np.zeros((n, 4), np.float32)
+        check(self.L.pbd_debug_dump(self.h, _up(keys), _up(perm), _up(cs), _up(ce), ncells, _fp(lam), _fp(fext), _fp(om)))
+        return {"keys": keys, "perm": perm, "cell_start": cs, "cell_end": ce, "lambda": lam, "fext": fext, "omega": om}
+
+    def neighbours(self, max_entries):
+        n = self.n
+        lst = np.zeros((n, max_entries), np.uint32); cnt = np.zeros(n, np.uint32); con = np.zeros(n, np.uint32)
+        check(self.L.pbd_debug_neighbours(self.h, max_entries, _up(lst), _up(cnt), _up(con)))
+        return lst, cnt, con
+
+    def front(self, stream=0):
+        check(self.L.pbd_debug_front(self.h, C.c_void_p(stream)))
+
+    def profile(self, nsteps, stream=0):
+        """{kernel name: (launches, total device ms)} over `nsteps` directly launched frames."""
+        stats = (KernelStat * 32)()
+        n = C.c_uint32()
+        check(self.L.pbd_profile_frames(self.h, nsteps, C.c_void_p(stream), stats, 32, C.byref(n)))
+        return {stats[k].name.decode(): (stats[k].launches, stats[k].total_ms) for k in range(n.value)}
+
+    def device_state(self):
+        x, v, p = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(self.L.pbd_get_device_state(self.h, C.byref(x), C.byref(v), C.byref(p)))
+        return x.value, v.value, p.value
+
+    def launches_per_step(self):
+        v = C.c_uint32()
+        check(self.L.pbd_launches_per_step(self.h, C.byref(v)))
+        return v.value

@@ -1,0 +1,47 @@
+"""Shared helpers for the parity tests (scene set-up on both backends, comparisons)."""
+import numpy as np
+
+
+def workload(pbd, scenes, shape=(8, 8, 8), box=16, seed=1, rho0=1000.0, eps=0.1, vorticity=0.0, viscosity=0.0,
+             iterations=4, flags_extra=0):
+    p = scenes.workload_params(pbd, box, rho0, vorticity=vorticity, viscosity=viscosity, iterations=iterations)
+    p.lambda_epsilon = eps
+    p.flags |= flags_extra
+    pos, vel = scenes.lattice(*shape, seed=seed)
+    return p, pos, vel
+
+
+def by_id(state):
+    order = np.argsort(state["ids"], kind="stable")
+    return {k: (v[order] if hasattr(v, "__len__") and len(v) == len(order) else v) for k, v in state.items()}
+
+
+def maxdiff(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b))) if a.size else 0.0
+
+
+def expand_bits_np(v):
+    v = v.astype(np.uint64)
+    v = (v * np.uint64(0x00010001)) & np.uint64(0xFF0000FF)
+    v = (v * np.uint64(0x00000101)) & np.uint64(0x0F00F00F)
+    v = (v * np.uint64(0x00000011)) & np.uint64(0xC30C30C3)
+    v = (v * np.uint64(0x00000005)) & np.uint64(0x49249249)
+    return v.astype(np.uint32)
+
+
+def morton_np(p):
+    """Hash.h:21-29 on float32 (n, >=3) positions."""
+    c = np.clip(np.asarray(p, np.float32)[:, :3], np.float32(0), np.float32(1023)).astype(np.uint32)
+    with np.errstate(over="ignore"):
+        return (expand_bits_np(c[:, 0]) << np.uint32(2)) + (expand_bits_np(c[:, 1]) << np.uint32(1)) + expand_bits_np(c[:, 2])
+
+
+def setup_pair(pbd, oracle_mod, params, pos, vel, precision="f32", capacity=None):
+    cap = capacity or pos.shape[0]
+    sim = pbd.Sim(params, cap)
+    sim.add_particles(pos, vel)
+    orc = oracle_mod.Oracle(params, cap, precision)
+    orc.add_particles(pos, vel)
+    return sim, orc
