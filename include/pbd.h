@@ -171,9 +171,11 @@ int pbd_debug_dump(pbd_sim* sim, uint32_t* keys, uint32_t* perm, uint32_t* cell_
                    float* omega4);
 /* Materialise the neighbour list the reference would build this frame (findContacts +
  * findNeighbours, kernel/Collision.h:11-160): `list` is N x max_entries uint32, `count`
- * and `contacts` are N uint32.  Entries beyond max_entries are counted but not stored. */
+ * and `contacts` are N uint32.  Entries beyond max_entries are counted but not stored.
+ * `walker` selects the traversal: 0 one thread per particle, 1 one warp per particle (the
+ * path taken by particles whose list meets a very long cell range). */
 int pbd_debug_neighbours(pbd_sim* sim, uint32_t max_entries, uint32_t* list,
-                         uint32_t* count, uint32_t* contacts);
+                         uint32_t* count, uint32_t* contacts, int walker);
 /* Run only the front of a frame: applyForces, initializeCellIds, sortIds, reorder,
  * resetCellInfo/computeCellInfo (Fluid.cu:21-33).  For bit-exact tests of keys,
  * permutation and cell ranges. */

@@ -43,7 +43,10 @@ def build(force=False, verbose=False, extra_nvcc=()):
         o = os.path.join(OBJ, f + ".o")
         objs.append(o)
         if force or _newer(o, deps):
-            cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE,
+            # -prec-div/-prec-sqrt=false: the neighbour passes use the hardware approximations
+            # (as the reference's FastMath build does); bit-exact steps use explicit _rn intrinsics
+            cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-prec-div=false", "-prec-sqrt=false",
+                   "-Xcompiler", "-fPIC,-O2", "-I", INCLUDE,
                    *extra_nvcc, "-c", os.path.join(CSRC, f), "-o", o]
             jobs.append(cmd)
     for f in CPP:

@@ -26,6 +26,7 @@ struct DevParams {
     uint32_t far_pairs_zero;  // 1 when pairs beyond every kernel support contribute exactly 0
     float d;               // particleDiameter = 2 r
     float dt, gravity;
+    float inv_dt;          // 1 / dt: v = (p - x) / dt as a multiply (Update.h:22)
     float rho0;
     float hs, hp;          // spiky width (x diameter already applied), poly width
     float hp2;             // hp*hp
@@ -38,6 +39,8 @@ struct DevParams {
     float poly_inv_den;    // 1 / (0.001 + 64 pi hp^9)   (Density.h:21, double there)
     float spiky_den;       // pi * hs^6                  (Density.h:37)
     float wq;              // poly6(q), the s_corr reference value (Density.h:138)
+    float inv_wq;          // 1 / wq
+    float inv_spiky_den;   // 1 / spiky_den
     float cut2;            // max(hp, hs, d)^2: beyond it no kernel and no contact is non-zero
 };
 
@@ -76,7 +79,7 @@ __device__ __forceinline__ float poly6(const DevParams& P, float dist) {
 __device__ __forceinline__ float spiky_scale(const DevParams& P, float dist, float r2w) {
     if (dist > 0.0001f && (P.hs - dist) > 0.0001f) {
         float a = P.hs - dist;
-        return 15.0f * __fdiv_rn(a * a, P.spiky_den) * rsqrtf(r2w);
+        return 15.0f * (a * a * P.inv_spiky_den) * rsqrtf(r2w);
     }
     return 0.0f;
 }

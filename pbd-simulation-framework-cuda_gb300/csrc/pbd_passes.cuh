@@ -1,0 +1,606 @@
+// pbd_passes.cuh -- the neighbour passes of a frame (no stored neighbour list).
+//
+// The reference builds an explicit N x M list once per frame (findContacts +
+// findNeighbours, kernel/Collision.h:11-160) and every density/vorticity/viscosity kernel
+// loops over it (kernel/Density.h).  Here every pass re-walks the cells in exactly the order
+// the list would hold them (27 cells with the x offset outer and z inner, then the shells of
+// findNeighbours), skipping self and stopping at the cap M, so sums run in the list's order.
+//
+// Each pass is split into a per-candidate contribution (`contrib`) and an in-order
+// accumulation (`add`).  Two walkers drive them:
+//  - walk_seq: one thread per particle (the common case);
+//  - walk_coop: one warp per particle.  Lanes evaluate 32 candidates at once and the
+//    contributions are added in list order through shuffles, so the result is bit-identical
+//    to walk_seq.  It takes the particles whose walk meets a cell range longer than
+//    kLongRange -- in practice the range that SortReorder.h:183-184 extends to N (up to M
+//    entries) -- which would otherwise serialise a whole warp behind one thread.
+#pragma once
+#include "pbd_device.cuh"
+#include "../../include/pbd.h"
+
+namespace pbd {
+
+constexpr uint32_t kLongRange = 32;
+constexpr uint32_t kFullMask = 0xffffffffu;
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t lanemask_lt_u() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Particles whose walk is handed to the warp-cooperative kernel.
+struct DeferList {
+    uint32_t* items;
+    uint32_t* count;
+    uint32_t* done;
+    uint32_t cap;
+};
+
+// Enumerate the non-empty cell ranges [s, e) of particle i's list in the reference's
+// order.  f(s, e, contact) returns true to stop; end_contacts(n) marks the end of the
+// 27-cell part (Collision.h:38-39).
+template <class F, class G>
+__device__ __forceinline__ void for_each_range(const DevParams& P, float4 pi, const uint32_t* __restrict__ cs,
+                                               const uint32_t* __restrict__ ce, F& f, G& end_contacts) {
+    const uint32_t N = P.N;
+    const bool quirk = (P.flags & PBD_FLAG_CELL_END_QUIRK) && N >= 2;
+    if (P.active & PBD_ACTIVE_FIND_CONTACTS) {
+        uint32_t mz[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) mz[c] = morton_axis(__fmaf_rn((float)(c - 1), P.d, pi.z));
+#pragma unroll 1
+        for (int a = -1; a <= 1; ++a) {
+            const uint32_t hx = morton_axis(__fmaf_rn((float)a, P.d, pi.x)) << 2;
+#pragma unroll 1
+            for (int b = -1; b <= 1; ++b) {
+                const uint32_t hxy = hx + (morton_axis(__fmaf_rn((float)b, P.d, pi.y)) << 1);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const uint32_t h = hxy + mz[c];
+                    if (h >= P.G) continue;
+                    const uint32_t s = __ldg(cs + h);
+                    if (s >= N) continue;
+                    uint32_t e = __ldg(ce + h);
+                    if ((quirk && h == N - 1) || e > N) e = N;   // entries >= N are skipped (Collision.h:59)
+                    if (f(s, e, true)) return;
+                }
+            }
+        }
+    }
+    if (end_contacts()) return;
+    if (P.active & PBD_ACTIVE_FIND_NEIGHBOURS) {
+        const int K = (int)P.K;
+#pragma unroll 1
+        for (int sh = 2; sh <= K; ++sh) {
+#pragma unroll 1
+            for (int a = -sh; a <= sh; ++a) {
+                const uint32_t hx = morton_axis(__fmaf_rn((float)a, P.d, pi.x)) << 2;
+#pragma unroll 1
+                for (int b = -sh; b <= sh; ++b) {
+                    const uint32_t hy = morton_axis(__fmaf_rn((float)b, P.d, pi.y)) << 1;
+                    const bool edge_ab = (a == sh || a == -sh || b == sh || b == -sh);
+                    const int cstep = edge_ab ? 1 : 2 * sh;   // interior columns: only c = +-sh
+#pragma unroll 1
+                    for (int c = -sh; c <= sh; c += cstep) {
+                        const uint32_t h = hx + hy + morton_axis(__fmaf_rn((float)c, P.d, pi.z));
+                        if (h >= P.G) continue;
+                        const uint32_t s = __ldg(cs + h);
+                        uint32_t e = __ldg(ce + h);
+                        if (s == kEmptyCell) continue;
+                        if ((quirk && h == N - 1) || e > N) e = N;   // entries >= N are skipped (Collision.h:142)
+                        if (f(s, e, false)) return;
+                    }
+                }
+            }
+        }
+    }
+}
+
+// One thread per particle.  Returns the list length; sets *deferred (and stops) when a
+// range longer than kLongRange is met and `defer` is set.
+template <class V>
+__device__ __forceinline__ uint32_t walk_seq(const DevParams& P, uint32_t i, float4 pi, const float4* __restrict__ p,
+                                             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                                             V& vis, bool defer, bool* deferred) {
+    const uint32_t M = P.M;
+    uint32_t cnt = 0;
+    if (M == 0) return 0;
+    auto range = [&](uint32_t s, uint32_t e, bool contact) -> bool {
+        if (defer && e - s > kLongRange) { *deferred = true; return true; }
+        for (uint32_t j = s; j < e; ++j) {
+            if (j == i) continue;
+            vis.add(vis.contrib(j, __ldg(p + j), contact), contact);
+            if (++cnt == M) return true;
+        }
+        return false;
+    };
+    auto endc = [&]() -> bool { vis.end_contacts(cnt); return false; };
+    for_each_range(P, pi, cs, ce, range, endc);
+    return cnt;
+}
+
+// One warp per particle (all 32 lanes call it with the same i).  Same list, same order.
+template <class V>
+__device__ __forceinline__ uint32_t walk_coop(const DevParams& P, uint32_t i, float4 pi, const float4* __restrict__ p,
+                                              const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, V& vis) {
+    const uint32_t M = P.M;
+    const uint32_t lane = lane_id(), lt = lanemask_lt_u();
+    uint32_t cnt = 0;
+    if (M == 0) return 0;
+    auto range = [&](uint32_t s, uint32_t e, bool contact) -> bool {
+        for (uint32_t c0 = s; c0 < e; c0 += 32u) {
+            const uint32_t j = c0 + lane;
+            bool valid = j < e && j != i;
+            const uint32_t b = __ballot_sync(kFullMask, valid);
+            valid = valid && __popc(b & lt) < M - cnt;
+            typename V::Contrib c = valid ? vis.contrib(j, __ldg(p + j), contact) : V::zero();
+            const uint32_t n = __popc(__ballot_sync(kFullMask, valid));
+            // only entries whose contribution changes a sum are added (in order); the others
+            // are exact no-ops of add() and still count toward the cap
+            uint32_t take = __ballot_sync(kFullMask, valid && V::effective(c));
+            while (take) {
+                const int k = __ffs(take) - 1;
+                take &= take - 1u;
+                vis.add(V::shfl(c, k), contact);
+            }
+            cnt += n;
+            if (cnt == M) return true;
+        }
+        return false;
+    };
+    auto endc = [&]() -> bool { vis.end_contacts(cnt); return false; };
+    for_each_range(P, pi, cs, ce, range, endc);
+    return cnt;
+}
+
+__device__ __forceinline__ float shfl_f(float v, int k) { return __shfl_sync(kFullMask, v, k); }
+__device__ __forceinline__ uint32_t shfl_u(uint32_t v, int k) { return __shfl_sync(kFullMask, v, k); }
+
+// Hand particle i to the cooperative kernel; if the list is full, walk it here.
+__device__ __forceinline__ bool defer_particle(const DeferList& D, uint32_t i) {
+    const uint32_t k = atomicAdd(D.count, 1u);
+    if (k < D.cap) { D.items[k] = i; return true; }
+    return false;
+}
+
+// Grid-stride loop of the cooperative kernels over the deferred particles, then the last
+// block to finish empties the list for the next pass.
+template <class F>
+__device__ __forceinline__ void for_each_deferred(const DeferList& D, F&& f) {
+    const uint32_t n = min(*((volatile uint32_t*)D.count), D.cap);
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < n; w += warps) f(D.items[w]);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(D.done, 1u) == gridDim.x - 1) {
+            *D.count = 0u;
+            *D.done = 0u;
+            __threadfence();
+        }
+    }
+}
+
+// ======================================================================================
+// computeLambda (Density.h:48-93)
+// ======================================================================================
+struct LambdaVisit {
+    struct Contrib { float a, b, gx, gy, gz, gw; uint32_t near; };
+    const DevParams& P;
+    float4 pi;
+    float A = 0.f, B = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f, Cw = 0.f;
+    __device__ LambdaVisit(const DevParams& P_, float4 pi_) : P(P_), pi(pi_) {}
+    __device__ void reset() { A = B = Cx = Cy = Cz = Cw = 0.f; }
+    __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u}; }
+    __device__ static bool effective(const Contrib& c) { return c.near != 0u; }
+    __device__ static Contrib shfl(const Contrib& c, int k) {
+        return Contrib{shfl_f(c.a, k), shfl_f(c.b, k), shfl_f(c.gx, k), shfl_f(c.gy, k), shfl_f(c.gz, k),
+                       shfl_f(c.gw, k), shfl_u(c.near, k)};
+    }
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, bool) const {
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z, rw = pi.w - pj.w;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (r2 >= P.cut2) return zero();      // every kernel is exactly 0 there
+        const float dist = sqrtf(r2);
+        const float s = spiky_scale(P, dist, r2 + rw * rw);
+        const float gx = s * rx, gy = s * ry, gz = s * rz, gw = s * rw;
+        return Contrib{poly6(P, dist), gx * gx + gy * gy + gz * gz + gw * gw, gx, gy, gz, gw, 1u};
+    }
+    __device__ __forceinline__ void add(const Contrib& c, bool) {
+        if (!c.near) return;
+        A += c.a; B += c.b;
+        Cx += c.gx; Cy += c.gy; Cz += c.gz; Cw += c.gw;
+    }
+    __device__ __forceinline__ float finish() const {
+        const float a = A / P.rho0 - 1.0f;
+        const float b = B / P.rho0;
+        const float c = (Cx * Cx + Cy * Cy + Cz * Cz + Cw * Cw) / P.rho0;
+        return -a / (b + c + P.lambda_eps);
+    }
+};
+
+__global__ void __launch_bounds__(128)
+lambda_kernel(DevParams P, const float4* __restrict__ p, const uint32_t* __restrict__ cs,
+              const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    LambdaVisit vis(P, p[i]);
+    bool deferred = false;
+    walk_seq(P, i, vis.pi, p, cs, ce, vis, true, &deferred);
+    if (deferred) {
+        if (defer_particle(D, i)) return;
+        vis.reset();
+        walk_seq(P, i, vis.pi, p, cs, ce, vis, false, &deferred);
+    }
+    lambda[i] = vis.finish();
+}
+
+__global__ void __launch_bounds__(128)
+lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const uint32_t* __restrict__ cs,
+                   const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D) {
+    for_each_deferred(D, [&](uint32_t i) {
+        LambdaVisit vis(P, p[i]);
+        walk_coop(P, i, vis.pi, p, cs, ce, vis);
+        if (lane_id() == 0) lambda[i] = vis.finish();
+    });
+}
+
+// ======================================================================================
+// computeDeltaPositions (Density.h:104-145) + solveCollisions type 0 (Collision.h:171-242,
+// Jacobi: contacts read the frame's snapshot, the adds of particle i apply in list order)
+// + applyDeltaPositions (Density.h:156-168) + updatePositions (Update.h:11-32).
+// ======================================================================================
+enum DeltaMode : uint32_t {
+    kDoDelta = 1u << 0,      // compute delta p from lambda
+    kDoCollide = 1u << 1,    // one solveCollisions pass over the contacts
+    kDoApply = 1u << 2,      // p -= delta
+    kLoadDelta = 1u << 3,    // delta from the buffer (not computed in this pass)
+    kStoreDelta = 1u << 4,   // keep delta in the buffer
+    kDoUpdate = 1u << 5,     // v = (p - x)/dt; x = p
+};
+
+struct DeltaVisit {
+    struct Contrib { float ax, ay, az, aw, cx, cy, cz; uint32_t flags; };   // flags: 1 delta part, 2 contact part
+    const DevParams& P;
+    const float* __restrict__ lambda;
+    float4 pi;
+    float li;
+    bool do_delta, do_collide, all_pairs;
+    float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;   // sum of (li + lj + sCorr) * grad
+    float4 pacc, xacc;                               // positions with the contact corrections added in order
+    float4 xi;
+    __device__ DeltaVisit(const DevParams& P_, const float* lam, float4 pi_, float li_, bool dd, bool dc, float4 xi_)
+        : P(P_), lambda(lam), pi(pi_), li(li_), do_delta(dd), do_collide(dc), all_pairs(P_.far_pairs_zero == 0u),
+          pacc(pi_), xacc(xi_), xi(xi_) {}
+    __device__ void reset() { ax = ay = az = aw = 0.f; pacc = pi; xacc = xi; }
+    __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u}; }
+    __device__ static bool effective(const Contrib& c) { return c.flags != 0u; }
+    __device__ static Contrib shfl(const Contrib& c, int k) {
+        return Contrib{shfl_f(c.ax, k), shfl_f(c.ay, k), shfl_f(c.az, k), shfl_f(c.aw, k), shfl_f(c.cx, k),
+                       shfl_f(c.cy, k), shfl_f(c.cz, k), shfl_u(c.flags, k)};
+    }
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool contact) const {
+        Contrib c = zero();
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z, rw = pi.w - pj.w;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (!all_pairs && r2 >= P.cut2) return c;
+        const float dist = sqrtf(r2);
+        if (do_delta) {
+            const float s = spiky_scale(P, dist, r2 + rw * rw);
+            if (s != 0.0f || all_pairs) {
+                const float W = poly6(P, dist);
+                const float sc = -P.k_scorr * powi(W * P.inv_wq, P.n_scorr);
+                const float coef = (li + __ldg(lambda + j) + sc) * s;
+                c.ax = coef * rx; c.ay = coef * ry; c.az = coef * rz; c.aw = coef * rw;
+                c.flags |= 1u;
+            }
+        }
+        if (contact && do_collide) {
+            const float overlap = P.d - dist;
+            if (overlap > 0.0f && dist > 0.00001f) {
+                const float sc = -0.5f * overlap;
+                const float inv = 1.0f / dist;      // dir / len with one reciprocal
+                c.cx = (sc * (-rx * inv)) * P.one_minus_stiffness;
+                c.cy = (sc * (-ry * inv)) * P.one_minus_stiffness;
+                c.cz = (sc * (-rz * inv)) * P.one_minus_stiffness;
+                c.flags |= 2u;
+            }
+        }
+        return c;
+    }
+    __device__ __forceinline__ void add(const Contrib& c, bool) {
+        if (c.flags & 1u) { ax += c.ax; ay += c.ay; az += c.az; aw += c.aw; }
+        if (c.flags & 2u) {
+            pacc.x += c.cx; xacc.x += c.cx;
+            pacc.y += c.cy; xacc.y += c.cy;
+            pacc.z += c.cz; xacc.z += c.cz;
+        }
+    }
+};
+
+__device__ __forceinline__ void delta_finish(const DevParams& P, uint32_t mode, uint32_t i, const DeltaVisit& vis,
+                                             float4* __restrict__ pout, float4* __restrict__ x, float4* __restrict__ v,
+                                             float4* __restrict__ delta) {
+    float4 pn = vis.pacc, xn = vis.xacc;
+    float4 dp = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (mode & kDoDelta) dp = make_float4(vis.ax / P.rho0, vis.ay / P.rho0, vis.az / P.rho0, vis.aw / P.rho0);
+    else if (mode & kLoadDelta) dp = delta[i];
+    if (mode & kStoreDelta) delta[i] = dp;
+    if (mode & kDoApply) { pn.x -= dp.x; pn.y -= dp.y; pn.z -= dp.z; pn.w -= dp.w; }
+    if (mode & kDoUpdate) {
+        const float r = P.inv_dt;
+        v[i] = make_float4((pn.x - xn.x) * r, (pn.y - xn.y) * r, (pn.z - xn.z) * r, (pn.w - xn.w) * r);
+        xn = pn;
+    }
+    pout[i] = pn;
+    if (mode & (kDoCollide | kDoUpdate)) x[i] = xn;
+}
+
+__global__ void __launch_bounds__(128, 4)
+delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, float4* __restrict__ pout,
+             float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
+             float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+             DeferList D) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const float4 pi = pin[i];
+    const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
+    const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
+    DeltaVisit vis(P, lambda, pi, li, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
+    if (mode & (kDoDelta | kDoCollide)) {
+        bool deferred = false;
+        walk_seq(P, i, pi, pin, cs, ce, vis, true, &deferred);
+        if (deferred) {
+            if (defer_particle(D, i)) return;
+            vis.reset();
+            walk_seq(P, i, pi, pin, cs, ce, vis, false, &deferred);
+        }
+    }
+    delta_finish(P, mode, i, vis, pout, x, v, delta);
+}
+
+__global__ void __launch_bounds__(128)
+delta_coop_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, float4* __restrict__ pout,
+                  float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
+                  float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                  DeferList D) {
+    for_each_deferred(D, [&](uint32_t i) {
+        const float4 pi = pin[i];
+        const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
+        const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
+        DeltaVisit vis(P, lambda, pi, li, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
+        walk_coop(P, i, pi, pin, cs, ce, vis);
+        if (lane_id() == 0) delta_finish(P, mode, i, vis, pout, x, v, delta);
+    });
+}
+
+// updatePositions on its own (Update.h:11-32), when no delta pass can carry it.
+__global__ void __launch_bounds__(256)
+update_kernel(DevParams P, const float4* __restrict__ p, float4* __restrict__ x, float4* __restrict__ v) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const float4 pp = p[i], xx = x[i];
+    const float r = P.inv_dt;
+    v[i] = make_float4((pp.x - xx.x) * r, (pp.y - xx.y) * r, (pp.z - xx.z) * r, (pp.w - xx.w) * r);
+    x[i] = pp;
+}
+
+// ======================================================================================
+// computeOmega (Density.h:232-269): omega_i = sum_j (v_j - v_i) x spiky(p_i, p_j)
+// ======================================================================================
+struct OmegaVisit {
+    struct Contrib { float ox, oy, oz; uint32_t near; };
+    const DevParams& P;
+    const float4* __restrict__ v;
+    float4 pi, vi;
+    float ox = 0.f, oy = 0.f, oz = 0.f;
+    __device__ OmegaVisit(const DevParams& P_, const float4* v_, float4 pi_, float4 vi_) : P(P_), v(v_), pi(pi_), vi(vi_) {}
+    __device__ void reset() { ox = oy = oz = 0.f; }
+    __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0u}; }
+    __device__ static bool effective(const Contrib& c) { return c.near != 0u; }
+    __device__ static Contrib shfl(const Contrib& c, int k) {
+        return Contrib{shfl_f(c.ox, k), shfl_f(c.oy, k), shfl_f(c.oz, k), shfl_u(c.near, k)};
+    }
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool) const {
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z, rw = pi.w - pj.w;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (r2 >= P.cut2) return zero();
+        const float dist = sqrtf(r2);
+        const float s = spiky_scale(P, dist, r2 + rw * rw);
+        if (s == 0.0f) return zero();
+        const float4 vj = __ldg(v + j);
+        const float wx = vj.x - vi.x, wy = vj.y - vi.y, wz = vj.z - vi.z;
+        const float gx = s * rx, gy = s * ry, gz = s * rz;
+        return Contrib{wy * gz - wz * gy, wz * gx - wx * gz, wx * gy - wy * gx, 1u};
+    }
+    __device__ __forceinline__ void add(const Contrib& c, bool) {
+        if (!c.near) return;
+        ox += c.ox; oy += c.oy; oz += c.oz;
+    }
+};
+
+__global__ void __launch_bounds__(128)
+omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ v,
+             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega, DeferList D) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    OmegaVisit vis(P, v, p[i], v[i]);
+    bool deferred = false;
+    walk_seq(P, i, vis.pi, p, cs, ce, vis, true, &deferred);
+    if (deferred) {
+        if (defer_particle(D, i)) return;
+        vis.reset();
+        walk_seq(P, i, vis.pi, p, cs, ce, vis, false, &deferred);
+    }
+    omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
+}
+
+__global__ void __launch_bounds__(128)
+omega_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ v,
+                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega,
+                  DeferList D) {
+    for_each_deferred(D, [&](uint32_t i) {
+        OmegaVisit vis(P, v, p[i], v[i]);
+        walk_coop(P, i, vis.pi, p, cs, ce, vis);
+        if (lane_id() == 0) omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
+    });
+}
+
+// ======================================================================================
+// computeVorticity (Density.h:179-221) + computeViscosity (Density.h:280-310, Jacobi).
+// Vorticity sums |omega_j - omega_i| / (p_j - p_i + 1e-8) componentwise over EVERY list
+// entry (no kernel weight), so with vorticity on no pair may be skipped.
+// ======================================================================================
+struct VortViscVisit {
+    struct Contrib { float gx, gy, gz, sx, sy, sz, sw; uint32_t flags; };   // 1 vorticity, 2 viscosity
+    const DevParams& P;
+    const float4* __restrict__ v;
+    const float4* __restrict__ omega;
+    float4 pi, vi, oi;
+    bool vort, visc;
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
+    __device__ VortViscVisit(const DevParams& P_, const float4* v_, const float4* om, float4 pi_, float4 vi_, float4 oi_,
+                             bool vo, bool vs)
+        : P(P_), v(v_), omega(om), pi(pi_), vi(vi_), oi(oi_), vort(vo), visc(vs) {}
+    __device__ void reset() { gx = gy = gz = sx = sy = sz = sw = 0.f; }
+    __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u}; }
+    __device__ static bool effective(const Contrib& c) { return c.flags != 0u; }
+    __device__ static Contrib shfl(const Contrib& c, int k) {
+        return Contrib{shfl_f(c.gx, k), shfl_f(c.gy, k), shfl_f(c.gz, k), shfl_f(c.sx, k),
+                       shfl_f(c.sy, k), shfl_f(c.sz, k), shfl_f(c.sw, k), shfl_u(c.flags, k)};
+    }
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool) const {
+        Contrib c = zero();
+        if (vort) {
+            const float4 oj = __ldg(omega + j);
+            const float dx = oj.x - oi.x, dy = oj.y - oi.y, dz = oj.z - oi.z;
+            const float ol = sqrtf(dx * dx + dy * dy + dz * dz);
+            c.gx = ol / ((pj.x - pi.x) + 0.00000001f);
+            c.gy = ol / ((pj.y - pi.y) + 0.00000001f);
+            c.gz = ol / ((pj.z - pi.z) + 0.00000001f);
+            c.flags |= 1u;
+        }
+        if (visc) {
+            const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            const float r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 >= P.hp2) return c;
+            const float W = poly6(P, sqrtf(r2));
+            if (W == 0.0f) return c;
+            const float4 vj = __ldg(v + j);
+            c.sx = (vj.x - vi.x) * W; c.sy = (vj.y - vi.y) * W;
+            c.sz = (vj.z - vi.z) * W; c.sw = (vj.w - vi.w) * W;
+            c.flags |= 2u;
+        }
+        return c;
+    }
+    __device__ __forceinline__ void add(const Contrib& c, bool) {
+        if (c.flags & 1u) { gx += c.gx; gy += c.gy; gz += c.gz; }
+        if (c.flags & 2u) { sx += c.sx; sy += c.sy; sz += c.sz; sw += c.sw; }
+    }
+};
+
+__device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i, const VortViscVisit& vis,
+                                                 float4* __restrict__ vout, float4* __restrict__ fext) {
+    if (vis.vort) {
+        const float EPS = 0.00000001f;
+        const float gl = sqrtf(vis.gx * vis.gx + vis.gy * vis.gy + vis.gz * vis.gz);
+        const float inv = 1.0f / (gl + EPS);
+        const float nx = inv * (vis.gx + EPS), ny = inv * (vis.gy + EPS), nz = inv * (vis.gz + EPS);
+        const float e = P.e_vort;
+        const float4 oi = vis.oi;
+        fext[i] = make_float4(e * (ny * oi.z - nz * oi.y), e * (nz * oi.x - nx * oi.z), e * (nx * oi.y - ny * oi.x), 0.f);
+    }
+    if (vis.visc) {
+        const float c = P.c_visc;
+        const float4 vi = vis.vi;
+        vout[i] = make_float4(vi.x + c * vis.sx, vi.y + c * vis.sy, vi.z + c * vis.sz, vi.w + c * vis.sw);
+    }
+}
+
+__global__ void __launch_bounds__(128, 4)
+vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ vin,
+                 float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
+                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
+                 DeferList D) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
+    bool deferred = false;
+    walk_seq(P, i, vis.pi, p, cs, ce, vis, true, &deferred);
+    if (deferred) {
+        if (defer_particle(D, i)) return;
+        vis.reset();
+        walk_seq(P, i, vis.pi, p, cs, ce, vis, false, &deferred);
+    }
+    vort_visc_finish(P, i, vis, vout, fext);
+}
+
+__global__ void __launch_bounds__(128)
+vort_visc_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ vin,
+                      float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
+                      const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
+                      DeferList D) {
+    for_each_deferred(D, [&](uint32_t i) {
+        const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
+        walk_coop(P, i, vis.pi, p, cs, ce, vis);
+        if (lane_id() == 0) vort_visc_finish(P, i, vis, vout, fext);
+    });
+}
+
+// ======================================================================================
+// Debug: materialise the neighbour list (findContacts + findNeighbours, Collision.h:11-160)
+// ======================================================================================
+struct ListVisit {
+    struct Contrib { uint32_t j; };
+    uint32_t* out;
+    uint32_t cap, n = 0, contacts = 0xFFFFFFFFu;
+    __device__ ListVisit(uint32_t* o, uint32_t c) : out(o), cap(c) {}
+    __device__ static Contrib zero() { return Contrib{0u}; }
+    __device__ static bool effective(const Contrib&) { return true; }
+    __device__ static Contrib shfl(const Contrib& c, int k) { return Contrib{shfl_u(c.j, k)}; }
+    __device__ __forceinline__ void end_contacts(uint32_t c) { contacts = c; }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4&, bool) const { return Contrib{j}; }
+    __device__ __forceinline__ void add(const Contrib& c, bool) {
+        if (n < cap) out[n] = c.j;
+        ++n;
+    }
+};
+
+__global__ void list_kernel(DevParams P, const float4* __restrict__ p, const uint32_t* __restrict__ cs,
+                            const uint32_t* __restrict__ ce, uint32_t cap, uint32_t* list,
+                            uint32_t* count, uint32_t* contacts, float4* col, int coop) {
+    // coop = 0: one thread per particle; coop = 1: one warp per particle (checks walk_coop)
+    const uint32_t i = coop ? (blockIdx.x * blockDim.x + threadIdx.x) >> 5 : blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    ListVisit vis(list + (size_t)i * cap, cap);
+    uint32_t n;
+    if (coop) {
+        ListVisit lv(lane_id() == 0 ? list + (size_t)i * cap : nullptr, lane_id() == 0 ? cap : 0u);
+        n = walk_coop(P, i, p[i], p, cs, ce, lv);
+        vis.contacts = lv.contacts;
+        if (lane_id() != 0) return;
+    } else {
+        bool deferred = false;
+        n = walk_seq(P, i, p[i], p, cs, ce, vis, false, &deferred);
+    }
+    if (vis.contacts == 0xFFFFFFFFu) vis.contacts = n;   // cap reached inside the 27 cells
+    count[i] = n;
+    contacts[i] = vis.contacts;
+    if (col) {
+        const float f = (float)n / (float)P.M;
+        col[i] = make_float4(f, f, f, 1.0f);
+    }
+}
+
+}  // namespace pbd

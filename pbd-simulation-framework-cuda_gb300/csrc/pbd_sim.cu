@@ -37,6 +37,7 @@ struct Cur {
 
 constexpr int kThreadsParticle = 256;
 constexpr int kThreadsNeighbour = 128;
+constexpr int kThreadsCoop = 128;         // 4 warps, one deferred particle per warp
 
 inline uint32_t div_up(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
@@ -55,6 +56,8 @@ struct pbd_sim {
     uint32_t *cell_start = nullptr, *cell_end = nullptr;
     uint32_t *hist = nullptr, *status = nullptr, *tile_counter = nullptr, *err = nullptr, *table_n = nullptr;
     uint32_t max_tiles = 0;
+    uint32_t *defer_items = nullptr, *defer_count = nullptr, *defer_done = nullptr;
+    uint32_t defer_cap = 0;
     Cur cur;
     int table_passes = -1;        // passes of the sort whose keys the cell tables hold (-1: none)
     uint32_t table_hint = 0;      // host upper bound of the device word table_n
@@ -105,6 +108,7 @@ DevParams make_dev_params(const pbd_sim* s) {
     P.n_scorr = p.n_scorr;
     P.d = 2.0f * p.particle_radius;                       // Initialize.h:43
     P.dt = p.delta_t;
+    P.inv_dt = 1.0f / p.delta_t;
     P.gravity = p.gravity;
     P.rho0 = p.rest_density;
     P.hs = P.d * p.kernel_width_spiky;                    // Initialize.h:45
@@ -132,6 +136,8 @@ DevParams make_dev_params(const pbd_sim* s) {
         wq = (315.0f * t3 * t3) * P.poly_inv_den;
     }
     P.wq = wq;
+    P.inv_wq = wq != 0.0f ? 1.0f / wq : 0.0f;
+    P.inv_spiky_den = 1.0f / P.spiky_den;
     P.far_pairs_zero = (wq > 0.0f && std::isfinite(wq) && p.n_scorr >= 0) ? 1u : 0u;
     const float c = std::max(P.hp, std::max(P.hs, P.d));
     P.cut2 = c * c * 1.0001f;
@@ -206,6 +212,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     if (front_only) return cudaGetLastError();
 
     const uint32_t gn = div_up(N, kThreadsNeighbour);
+    const DeferList D{s->defer_items, s->defer_count, s->defer_done, s->defer_cap};
+    const uint32_t gc = (uint32_t)s->num_sms * 2u;   // cooperative kernels: grid-stride over the deferred
     const uint32_t act = prm.active;
     const uint32_t I = prm.solver_iterations, Sx = prm.stabilization_iterations;
     const bool do_delta = act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS, do_apply = act & PBD_ACTIVE_APPLY_DELTA_POSITIONS;
@@ -215,9 +223,10 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     for (uint32_t it = 0; it < I; ++it) {
         if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
             PROF_BEGIN("lambda");
-            lambda_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->cell_start, s->cell_end, s->lambda);
+            lambda_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->cell_start, s->cell_end, s->lambda, D);
+            lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], s->cell_start, s->cell_end, s->lambda, D);
             PROF_END();
-            ++nl;
+            nl += 2;
             last_was_delta = false;
         }
         // passes of this iteration: pass 0 carries computeDeltaPositions and the first
@@ -240,9 +249,11 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             if (final_pass && do_update) mode |= kDoUpdate;
             PROF_BEGIN("delta");
             delta_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, mode, s->p[cur.p], s->p[cur.p ^ 1], s->x[cur.x],
-                                                            s->v[cur.v], s->lambda, s->delta, s->cell_start, s->cell_end);
+                                                            s->v[cur.v], s->lambda, s->delta, s->cell_start, s->cell_end, D);
+            delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], s->p[cur.p ^ 1], s->x[cur.x],
+                                                           s->v[cur.v], s->lambda, s->delta, s->cell_start, s->cell_end, D);
             PROF_END();
-            ++nl;
+            nl += 2;
             cur.p ^= 1;
             last_was_delta = (mode & kDoUpdate) != 0;
         }
@@ -255,17 +266,20 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     }
     if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
         PROF_BEGIN("omega");
-        omega_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->cell_start, s->cell_end, s->omega);
+        omega_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
+        omega_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
         PROF_END();
-        ++nl;
+        nl += 2;
     }
     const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     if (vort || visc) {
         PROF_BEGIN("vort_visc");
         vort_visc_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->v[cur.v ^ 1], s->omega,
-                                                            s->fext, s->cell_start, s->cell_end, vort, visc);
+                                                            s->fext, s->cell_start, s->cell_end, vort, visc, D);
+        vort_visc_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->v[cur.v ^ 1], s->omega,
+                                                           s->fext, s->cell_start, s->cell_end, vort, visc, D);
         PROF_END();
-        ++nl;
+        nl += 2;
         if (visc) cur.v ^= 1;
     }
     (void)G;
@@ -382,6 +396,9 @@ int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
     parts.push_back({(void**)&s->status, (size_t)kMaxPasses * s->max_tiles * kRadix * 4});
     parts.push_back({(void**)&s->tile_counter, kMaxPasses * 4}); parts.push_back({(void**)&s->err, 4});
     parts.push_back({(void**)&s->table_n, 4});
+    s->defer_cap = std::min<uint32_t>(capacity, 1u << 16);
+    parts.push_back({(void**)&s->defer_items, (size_t)s->defer_cap * 4});
+    parts.push_back({(void**)&s->defer_count, 4}); parts.push_back({(void**)&s->defer_done, 4});
     size_t total = 0;
     for (auto& pt : parts) total += (pt.second + 255) & ~size_t(255);
     e = cudaMalloc(&s->arena, total);
@@ -565,7 +582,8 @@ int pbd_debug_dump(pbd_sim* s, uint32_t* keys, uint32_t* perm, uint32_t* cell_st
     return PBD_OK;
 }
 
-int pbd_debug_neighbours(pbd_sim* s, uint32_t max_entries, uint32_t* list, uint32_t* count, uint32_t* contacts) {
+int pbd_debug_neighbours(pbd_sim* s, uint32_t max_entries, uint32_t* list, uint32_t* count, uint32_t* contacts,
+                         int walker) {
     clear_error();
     if (int rc = check_sim(s, "pbd_debug_neighbours")) return rc;
     if (int rc = sync_last(s)) return rc;
@@ -578,8 +596,10 @@ int pbd_debug_neighbours(pbd_sim* s, uint32_t max_entries, uint32_t* list, uint3
     CK(cudaMalloc(&dk, n * 4));
     const DevParams P = make_dev_params(s);
     const bool cols = (s->prm.flags & PBD_FLAG_COLORS) && (s->prm.active & PBD_ACTIVE_FIND_NEIGHBOURS);
-    list_kernel<<<div_up(n, 128), 128, 0, s->last_stream>>>(P, s->p[s->cur.p], s->cell_start, s->cell_end, max_entries,
-                                                            dl, dc, dk, cols ? s->col[s->cur.x] : nullptr);
+    const uint32_t threads = walker ? (uint32_t)n * 32u : (uint32_t)n;
+    list_kernel<<<div_up(threads, 128), 128, 0, s->last_stream>>>(P, s->p[s->cur.p], s->cell_start, s->cell_end,
+                                                                  max_entries, dl, dc, dk,
+                                                                  cols ? s->col[s->cur.x] : nullptr, walker ? 1 : 0);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->last_stream);
     if (e == cudaSuccess && list) e = cudaMemcpy(list, dl, n * (size_t)max_entries * 4, cudaMemcpyDeviceToHost);

@@ -91,7 +91,7 @@ def lib():
             "pbd_add_particle": [vp, fp, fp], "pbd_clear": [vp], "pbd_step": [vp, i32, vp], "pbd_sync": [vp],
             "pbd_get_state": [vp, fp, fp, fp, u32p], "pbd_get_device_state": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)],
             "pbd_debug_dump": [vp, u32p, u32p, u32p, u32p, u32, fp, fp, fp],
-            "pbd_debug_neighbours": [vp, u32, u32p, u32p, u32p], "pbd_debug_front": [vp, vp],
+            "pbd_debug_neighbours": [vp, u32, u32p, u32p, u32p, i32], "pbd_debug_front": [vp, vp],
             "pbd_launches_per_step": [vp, u32p],
             "pbd_profile_frames": [vp, i32, vp, C.POINTER(KernelStat), u32, u32p],
         }
@@ -214,10 +214,10 @@ class Sim:
         check(self.L.pbd_debug_dump(self.h, _up(keys), _up(perm), _up(cs), _up(ce), ncells, _fp(lam), _fp(fext), _fp(om)))
         return {"keys": keys, "perm": perm, "cell_start": cs, "cell_end": ce, "lambda": lam, "fext": fext, "omega": om}
 
-    def neighbours(self, max_entries):
+    def neighbours(self, max_entries, walker=0):
         n = self.n
         lst = np.zeros((n, max_entries), np.uint32); cnt = np.zeros(n, np.uint32); con = np.zeros(n, np.uint32)
-        check(self.L.pbd_debug_neighbours(self.h, max_entries, _up(lst), _up(cnt), _up(con)))
+        check(self.L.pbd_debug_neighbours(self.h, max_entries, _up(lst), _up(cnt), _up(con), walker))
         return lst, cnt, con
 
     def front(self, stream=0):

@@ -77,10 +77,33 @@ def test_neighbour_lists_shells_and_cap(need_gpu, pbd, scenes, oracle_mod):
         sim, orc = setup_pair(pbd, oracle_mod, params, pos, vel)
         sim.front()
         orc.step_phase(oracle_mod.PHASE_LISTS)
-        gl, gc, gk = sim.neighbours(cap)
         ol, oc, ok = orc.neighbours(cap)
+        for walker in (0, 1):
+            gl, gc, gk = sim.neighbours(cap, walker=walker)
+            assert np.array_equal(gc, oc) and np.array_equal(gk, ok)
+            assert np.array_equal(gl, ol)
+
+
+@pytest.mark.parametrize("cap", [512, 100, 30])
+def test_cell_end_quirk_long_range(need_gpu, pbd, scenes, oracle_mod, cap):
+    """8^3 lattice at cells 2..9: cell N-1 = 511 = (7,7,7) is occupied and not the last cell, so
+    SortReorder.h:183-184 stretches its range to N (~300 entries).  Those particles take the
+    warp-per-particle walker; lists, lambda and positions must match the oracle, with the cap
+    M falling inside the stretched range for the smaller caps."""
+    params, pos, vel = workload(pbd, scenes, shape=(8, 8, 8), box=16, seed=21, vorticity=0.0005, viscosity=0.01)
+    params.max_neighbours_per_particle = cap
+    sim, orc = setup_pair(pbd, oracle_mod, params, pos, vel)
+    sim.front()
+    orc.step_phase(oracle_mod.PHASE_LISTS)
+    ol, oc, ok = orc.neighbours(cap)
+    assert oc.max() == min(cap, 512) or oc.max() > 64     # the stretched range is present
+    for walker in (0, 1):
+        gl, gc, gk = sim.neighbours(cap, walker=walker)
         assert np.array_equal(gc, oc) and np.array_equal(gk, ok)
         assert np.array_equal(gl, ol)
+    g, o, sim2, orc2 = _run_both(pbd, oracle_mod, params, pos, vel, 2)
+    assert maxdiff(g["x"][:, :3], o["x"][:, :3]) < 10 * TOL_X1
+    assert maxdiff(g["v"][:, :3], o["v"][:, :3]) < 10 * TOL_V1
 
 
 def _run_both(pbd, oracle_mod, params, pos, vel, steps, precision="f32"):
