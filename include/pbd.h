@@ -194,6 +194,22 @@ typedef struct pbd_kernel_stat {
 int pbd_profile_frames(pbd_sim* sim, int nsteps, void* stream, pbd_kernel_stat* stats,
                        uint32_t max_stats, uint32_t* n_stats);
 
+/* ---- sorting without allocation -------------------------------------------------- */
+/* No counterpart in the reference.  For hosts that cannot call cudaMalloc where they sort
+ * (engines that own all device memory from start-up, frame loops that must not stall on an
+ * allocation): the step's stable radix sort of uint32 keys, with every byte of working memory
+ * taken from one fixed array inside the library.  Inputs and outputs are the caller's device
+ * buffers: d_keys_out receives the keys in ascending order and d_perm_out the input index of
+ * each output key (a stable sort, so equal keys keep their input order).  Only the low
+ * `key_bits` bits (1..32) are sorted.  d_keys_out and d_perm_out must not overlap d_keys_in.
+ * Limit: n <= 1,048,576 keys (the fixed array is about 10 MiB and stays on every GPU that loads
+ * the library until the process exits); larger n returns PBD_ERR_CAPACITY.  The first call on
+ * each device looks up the array's device address (make it before any stream capture).  All
+ * calls share the array: calls whose GPU work overlaps race and must be serialised by the
+ * caller.  Asynchronous on `stream`. */
+int pbd_sort_keys_noalloc(const uint32_t* d_keys_in, uint32_t* d_keys_out, uint32_t* d_perm_out,
+                          uint32_t n, uint32_t key_bits, void* stream);
+
 /* Text of the last error on this thread ("" if none). */
 const char* pbd_last_error(void);
 uint32_t pbd_abi_version(void);

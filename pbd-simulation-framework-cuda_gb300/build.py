@@ -16,7 +16,7 @@ INCLUDE = os.path.join(HERE, "..", "include")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU = ["pbd_sim.cu"]
+CU = ["pbd_sim.cu", "pbd_noalloc.cu"]
 CPP = ["pbd_config.cpp"]
 
 

@@ -27,7 +27,7 @@ EXPORTED = [
     "pbd_create", "pbd_destroy", "pbd_set_params", "pbd_get_params", "pbd_num_particles", "pbd_capacity",
     "pbd_add_particles", "pbd_add_particles_device", "pbd_add_particle", "pbd_clear", "pbd_step", "pbd_sync",
     "pbd_get_state", "pbd_get_device_state", "pbd_debug_dump", "pbd_debug_neighbours", "pbd_debug_front",
-    "pbd_launches_per_step", "pbd_profile_frames", "pbd_last_error", "pbd_abi_version",
+    "pbd_launches_per_step", "pbd_profile_frames", "pbd_sort_keys_noalloc", "pbd_last_error", "pbd_abi_version",
 ]
 
 
@@ -94,6 +94,7 @@ def lib():
             "pbd_debug_neighbours": [vp, u32, u32p, u32p, u32p, i32], "pbd_debug_front": [vp, vp],
             "pbd_launches_per_step": [vp, u32p],
             "pbd_profile_frames": [vp, i32, vp, C.POINTER(KernelStat), u32, u32p],
+            "pbd_sort_keys_noalloc": [vp, vp, vp, u32, u32, vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
