@@ -27,6 +27,9 @@
  *    applied after the boundary writes (the order of a sequential run of the kernel).
  *  - findContacts/findNeighbours disabled: the list part is empty (the reference would
  *    reuse a list whose indices refer to an earlier order).
+ * The restatement is pinned to the reference's own kernel code run on the CPU
+ * (oracle/refexec, fixtures in tests/golden): bit-exact front of a frame and neighbour lists,
+ * FP tolerance after whole frames.
  * The sort is a stable LSD counting sort over all 32 key bits: CUB's
  * DeviceRadixSort::SortPairs (kernel/SortReorder.h:39-47) is a stable LSD radix sort, so
  * any stable sort by the uint32 key gives the same permutation.

@@ -40,7 +40,10 @@ struct DeferList {
 
 // Enumerate the non-empty cell ranges [s, e) of particle i's list in the reference's
 // order.  f(s, e, contact) returns true to stop; end_contacts(n) marks the end of the
-// 27-cell part (Collision.h:38-39).
+// 27-cell part (Collision.h:38-39).  `pi` is the particle's anchor: its predicted position
+// right after the frame's re-order, from which the reference builds the list once per frame
+// (findContacts/findNeighbours run before the solver loop, Fluid.cu:41-47); passes later in
+// the frame use the moved positions for the physics but the anchor's cells.
 template <class F, class G>
 __device__ __forceinline__ void for_each_range(const DevParams& P, float4 pi, const uint32_t* __restrict__ cs,
                                                const uint32_t* __restrict__ ce, F& f, G& end_contacts) {
@@ -99,9 +102,10 @@ __device__ __forceinline__ void for_each_range(const DevParams& P, float4 pi, co
 }
 
 // One thread per particle.  Returns the list length; sets *deferred (and stops) when a
-// range longer than kLongRange is met and `defer` is set.
+// range longer than kLongRange is met and `defer` is set.  `anchor` selects the cells, `p`
+// holds the current positions.
 template <class V>
-__device__ __forceinline__ uint32_t walk_seq(const DevParams& P, uint32_t i, float4 pi, const float4* __restrict__ p,
+__device__ __forceinline__ uint32_t walk_seq(const DevParams& P, uint32_t i, float4 anchor, const float4* __restrict__ p,
                                              const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
                                              V& vis, bool defer, bool* deferred) {
     const uint32_t M = P.M;
@@ -117,13 +121,13 @@ __device__ __forceinline__ uint32_t walk_seq(const DevParams& P, uint32_t i, flo
         return false;
     };
     auto endc = [&]() -> bool { vis.end_contacts(cnt); return false; };
-    for_each_range(P, pi, cs, ce, range, endc);
+    for_each_range(P, anchor, cs, ce, range, endc);
     return cnt;
 }
 
 // One warp per particle (all 32 lanes call it with the same i).  Same list, same order.
 template <class V>
-__device__ __forceinline__ uint32_t walk_coop(const DevParams& P, uint32_t i, float4 pi, const float4* __restrict__ p,
+__device__ __forceinline__ uint32_t walk_coop(const DevParams& P, uint32_t i, float4 anchor, const float4* __restrict__ p,
                                               const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, V& vis) {
     const uint32_t M = P.M;
     const uint32_t lane = lane_id(), lt = lanemask_lt_u();
@@ -151,7 +155,7 @@ __device__ __forceinline__ uint32_t walk_coop(const DevParams& P, uint32_t i, fl
         return false;
     };
     auto endc = [&]() -> bool { vis.end_contacts(cnt); return false; };
-    for_each_range(P, pi, cs, ce, range, endc);
+    for_each_range(P, anchor, cs, ce, range, endc);
     return cnt;
 }
 
@@ -223,27 +227,27 @@ struct LambdaVisit {
 };
 
 __global__ void __launch_bounds__(128)
-lambda_kernel(DevParams P, const float4* __restrict__ p, const uint32_t* __restrict__ cs,
+lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
               const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     LambdaVisit vis(P, p[i]);
     bool deferred = false;
-    walk_seq(P, i, vis.pi, p, cs, ce, vis, true, &deferred);
+    walk_seq(P, i, pa[i], p, cs, ce, vis, true, &deferred);
     if (deferred) {
         if (defer_particle(D, i)) return;
         vis.reset();
-        walk_seq(P, i, vis.pi, p, cs, ce, vis, false, &deferred);
+        walk_seq(P, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
     lambda[i] = vis.finish();
 }
 
 __global__ void __launch_bounds__(128)
-lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const uint32_t* __restrict__ cs,
+lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
                    const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
         LambdaVisit vis(P, p[i]);
-        walk_coop(P, i, vis.pi, p, cs, ce, vis);
+        walk_coop(P, i, pa[i], p, cs, ce, vis);
         if (lane_id() == 0) lambda[i] = vis.finish();
     });
 }
@@ -341,7 +345,7 @@ __device__ __forceinline__ void delta_finish(const DevParams& P, uint32_t mode, 
 }
 
 __global__ void __launch_bounds__(128, 4)
-delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, float4* __restrict__ pout,
+delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const float4* __restrict__ pa, float4* __restrict__ pout,
              float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
              float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
              DeferList D) {
@@ -354,18 +358,18 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, float4*
     DeltaVisit vis(P, lambda, pi, li, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
     if (mode & (kDoDelta | kDoCollide)) {
         bool deferred = false;
-        walk_seq(P, i, pi, pin, cs, ce, vis, true, &deferred);
+        walk_seq(P, i, pa[i], pin, cs, ce, vis, true, &deferred);
         if (deferred) {
             if (defer_particle(D, i)) return;
             vis.reset();
-            walk_seq(P, i, pi, pin, cs, ce, vis, false, &deferred);
+            walk_seq(P, i, pa[i], pin, cs, ce, vis, false, &deferred);
         }
     }
     delta_finish(P, mode, i, vis, pout, x, v, delta);
 }
 
 __global__ void __launch_bounds__(128)
-delta_coop_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, float4* __restrict__ pout,
+delta_coop_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const float4* __restrict__ pa, float4* __restrict__ pout,
                   float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
                   float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
                   DeferList D) {
@@ -375,7 +379,7 @@ delta_coop_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, fl
         const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
         DeltaVisit vis(P, lambda, pi, li, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
-        walk_coop(P, i, pi, pin, cs, ce, vis);
+        walk_coop(P, i, pa[i], pin, cs, ce, vis);
         if (lane_id() == 0) delta_finish(P, mode, i, vis, pout, x, v, delta);
     });
 }
@@ -427,28 +431,28 @@ struct OmegaVisit {
 };
 
 __global__ void __launch_bounds__(128)
-omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ v,
+omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ v,
              const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega, DeferList D) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     OmegaVisit vis(P, v, p[i], v[i]);
     bool deferred = false;
-    walk_seq(P, i, vis.pi, p, cs, ce, vis, true, &deferred);
+    walk_seq(P, i, pa[i], p, cs, ce, vis, true, &deferred);
     if (deferred) {
         if (defer_particle(D, i)) return;
         vis.reset();
-        walk_seq(P, i, vis.pi, p, cs, ce, vis, false, &deferred);
+        walk_seq(P, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
     omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
 }
 
 __global__ void __launch_bounds__(128)
-omega_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ v,
+omega_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ v,
                   const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega,
                   DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
         OmegaVisit vis(P, v, p[i], v[i]);
-        walk_coop(P, i, vis.pi, p, cs, ce, vis);
+        walk_coop(P, i, pa[i], p, cs, ce, vis);
         if (lane_id() == 0) omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
     });
 }
@@ -527,7 +531,7 @@ __device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i,
 }
 
 __global__ void __launch_bounds__(128, 4)
-vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ vin,
+vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ vin,
                  float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
                  DeferList D) {
@@ -536,24 +540,24 @@ vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
     const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
     bool deferred = false;
-    walk_seq(P, i, vis.pi, p, cs, ce, vis, true, &deferred);
+    walk_seq(P, i, pa[i], p, cs, ce, vis, true, &deferred);
     if (deferred) {
         if (defer_particle(D, i)) return;
         vis.reset();
-        walk_seq(P, i, vis.pi, p, cs, ce, vis, false, &deferred);
+        walk_seq(P, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
     vort_visc_finish(P, i, vis, vout, fext);
 }
 
 __global__ void __launch_bounds__(128)
-vort_visc_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ vin,
+vort_visc_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ vin,
                       float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
                       const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
                       DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
         const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
-        walk_coop(P, i, vis.pi, p, cs, ce, vis);
+        walk_coop(P, i, pa[i], p, cs, ce, vis);
         if (lane_id() == 0) vort_visc_finish(P, i, vis, vout, fext);
     });
 }

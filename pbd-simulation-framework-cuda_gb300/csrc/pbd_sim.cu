@@ -6,9 +6,12 @@
 //    allocates, unlike the per-frame parameter upload of Initialize.h:71;
 //  - a frame is recorded once into a CUDA graph and replayed per pbd_step call; the graph is
 //    re-recorded only when N or the parameters change;
-//  - double-buffered arrays are addressed through a small "which buffer is current" record
-//    (Cur).  A frame flips some of them; when the flips do not cancel, two graphs are kept,
-//    one per starting parity, and replayed alternately.
+//  - multi-buffered arrays are addressed through a small "which buffer is current" record
+//    (Cur).  Predicted positions have three buffers: the frame's anchor (p* right after the
+//    re-order, which the neighbour cells are taken from for the whole frame, as the reference
+//    builds its list once per frame) and two the solver passes alternate between.  A frame
+//    moves the record through a short cycle; one graph is recorded per starting record and
+//    the graphs are replayed in turn.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -32,8 +35,8 @@ namespace {
 struct Cur {
     int x = 0, p = 0, v = 0;   // current buffer of positions (also colours, ids), predictions, velocities
     bool operator==(const Cur& o) const { return x == o.x && p == o.p && v == o.v; }
-    bool operator!=(const Cur& o) const { return !(*this == o); }
 };
+constexpr int kMaxGraphs = 8;
 
 constexpr int kThreadsParticle = 256;
 constexpr int kThreadsNeighbour = 128;
@@ -48,7 +51,7 @@ struct pbd_sim {
     uint32_t cap = 0, N = 0;
     int device = 0, num_sms = 0;
     void* arena = nullptr;
-    float4 *x[2]{}, *p[2]{}, *v[2]{}, *col[2]{};
+    float4 *x[2]{}, *p[3]{}, *v[2]{}, *col[2]{};
     uint32_t* ids[2]{};
     float4 *fext = nullptr, *omega = nullptr, *delta = nullptr;
     float* lambda = nullptr;
@@ -63,10 +66,10 @@ struct pbd_sim {
     uint32_t table_hint = 0;      // host upper bound of the device word table_n
     cudaStream_t last_stream = nullptr;
     cudaStream_t cap_stream = nullptr;
-    cudaGraphExec_t exec[2]{};
-    Cur exec_start[2];
+    cudaGraphExec_t exec[kMaxGraphs]{};
+    Cur exec_start[kMaxGraphs];
+    Cur exec_end[kMaxGraphs];
     int nexec = 0;
-    Cur flips;
     uint32_t graph_n = 0xFFFFFFFFu;
     bool dirty = true;
     uint32_t launches = 0;
@@ -200,16 +203,19 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     // copy + reorder + computeCellInfo
     const int fin = np % 2;
     const bool cols = (prm.flags & PBD_FLAG_COLORS) != 0, ids = (prm.flags & PBD_FLAG_TRACK_IDS) != 0;
+    const int anchor = (cur.p + 1) % 3;   // this frame's anchor: never written again in the frame
     ReorderArgs A{s->keys[fin], s->vals[fin], s->x[cur.x], s->p[cur.p], s->v[cur.v], s->col[cur.x],
-                  s->x[cur.x ^ 1], s->p[cur.p ^ 1], s->v[cur.v ^ 1], cols ? s->col[cur.x ^ 1] : nullptr,
+                  s->x[cur.x ^ 1], s->p[anchor], s->v[cur.v ^ 1], cols ? s->col[cur.x ^ 1] : nullptr,
                   s->ids[cur.x], ids ? s->ids[cur.x ^ 1] : nullptr, s->cell_start, s->cell_end, s->table_n};
     const uint32_t greo = std::max(div_up(N, kThreadsParticle), div_up((uint64_t)ntiles * kRadix, kThreadsParticle));
     PROF_BEGIN("reorder_cells");
     reorder_cells_kernel<<<std::max(1u, greo), kThreadsParticle, 0, st>>>(P, A, S, np, ntiles);
     PROF_END();
     ++nl;
-    cur.x ^= 1; cur.p ^= 1; cur.v ^= 1;
+    cur.x ^= 1; cur.p = anchor; cur.v ^= 1;
     if (front_only) return cudaGetLastError();
+    const float4* pa = s->p[anchor];
+    auto next_p = [&](int c) { return c == anchor ? (anchor + 1) % 3 : 3 - c - anchor; };
 
     const uint32_t gn = div_up(N, kThreadsNeighbour);
     const DeferList D{s->defer_items, s->defer_count, s->defer_done, s->defer_cap};
@@ -223,8 +229,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     for (uint32_t it = 0; it < I; ++it) {
         if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
             PROF_BEGIN("lambda");
-            lambda_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->cell_start, s->cell_end, s->lambda, D);
-            lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], s->cell_start, s->cell_end, s->lambda, D);
+            lambda_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, s->lambda, D);
+            lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, s->lambda, D);
             PROF_END();
             nl += 2;
             last_was_delta = false;
@@ -248,13 +254,14 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             const bool final_pass = last && (it + 1 == I);
             if (final_pass && do_update) mode |= kDoUpdate;
             PROF_BEGIN("delta");
-            delta_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, mode, s->p[cur.p], s->p[cur.p ^ 1], s->x[cur.x],
+            const int pout = next_p(cur.p);
+            delta_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
                                                             s->v[cur.v], s->lambda, s->delta, s->cell_start, s->cell_end, D);
-            delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], s->p[cur.p ^ 1], s->x[cur.x],
+            delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
                                                            s->v[cur.v], s->lambda, s->delta, s->cell_start, s->cell_end, D);
             PROF_END();
             nl += 2;
-            cur.p ^= 1;
+            cur.p = pout;
             last_was_delta = (mode & kDoUpdate) != 0;
         }
     }
@@ -266,17 +273,17 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     }
     if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
         PROF_BEGIN("omega");
-        omega_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
-        omega_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
+        omega_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
+        omega_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
         PROF_END();
         nl += 2;
     }
     const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     if (vort || visc) {
         PROF_BEGIN("vort_visc");
-        vort_visc_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->v[cur.v ^ 1], s->omega,
+        vort_visc_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
                                                             s->fext, s->cell_start, s->cell_end, vort, visc, D);
-        vort_visc_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->v[cur.v ^ 1], s->omega,
+        vort_visc_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
                                                            s->fext, s->cell_start, s->cell_end, vort, visc, D);
         PROF_END();
         nl += 2;
@@ -287,7 +294,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
 }
 
 void destroy_graphs(pbd_sim* s) {
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < kMaxGraphs; ++k)
         if (s->exec[k]) { cudaGraphExecDestroy(s->exec[k]); s->exec[k] = nullptr; }
     s->nexec = 0;
 }
@@ -321,26 +328,27 @@ int settle_tables(pbd_sim* s, cudaStream_t st) {
 
 int build_graphs(pbd_sim* s) {
     destroy_graphs(s);
-    Cur c0 = s->cur, c = c0;
+    Cur c = s->cur;
     uint32_t nl = 0;
-    int rc = capture_one(s, c, &s->exec[0], nl);
-    if (rc) return rc;
-    s->exec_start[0] = c0;
-    s->nexec = 1;
-    s->flips.x = c.x ^ c0.x; s->flips.p = c.p ^ c0.p; s->flips.v = c.v ^ c0.v;
-    if (c != c0) {
-        Cur c1 = c;
-        uint32_t nl1 = 0;
-        rc = capture_one(s, c, &s->exec[1], nl1);
+    // follow the cycle of starting records: frame k starts where frame k-1 ended
+    for (int k = 0; k < kMaxGraphs; ++k) {
+        const Cur start = c;
+        int rc = capture_one(s, c, &s->exec[k], nl);
         if (rc) return rc;
-        s->exec_start[1] = c1;
-        s->nexec = 2;
-        if (c != c0) { set_error("internal: frame buffer flips do not return to the start"); return PBD_ERR_CUDA; }
+        s->exec_start[k] = start;
+        s->exec_end[k] = c;
+        s->nexec = k + 1;
+        bool closed = false;
+        for (int j = 0; j <= k; ++j) closed = closed || (s->exec_start[j] == c);
+        if (closed) {
+            s->launches = nl;
+            s->graph_n = s->N;
+            s->dirty = false;
+            return PBD_OK;
+        }
     }
-    s->launches = nl;
-    s->graph_n = s->N;
-    s->dirty = false;
-    return PBD_OK;
+    set_error("internal: the frame's buffer records do not cycle");
+    return PBD_ERR_CUDA;
 }
 
 int check_sim(const pbd_sim* s, const char* fn) {
@@ -384,11 +392,12 @@ int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
     const size_t C = capacity, G = prm->max_grid;
     std::vector<std::pair<void**, size_t>> parts;
     for (int b = 0; b < 2; ++b) {
-        parts.push_back({(void**)&s->x[b], C * 16}); parts.push_back({(void**)&s->p[b], C * 16});
+        parts.push_back({(void**)&s->x[b], C * 16});
         parts.push_back({(void**)&s->v[b], C * 16}); parts.push_back({(void**)&s->col[b], C * 16});
         parts.push_back({(void**)&s->ids[b], C * 4});
         parts.push_back({(void**)&s->keys[b], C * 4}); parts.push_back({(void**)&s->vals[b], C * 4});
     }
+    for (int b = 0; b < 3; ++b) parts.push_back({(void**)&s->p[b], C * 16});
     parts.push_back({(void**)&s->fext, C * 16}); parts.push_back({(void**)&s->omega, C * 16});
     parts.push_back({(void**)&s->delta, C * 16}); parts.push_back({(void**)&s->lambda, C * 4});
     parts.push_back({(void**)&s->cell_start, G * 4}); parts.push_back({(void**)&s->cell_end, G * 4});
@@ -519,9 +528,15 @@ int pbd_step(pbd_sim* s, int nsteps, void* stream) {
         if (int rc = build_graphs(s)) return rc;
     }
     for (int k = 0; k < nsteps; ++k) {
-        const int g = (s->nexec == 2 && s->cur == s->exec_start[1]) ? 1 : 0;
+        int g = -1;
+        for (int j = 0; j < s->nexec; ++j)
+            if (s->exec_start[j] == s->cur) { g = j; break; }
+        if (g < 0) {   // state moved outside the recorded cycle (a debug front): record again
+            if (int rc = build_graphs(s)) return rc;
+            g = 0;
+        }
         CK(cudaGraphLaunch(s->exec[g], st));
-        s->cur.x ^= s->flips.x; s->cur.p ^= s->flips.p; s->cur.v ^= s->flips.v;
+        s->cur = s->exec_end[g];
     }
     s->table_hint = s->N;
     s->last_stream = st;

@@ -45,3 +45,26 @@ def setup_pair(pbd, oracle_mod, params, pos, vel, precision="f32", capacity=None
     orc = oracle_mod.Oracle(params, cap, precision)
     orc.add_particles(pos, vel)
     return sim, orc
+
+
+GOLDEN_DIR = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.abspath(__file__)), "golden")
+GOLDEN_SCENES = ("config_txt", "h1_quirk")
+
+
+def load_golden(pbd, name):
+    """Inputs and the reference's own outputs (tests/golden/make_golden.py)."""
+    import os
+    d = dict(np.load(os.path.join(GOLDEN_DIR, f"{name}.npz")))
+    d["params_struct"] = pbd.Params.from_buffer_copy(d["params"].tobytes())
+    return d
+
+
+def golden_lists(g):
+    """Per-particle lists from the flattened fixture."""
+    cnt = g["list_count"].astype(np.int64)
+    offs = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+    return [g["list_entries"][int(offs[i]):int(offs[i + 1])] for i in range(len(cnt))]
+
+
+def scale(a):
+    return max(1.0, float(np.max(np.abs(a))))
