@@ -138,7 +138,15 @@ int pbd_capacity(const pbd_sim* sim, uint32_t* cap);
  * returns silently).  Synchronous with respect to the host arrays. */
 int pbd_add_particles(pbd_sim* sim, uint32_t n, const float* pos4, const float* vel4,
                       const float* col4);
-/* Same, from device pointers (no host copy); queued on `stream`. */
+/* Same, with a per-particle inverse mass (unified solids).  The reference forces mass 1
+ * everywhere (Forces.h:75,94; Collision.h:223-224) while its collision code weighs the overlap
+ * by inverseMass1 / (inverseMass1 + inverseMass2) (Collision.h:225): here that weight uses the
+ * given inverse masses, a particle with inverse mass 0 (a solid) takes no gravity, external
+ * force, density correction or viscosity, and all particles added without this call have
+ * inverse mass 1 -- the reference's behaviour. */
+int pbd_add_particles_mass(pbd_sim* sim, uint32_t n, const float* pos4, const float* vel4,
+                           const float* col4, const float* inv_mass);
+/* Same as pbd_add_particles, from device pointers (no host copy); queued on `stream`. */
 int pbd_add_particles_device(pbd_sim* sim, uint32_t n, const float* d_pos4,
                              const float* d_vel4, const float* d_col4, void* stream);
 /* addParticleCallback: one particle at pos with velocity 50*dir, w = 0. */

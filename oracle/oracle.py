@@ -27,6 +27,7 @@ def _lib(precision):
         lib.orc_set_params.argtypes = [vp, vp]
         lib.orc_add_particles.argtypes = [vp, u32, f32p, f32p, f32p]
         lib.orc_add_particle.argtypes = [vp, f32p, f32p]
+        lib.orc_add_particles_mass.argtypes = [vp, u32, f32p, f32p, f32p, f32p]
         lib.orc_clear.argtypes = [vp]
         lib.orc_step.argtypes = [vp, i32]
         lib.orc_step_phase.argtypes = [vp, i32]
@@ -95,6 +96,14 @@ class Oracle:
         vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
         col4 = None if col4 is None else np.ascontiguousarray(col4, dtype=np.float32)
         return self.lib.orc_add_particles(self.h, pos4.shape[0], _ptr(pos4, C.c_float), _ptr(vel4, C.c_float), _ptr(col4, C.c_float))
+
+    def add_particles_mass(self, pos4, vel4, inv_mass, col4=None):
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
+        w = np.ascontiguousarray(inv_mass, dtype=np.float32)
+        col4 = None if col4 is None else np.ascontiguousarray(col4, dtype=np.float32)
+        return self.lib.orc_add_particles_mass(self.h, pos4.shape[0], _ptr(pos4, C.c_float), _ptr(vel4, C.c_float),
+                                               _ptr(col4, C.c_float), _ptr(w, C.c_float))
 
     def add_particle(self, pos, direction):
         p = np.ascontiguousarray(pos, dtype=np.float32)

@@ -87,6 +87,8 @@ typedef struct orc_sim {
     r4 *x, *p, *v, *col, *fext, *delta, *omega;
     r4 *xc, *pc, *vc, *colc;    /* copies for the gather re-order */
     real *lambda;
+    real *w, *wc;               /* inverse masses (unified solids; 1 = the reference) */
+    int mass_used;
     uint32_t *ids, *idsc;
     uint32_t *keys_in, *keys_out, *vals_in, *vals_out, *tmpk, *tmpv;
     uint32_t *cell_start, *cell_end;
@@ -181,6 +183,8 @@ orc_sim* orc_create(const pbd_params* prm, uint32_t capacity) {
     s->xc = zalloc(c * sizeof(r4)); s->pc = zalloc(c * sizeof(r4)); s->vc = zalloc(c * sizeof(r4));
     s->colc = zalloc(c * sizeof(r4));
     s->lambda = zalloc(c * sizeof(real));
+    s->w = zalloc(c * sizeof(real)); s->wc = zalloc(c * sizeof(real));
+    for (size_t k = 0; k < c; ++k) s->w[k] = 1;
     s->ids = zalloc(c * 4); s->idsc = zalloc(c * 4);
     s->keys_in = zalloc(c * 4); s->keys_out = zalloc(c * 4); s->vals_in = zalloc(c * 4);
     s->vals_out = zalloc(c * 4); s->tmpk = zalloc(c * 4); s->tmpv = zalloc(c * 4);
@@ -196,7 +200,7 @@ orc_sim* orc_create(const pbd_params* prm, uint32_t capacity) {
 void orc_destroy(orc_sim* s) {
     if (!s) return;
     void* bufs[] = {s->x, s->p, s->v, s->col, s->fext, s->delta, s->omega, s->xc, s->pc, s->vc, s->colc,
-                    s->lambda, s->ids, s->idsc, s->keys_in, s->keys_out, s->vals_in, s->vals_out,
+                    s->lambda, s->w, s->wc, s->ids, s->idsc, s->keys_in, s->keys_out, s->vals_in, s->vals_out,
                     s->tmpk, s->tmpv, s->cell_start, s->cell_end, s->nbr, s->nbr_count, s->contact_count};
     for (size_t k = 0; k < sizeof(bufs) / sizeof(bufs[0]); ++k) free(bufs[k]);
     free(s);
@@ -228,8 +232,18 @@ int orc_max_threads(void) {
 }
 
 /* --------------------------------------------- Communication.h:22-67, 626-660 ------ */
+int orc_add_particles_mass(orc_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4,
+                           const float* inv_mass);
 int orc_add_particles(orc_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4) {
+    return orc_add_particles_mass(s, n, pos4, vel4, col4, NULL);
+}
+
+/* Unified solids: inverse mass per particle (1 for everything added without it). */
+int orc_add_particles_mass(orc_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4,
+                           const float* inv_mass) {
     if ((uint64_t)s->N + n > s->cap) return PBD_ERR_CAPACITY;   /* :645 (silent there) */
+    if (inv_mass) s->mass_used = 1;
+    for (uint32_t k = 0; k < n; ++k) s->w[s->N + k] = inv_mass ? (real)inv_mass[k] : (real)1;
     for (uint32_t k = 0; k < n; ++k) {
         uint32_t i = s->N + k;
         s->x[i] = mk4(pos4[4 * k], pos4[4 * k + 1], pos4[4 * k + 2], pos4[4 * k + 3]);
@@ -248,6 +262,7 @@ int orc_add_particle(orc_sim* s, const float pos[3], const float dir[3]) {
     s->v[i] = mk4(50.0f * dir[0], 50.0f * dir[1], 50.0f * dir[2], 0);   /* :27 */
     s->col[i] = mk4(1, 0, 0, 1);
     s->ids[i] = i;
+    s->w[i] = 1;
     s->N += 1;
     return PBD_OK;
 }
@@ -266,10 +281,12 @@ static void apply_forces(orc_sim* s) {
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < N; ++i) {
         r4 v = s->v[i];
-        v.y = FMA(g, dt, v.y);                        /* velocity.y += inverseMass*gravity*deltaT */
-        r4 f = s->fext[i];
-        v.x = FMA(f.x, dt, v.x); v.y = FMA(f.y, dt, v.y);
-        v.z = FMA(f.z, dt, v.z); v.w = FMA(f.w, dt, v.w);  /* velocity += externalForces*deltaT */
+        if (s->w[i] != 0) {                           /* solids (inverse mass 0) take no forces */
+            v.y = FMA(g, dt, v.y);                    /* velocity.y += inverseMass*gravity*deltaT */
+            r4 f = s->fext[i];
+            v.x = FMA(f.x, dt, v.x); v.y = FMA(f.y, dt, v.y);
+            v.z = FMA(f.z, dt, v.z); v.w = FMA(f.w, dt, v.w);  /* velocity += externalForces*deltaT */
+        }
         r4 x = s->x[i];
         r4 p = mk4(FMA(v.x, dt, x.x), FMA(v.y, dt, x.y), FMA(v.z, dt, x.z), FMA(v.w, dt, x.w));
         int upd = 0;
@@ -327,11 +344,13 @@ static void reorder(orc_sim* s) {          /* copy (:53-75) + reorder (:86-115) 
     memcpy(s->xc, s->x, N * sizeof(r4)); memcpy(s->pc, s->p, N * sizeof(r4));
     memcpy(s->vc, s->v, N * sizeof(r4)); memcpy(s->colc, s->col, N * sizeof(r4));
     memcpy(s->idsc, s->ids, N * 4u);
+    memcpy(s->wc, s->w, N * sizeof(real));
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < N; ++i) {
         uint32_t o = s->vals_out[i];
         s->x[i] = s->xc[o]; s->p[i] = s->pc[o]; s->v[i] = s->vc[o]; s->col[i] = s->colc[o];
         s->ids[i] = s->idsc[o];
+        s->w[i] = s->wc[o];
     }
 }
 
@@ -473,7 +492,7 @@ static void compute_delta_positions(orc_sim* s) {
 static void apply_delta_positions(orc_sim* s) {
     const int N = (int)s->N;
 #pragma omp parallel for schedule(static)
-    for (int i = 0; i < N; ++i) s->p[i] = sub4(s->p[i], s->delta[i]);
+    for (int i = 0; i < N; ++i) s->p[i] = sub4(s->p[i], s->mass_used ? scl4(s->w[i], s->delta[i]) : s->delta[i]);
 }
 
 /* --------------------------------------------------- Collision.h:171-242 (Jacobi) --- */
@@ -491,11 +510,17 @@ static void solve_collisions(orc_sim* s) {
             r4 dir = sub4(p2, p1);
             real len = len3(dir);
             real overlap = d - len;
+            real share = (real)0.5;   /* inverseMass1 / (inverseMass1 + inverseMass2), Collision.h:223-225 */
+            if (s->mass_used) {
+                const real wi = s->w[i], wj = s->w[list[kk]];
+                share = (wi + wj) > 0 ? wi / (wi + wj) : 0;
+                if (share == 0) continue;
+            }
             if (overlap > 0) {
                 if (len <= (real)0.00001f) continue;
                 real nx = dir.x / len, ny = dir.y / len, nz = dir.z / len;
                 /* -1.0 * inverseMass * overlap is evaluated in double (Collision.h:227) */
-                real sc = ORC_IS_F32 ? (real)(float)(-1.0 * 0.5 * (double)overlap) : (real)(-0.5) * overlap;
+                real sc = ORC_IS_F32 ? (real)(float)(-1.0 * (double)share * (double)overlap) : -share * overlap;
                 real one_m = (real)1 - st;
                 real ax = sc * nx * one_m, ay = sc * ny * one_m, az = sc * nz * one_m;
                 pa.x += ax; xa.x += ax;
@@ -581,7 +606,7 @@ static void compute_viscosity(orc_sim* s) {
             r4 vij = sub4(s->vc[j], vi);
             sum = add4(sum, scl4(poly6(s, len3(sub4(pi, s->p[j]))), vij));
         }
-        s->v[i] = add4(vi, scl4(c, sum));
+        s->v[i] = add4(vi, scl4(s->mass_used ? s->w[i] * c : c, sum));
     }
 }
 

@@ -30,7 +30,7 @@ namespace pbd {
 // --------------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)
 predict_key_kernel(DevParams P, float4* __restrict__ x, float4* __restrict__ v, float4* __restrict__ p,
-                   const float4* __restrict__ fext, uint32_t* keys, const uint32_t* old_keys,
+                   const float4* __restrict__ fext, const float* __restrict__ w, uint32_t* keys, const uint32_t* old_keys,
                    const uint32_t* __restrict__ table_n, uint32_t* __restrict__ cell_start,
                    uint32_t* __restrict__ hist, int npasses, uint32_t* __restrict__ err) {
     __shared__ uint32_t sh[kMaxPasses * kRadix];
@@ -49,14 +49,16 @@ predict_key_kernel(DevParams P, float4* __restrict__ x, float4* __restrict__ v, 
         float4 pp;
         if (forces) {
             float4 vv = v[i];
-            const float4 f = fext[i];
             float4 xx = x[i];
             const float dt = P.dt;
-            vv.y = __fmaf_rn(P.gravity, dt, vv.y);
-            vv.x = __fmaf_rn(f.x, dt, vv.x);
-            vv.y = __fmaf_rn(f.y, dt, vv.y);
-            vv.z = __fmaf_rn(f.z, dt, vv.z);
-            vv.w = __fmaf_rn(f.w, dt, vv.w);
+            if (!w || w[i] != 0.0f) {           // solids (inverse mass 0) take no forces
+                const float4 f = fext[i];
+                vv.y = __fmaf_rn(P.gravity, dt, vv.y);
+                vv.x = __fmaf_rn(f.x, dt, vv.x);
+                vv.y = __fmaf_rn(f.y, dt, vv.y);
+                vv.z = __fmaf_rn(f.z, dt, vv.z);
+                vv.w = __fmaf_rn(f.w, dt, vv.w);
+            }
             pp = make_float4(__fmaf_rn(vv.x, dt, xx.x), __fmaf_rn(vv.y, dt, xx.y),
                              __fmaf_rn(vv.z, dt, xx.z), __fmaf_rn(vv.w, dt, xx.w));
             bool upd = false;
@@ -102,6 +104,8 @@ struct ReorderArgs {
     float4 *xo, *po, *vo, *co;
     const uint32_t* idi;
     uint32_t* ido;
+    const float* wi;         // inverse masses (solids), or null
+    float* wo;
     uint32_t* cell_start;
     uint32_t* cell_end;
     uint32_t* table_n;       // set to N: the cells of these sorted keys are now in the tables
@@ -128,6 +132,7 @@ reorder_cells_kernel(DevParams P, ReorderArgs A, SortScratch S, int npasses, uin
         A.vo[i] = A.vi[o];
         if (A.co) A.co[i] = A.ci[o];
         if (A.ido) A.ido[i] = A.idi[o];
+        if (A.wo) A.wo[i] = A.wi[o];
         const uint32_t k = A.skeys[i];
         if (k < P.G) {
             if (i == 0 || A.skeys[i - 1] != k) A.cell_start[k] = i;
@@ -146,13 +151,22 @@ __global__ void clear_cells_kernel(const uint32_t* __restrict__ old_keys, const 
     }
 }
 
-__global__ void fill_ids_kernel(uint32_t* ids, uint32_t first, uint32_t n) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < n) ids[first + k] = first + k;
+__global__ void fill_float_kernel(float* a, float value, uint32_t n) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) a[k] = value;
 }
 
-__global__ void add_one_kernel(float4* x, float4* v, float4* col, uint32_t* ids, uint32_t at,
+// New particles: ids first..first+n-1 and inverse mass 1 unless given.
+__global__ void fill_new_kernel(uint32_t* ids, float* w, int keep_w, uint32_t first, uint32_t n) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) {
+        ids[first + k] = first + k;
+        if (!keep_w) w[first + k] = 1.0f;
+    }
+}
+
+__global__ void add_one_kernel(float4* x, float4* v, float4* col, uint32_t* ids, float* w, uint32_t at,
                                float px, float py, float pz, float dx, float dy, float dz) {
+    w[at] = 1.0f;
     x[at] = make_float4(px, py, pz, 0.0f);
     v[at] = make_float4(50.0f * dx, 50.0f * dy, 50.0f * dz, 0.0f);   // Communication.h:27
     if (col) col[at] = make_float4(1.0f, 0.0f, 0.0f, 1.0f);

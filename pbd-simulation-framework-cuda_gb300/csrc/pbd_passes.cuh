@@ -270,15 +270,17 @@ struct DeltaVisit {
     struct Contrib { float ax, ay, az, aw, cx, cy, cz; uint32_t flags; };   // flags: 1 delta part, 2 contact part
     const DevParams& P;
     const float* __restrict__ lambda;
+    const float* __restrict__ w;       // inverse masses, or null (all 1, the reference)
     float4 pi;
-    float li;
+    float li, wi;
     bool do_delta, do_collide, all_pairs;
     float ax = 0.f, ay = 0.f, az = 0.f, aw = 0.f;   // sum of (li + lj + sCorr) * grad
     float4 pacc, xacc;                               // positions with the contact corrections added in order
     float4 xi;
-    __device__ DeltaVisit(const DevParams& P_, const float* lam, float4 pi_, float li_, bool dd, bool dc, float4 xi_)
-        : P(P_), lambda(lam), pi(pi_), li(li_), do_delta(dd), do_collide(dc), all_pairs(P_.far_pairs_zero == 0u),
-          pacc(pi_), xacc(xi_), xi(xi_) {}
+    __device__ DeltaVisit(const DevParams& P_, const float* lam, const float* w_, float4 pi_, float li_, float wi_,
+                          bool dd, bool dc, float4 xi_)
+        : P(P_), lambda(lam), w(w_), pi(pi_), li(li_), wi(wi_), do_delta(dd), do_collide(dc),
+          all_pairs(P_.far_pairs_zero == 0u), pacc(pi_), xacc(xi_), xi(xi_) {}
     __device__ void reset() { ax = ay = az = aw = 0.f; pacc = pi; xacc = xi; }
     __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u}; }
     __device__ static bool effective(const Contrib& c) { return c.flags != 0u; }
@@ -305,8 +307,15 @@ struct DeltaVisit {
         }
         if (contact && do_collide) {
             const float overlap = P.d - dist;
-            if (overlap > 0.0f && dist > 0.00001f) {
-                const float sc = -0.5f * overlap;
+            // share of the overlap this particle takes: inverseMass1 / (inverseMass1 + inverseMass2)
+            // (Collision.h:223-225, where both are forced to 1); solids have inverse mass 0
+            float share = 0.5f;
+            if (w) {
+                const float wj = __ldg(w + j);
+                share = (wi + wj) > 0.0f ? wi / (wi + wj) : 0.0f;
+            }
+            if (overlap > 0.0f && dist > 0.00001f && share != 0.0f) {
+                const float sc = -share * overlap;
                 const float inv = 1.0f / dist;      // dir / len with one reciprocal
                 c.cx = (sc * (-rx * inv)) * P.one_minus_stiffness;
                 c.cy = (sc * (-ry * inv)) * P.one_minus_stiffness;
@@ -329,12 +338,16 @@ struct DeltaVisit {
 __device__ __forceinline__ void delta_finish(const DevParams& P, uint32_t mode, uint32_t i, const DeltaVisit& vis,
                                              float4* __restrict__ pout, float4* __restrict__ x, float4* __restrict__ v,
                                              float4* __restrict__ delta) {
+    // a solid (inverse mass 0) takes no density correction
     float4 pn = vis.pacc, xn = vis.xacc;
     float4 dp = make_float4(0.f, 0.f, 0.f, 0.f);
     if (mode & kDoDelta) dp = make_float4(vis.ax / P.rho0, vis.ay / P.rho0, vis.az / P.rho0, vis.aw / P.rho0);
     else if (mode & kLoadDelta) dp = delta[i];
     if (mode & kStoreDelta) delta[i] = dp;
-    if (mode & kDoApply) { pn.x -= dp.x; pn.y -= dp.y; pn.z -= dp.z; pn.w -= dp.w; }
+    if (mode & kDoApply) {
+        if (vis.w) { dp.x *= vis.wi; dp.y *= vis.wi; dp.z *= vis.wi; dp.w *= vis.wi; }
+        pn.x -= dp.x; pn.y -= dp.y; pn.z -= dp.z; pn.w -= dp.w;
+    }
     if (mode & kDoUpdate) {
         const float r = P.inv_dt;
         v[i] = make_float4((pn.x - xn.x) * r, (pn.y - xn.y) * r, (pn.z - xn.z) * r, (pn.w - xn.w) * r);
@@ -346,7 +359,7 @@ __device__ __forceinline__ void delta_finish(const DevParams& P, uint32_t mode, 
 
 __global__ void __launch_bounds__(128, 4)
 delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const float4* __restrict__ pa, float4* __restrict__ pout,
-             float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
+             float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda, const float* __restrict__ w,
              float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
              DeferList D) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -355,7 +368,7 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const f
     const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
     const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
-    DeltaVisit vis(P, lambda, pi, li, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
+    DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
     if (mode & (kDoDelta | kDoCollide)) {
         bool deferred = false;
         walk_seq(P, i, pa[i], pin, cs, ce, vis, true, &deferred);
@@ -370,7 +383,7 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const f
 
 __global__ void __launch_bounds__(128)
 delta_coop_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const float4* __restrict__ pa, float4* __restrict__ pout,
-                  float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
+                  float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda, const float* __restrict__ w,
                   float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
                   DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
@@ -378,7 +391,7 @@ delta_coop_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, co
         const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
         const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
-        DeltaVisit vis(P, lambda, pi, li, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
+        DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
         walk_coop(P, i, pa[i], pin, cs, ce, vis);
         if (lane_id() == 0) delta_finish(P, mode, i, vis, pout, x, v, delta);
     });
@@ -513,7 +526,8 @@ struct VortViscVisit {
 };
 
 __device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i, const VortViscVisit& vis,
-                                                 float4* __restrict__ vout, float4* __restrict__ fext) {
+                                                 float4* __restrict__ vout, float4* __restrict__ fext,
+                                                 const float* __restrict__ w) {
     if (vis.vort) {
         const float EPS = 0.00000001f;
         const float gl = sqrtf(vis.gx * vis.gx + vis.gy * vis.gy + vis.gz * vis.gz);
@@ -524,7 +538,7 @@ __device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i,
         fext[i] = make_float4(e * (ny * oi.z - nz * oi.y), e * (nz * oi.x - nx * oi.z), e * (nx * oi.y - ny * oi.x), 0.f);
     }
     if (vis.visc) {
-        const float c = P.c_visc;
+        const float c = w ? w[i] * P.c_visc : P.c_visc;   // a solid keeps its velocity
         const float4 vi = vis.vi;
         vout[i] = make_float4(vi.x + c * vis.sx, vi.y + c * vis.sy, vi.z + c * vis.sz, vi.w + c * vis.sw);
     }
@@ -534,7 +548,7 @@ __global__ void __launch_bounds__(128, 4)
 vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ vin,
                  float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
-                 DeferList D) {
+                 const float* __restrict__ w, DeferList D) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -546,19 +560,19 @@ vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
         vis.reset();
         walk_seq(P, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
-    vort_visc_finish(P, i, vis, vout, fext);
+    vort_visc_finish(P, i, vis, vout, fext, w);
 }
 
 __global__ void __launch_bounds__(128)
 vort_visc_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ vin,
                       float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
                       const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
-                      DeferList D) {
+                      const float* __restrict__ w, DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
         const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
         walk_coop(P, i, pa[i], p, cs, ce, vis);
-        if (lane_id() == 0) vort_visc_finish(P, i, vis, vout, fext);
+        if (lane_id() == 0) vort_visc_finish(P, i, vis, vout, fext, w);
     });
 }
 

@@ -53,6 +53,8 @@ struct pbd_sim {
     void* arena = nullptr;
     float4 *x[2]{}, *p[3]{}, *v[2]{}, *col[2]{};
     uint32_t* ids[2]{};
+    float* w[2]{};                // inverse masses (solids = 0), carried through re-orders once used
+    bool mass_used = false;
     float4 *fext = nullptr, *omega = nullptr, *delta = nullptr;
     float* lambda = nullptr;
     uint32_t *keys[2]{}, *vals[2]{};
@@ -183,7 +185,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const uint32_t total = std::max(N, s->table_hint);
     const uint32_t gpred = std::max(1u, std::min(div_up(total, kThreadsParticle), (uint32_t)s->num_sms * 8u));
     PROF_BEGIN("predict_key");
-    predict_key_kernel<<<gpred, kThreadsParticle, 0, st>>>(P, s->x[cur.x], s->v[cur.v], s->p[cur.p], s->fext,
+    const float* wcur = s->mass_used ? s->w[cur.x] : nullptr;
+    predict_key_kernel<<<gpred, kThreadsParticle, 0, st>>>(P, s->x[cur.x], s->v[cur.v], s->p[cur.p], s->fext, wcur,
                                                            s->keys[0], s->keys[np % 2], s->table_n, s->cell_start,
                                                            s->hist, np, s->err);
     PROF_END();
@@ -206,7 +209,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const int anchor = (cur.p + 1) % 3;   // this frame's anchor: never written again in the frame
     ReorderArgs A{s->keys[fin], s->vals[fin], s->x[cur.x], s->p[cur.p], s->v[cur.v], s->col[cur.x],
                   s->x[cur.x ^ 1], s->p[anchor], s->v[cur.v ^ 1], cols ? s->col[cur.x ^ 1] : nullptr,
-                  s->ids[cur.x], ids ? s->ids[cur.x ^ 1] : nullptr, s->cell_start, s->cell_end, s->table_n};
+                  s->ids[cur.x], ids ? s->ids[cur.x ^ 1] : nullptr, s->w[cur.x], s->mass_used ? s->w[cur.x ^ 1] : nullptr,
+                  s->cell_start, s->cell_end, s->table_n};
     const uint32_t greo = std::max(div_up(N, kThreadsParticle), div_up((uint64_t)ntiles * kRadix, kThreadsParticle));
     PROF_BEGIN("reorder_cells");
     reorder_cells_kernel<<<std::max(1u, greo), kThreadsParticle, 0, st>>>(P, A, S, np, ntiles);
@@ -215,6 +219,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     cur.x ^= 1; cur.p = anchor; cur.v ^= 1;
     if (front_only) return cudaGetLastError();
     const float4* pa = s->p[anchor];
+    const float* wf = s->mass_used ? s->w[cur.x] : nullptr;   // after the re-order
     auto next_p = [&](int c) { return c == anchor ? (anchor + 1) % 3 : 3 - c - anchor; };
 
     const uint32_t gn = div_up(N, kThreadsNeighbour);
@@ -256,9 +261,9 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             PROF_BEGIN("delta");
             const int pout = next_p(cur.p);
             delta_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
-                                                            s->v[cur.v], s->lambda, s->delta, s->cell_start, s->cell_end, D);
+                                                            s->v[cur.v], s->lambda, wf, s->delta, s->cell_start, s->cell_end, D);
             delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
-                                                           s->v[cur.v], s->lambda, s->delta, s->cell_start, s->cell_end, D);
+                                                           s->v[cur.v], s->lambda, wf, s->delta, s->cell_start, s->cell_end, D);
             PROF_END();
             nl += 2;
             cur.p = pout;
@@ -282,9 +287,9 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     if (vort || visc) {
         PROF_BEGIN("vort_visc");
         vort_visc_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
-                                                            s->fext, s->cell_start, s->cell_end, vort, visc, D);
+                                                            s->fext, s->cell_start, s->cell_end, vort, visc, wf, D);
         vort_visc_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
-                                                           s->fext, s->cell_start, s->cell_end, vort, visc, D);
+                                                           s->fext, s->cell_start, s->cell_end, vort, visc, wf, D);
         PROF_END();
         nl += 2;
         if (visc) cur.v ^= 1;
@@ -394,7 +399,7 @@ int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
     for (int b = 0; b < 2; ++b) {
         parts.push_back({(void**)&s->x[b], C * 16});
         parts.push_back({(void**)&s->v[b], C * 16}); parts.push_back({(void**)&s->col[b], C * 16});
-        parts.push_back({(void**)&s->ids[b], C * 4});
+        parts.push_back({(void**)&s->ids[b], C * 4}); parts.push_back({(void**)&s->w[b], C * 4});
         parts.push_back({(void**)&s->keys[b], C * 4}); parts.push_back({(void**)&s->vals[b], C * 4});
     }
     for (int b = 0; b < 3; ++b) parts.push_back({(void**)&s->p[b], C * 16});
@@ -416,6 +421,10 @@ int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
     for (auto& pt : parts) { *pt.first = cur; cur += (pt.second + 255) & ~size_t(255); }
     e = cudaMemset(s->arena, 0, total);
     if (e == cudaSuccess) e = cudaMemset(s->cell_start, 0xFF, G * 4);   // all cells empty
+    if (e == cudaSuccess) {                                               // inverse mass 1 everywhere
+        for (int b = 0; b < 2; ++b) fill_float_kernel<<<256, 256>>>(s->w[b], 1.0f, capacity);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) { cudaFree(s->arena); delete s; return cuda_fail("pbd_create init", e); }
@@ -466,7 +475,7 @@ int pbd_capacity(const pbd_sim* s, uint32_t* c) {
 }
 
 static int add_common(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4,
-                      cudaMemcpyKind kind, cudaStream_t st, bool sync) {
+                      const float* inv_mass, cudaMemcpyKind kind, cudaStream_t st, bool sync) {
     if (int rc = check_sim(s, "pbd_add_particles")) return rc;
     if (n == 0) return PBD_OK;
     if (!pos4 || !vel4) { set_error("pbd_add_particles: null position or velocity array"); return PBD_ERR_INVALID_ARG; }
@@ -478,7 +487,11 @@ static int add_common(pbd_sim* s, uint32_t n, const float* pos4, const float* ve
     CK(cudaMemcpyAsync(s->x[s->cur.x] + off, pos4, bytes, kind, st));
     CK(cudaMemcpyAsync(s->v[s->cur.v] + off, vel4, bytes, kind, st));
     if (col4) CK(cudaMemcpyAsync(s->col[s->cur.x] + off, col4, bytes, kind, st));
-    fill_ids_kernel<<<div_up(n, 256), 256, 0, st>>>(s->ids[s->cur.x], s->N, n);
+    if (inv_mass) {
+        CK(cudaMemcpyAsync(s->w[s->cur.x] + off, inv_mass, (size_t)n * 4, kind, st));
+        if (!s->mass_used) { s->mass_used = true; s->dirty = true; }   // all earlier masses are 1: order-free
+    }
+    fill_new_kernel<<<div_up(n, 256), 256, 0, st>>>(s->ids[s->cur.x], s->w[s->cur.x], inv_mass != nullptr, s->N, n);
     CK(cudaGetLastError());
     if (sync) CK(cudaStreamSynchronize(st));
     s->N += n;
@@ -489,12 +502,25 @@ static int add_common(pbd_sim* s, uint32_t n, const float* pos4, const float* ve
 int pbd_add_particles(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4) {
     clear_error();
     if (int rc = check_sim(s, "pbd_add_particles")) return rc;
-    return add_common(s, n, pos4, vel4, col4, cudaMemcpyHostToDevice, s->last_stream, true);
+    return add_common(s, n, pos4, vel4, col4, nullptr, cudaMemcpyHostToDevice, s->last_stream, true);
+}
+
+int pbd_add_particles_mass(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4,
+                           const float* inv_mass) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_add_particles_mass")) return rc;
+    if (!inv_mass) { set_error("pbd_add_particles_mass: null inverse-mass array"); return PBD_ERR_INVALID_ARG; }
+    for (uint32_t k = 0; k < n; ++k)
+        if (!(inv_mass[k] >= 0.0f) || !std::isfinite(inv_mass[k])) {
+            set_error("pbd_add_particles_mass: inverse masses must be finite and >= 0");
+            return PBD_ERR_RANGE;
+        }
+    return add_common(s, n, pos4, vel4, col4, inv_mass, cudaMemcpyHostToDevice, s->last_stream, true);
 }
 
 int pbd_add_particles_device(pbd_sim* s, uint32_t n, const float* d_pos4, const float* d_vel4, const float* d_col4, void* stream) {
     clear_error();
-    return add_common(s, n, d_pos4, d_vel4, d_col4, cudaMemcpyDeviceToDevice, (cudaStream_t)stream, false);
+    return add_common(s, n, d_pos4, d_vel4, d_col4, nullptr, cudaMemcpyDeviceToDevice, (cudaStream_t)stream, false);
 }
 
 int pbd_add_particle(pbd_sim* s, const float pos[3], const float dir[3]) {
@@ -502,7 +528,8 @@ int pbd_add_particle(pbd_sim* s, const float pos[3], const float dir[3]) {
     if (int rc = check_sim(s, "pbd_add_particle")) return rc;
     if (!pos || !dir) { set_error("pbd_add_particle: null"); return PBD_ERR_INVALID_ARG; }
     if ((uint64_t)s->N + 1 > s->cap) { set_error("pbd_add_particle: capacity reached"); return PBD_ERR_CAPACITY; }
-    add_one_kernel<<<1, 1, 0, s->last_stream>>>(s->x[s->cur.x], s->v[s->cur.v], s->col[s->cur.x], s->ids[s->cur.x], s->N,
+    add_one_kernel<<<1, 1, 0, s->last_stream>>>(s->x[s->cur.x], s->v[s->cur.v], s->col[s->cur.x], s->ids[s->cur.x],
+                                                 s->w[s->cur.x], s->N,
                                                  pos[0], pos[1], pos[2], dir[0], dir[1], dir[2]);
     CK(cudaGetLastError());
     s->N += 1;

@@ -25,7 +25,7 @@ FLAG_CELL_END_QUIRK, FLAG_TRACK_IDS, FLAG_COLORS = 1, 2, 4
 EXPORTED = [
     "pbd_params_default", "pbd_load_config", "pbd_parse_config", "pbd_write_config", "pbd_validate_params",
     "pbd_create", "pbd_destroy", "pbd_set_params", "pbd_get_params", "pbd_num_particles", "pbd_capacity",
-    "pbd_add_particles", "pbd_add_particles_device", "pbd_add_particle", "pbd_clear", "pbd_step", "pbd_sync",
+    "pbd_add_particles", "pbd_add_particles_mass", "pbd_add_particles_device", "pbd_add_particle", "pbd_clear", "pbd_step", "pbd_sync",
     "pbd_get_state", "pbd_get_device_state", "pbd_debug_dump", "pbd_debug_neighbours", "pbd_debug_front",
     "pbd_launches_per_step", "pbd_profile_frames", "pbd_sort_keys_noalloc", "pbd_last_error", "pbd_abi_version",
 ]
@@ -88,6 +88,7 @@ def lib():
             "pbd_create": [P, u32, C.POINTER(vp)], "pbd_destroy": [vp], "pbd_set_params": [vp, P],
             "pbd_get_params": [vp, P], "pbd_num_particles": [vp, u32p], "pbd_capacity": [vp, u32p],
             "pbd_add_particles": [vp, u32, fp, fp, fp], "pbd_add_particles_device": [vp, u32, vp, vp, vp, vp],
+            "pbd_add_particles_mass": [vp, u32, fp, fp, fp, fp],
             "pbd_add_particle": [vp, fp, fp], "pbd_clear": [vp], "pbd_step": [vp, i32, vp], "pbd_sync": [vp],
             "pbd_get_state": [vp, fp, fp, fp, u32p], "pbd_get_device_state": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)],
             "pbd_debug_dump": [vp, u32p, u32p, u32p, u32p, u32, fp, fp, fp],
@@ -185,6 +186,13 @@ class Sim:
         vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
         col4 = None if col4 is None else np.ascontiguousarray(col4, dtype=np.float32)
         check(self.L.pbd_add_particles(self.h, pos4.shape[0], _fp(pos4), _fp(vel4), _fp(col4)))
+
+    def add_particles_mass(self, pos4, vel4, inv_mass, col4=None):
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
+        w = np.ascontiguousarray(inv_mass, dtype=np.float32)
+        col4 = None if col4 is None else np.ascontiguousarray(col4, dtype=np.float32)
+        check(self.L.pbd_add_particles_mass(self.h, pos4.shape[0], _fp(pos4), _fp(vel4), _fp(col4), _fp(w)))
 
     def add_particle(self, pos, direction):
         p = np.ascontiguousarray(pos, dtype=np.float32)

@@ -8,6 +8,8 @@ jittered by SplitMix64 (Vigna's published 64-bit mixer, restated below), so ever
 Workloads (kernel radius h = 1 = particle diameter, dt = 1/60, 4 solver iterations):
   dam_break_32k   32^3 fluid particles in a 64^3-cell box, seed 1
   fluid_1m        100^3 fluid particles in a 128^3-cell domain, vorticity 5e-4, XSPH 0.01, seed 2
+  solids_328k     64^3 fluid particles + 8 static solid boxes of 8,192 particles (inverse mass 0)
+                  in a 128^3-cell domain, seed 3
 """
 import numpy as np
 
@@ -74,7 +76,47 @@ def workload_params(pbd, box, rest_density, vorticity=0.0, viscosity=0.0, iterat
     return p
 
 
+def solid_boxes(n_boxes, box_shape, region_min, region_max, seed):
+    """Static solid boxes on the floor: unit-spacing lattices of `box_shape` cells, placed at
+    seeded cell-aligned offsets inside [region_min, region_max) on a grid that keeps them apart."""
+    bx, by, bz = box_shape
+    nx = max(1, int((region_max[0] - region_min[0]) // (bx + 2)))
+    nz = max(1, int((region_max[2] - region_min[2]) // (bz + 2)))
+    slots = [(a, c) for a in range(nx) for c in range(nz)]
+    u = uniform01(seed, 4 * len(slots))
+    order = np.argsort(u[: len(slots)], kind="stable")
+    if n_boxes > len(slots):
+        raise ValueError("solid boxes do not fit the region")
+    pos = []
+    for k in range(n_boxes):
+        a, c = slots[order[k]]
+        sx = int(u[len(slots) + k] * ((region_max[0] - region_min[0]) / nx - bx - 1))
+        sz = int(u[2 * len(slots) + k] * ((region_max[2] - region_min[2]) / nz - bz - 1))
+        ox = region_min[0] + a * (region_max[0] - region_min[0]) / nx + sx
+        oz = region_min[2] + c * (region_max[2] - region_min[2]) / nz + sz
+        i, j, l = np.meshgrid(np.arange(bx), np.arange(by), np.arange(bz), indexing="ij")
+        b = np.stack([i.ravel() + np.floor(ox) + 0.5, j.ravel() + region_min[1] + 0.5, l.ravel() + np.floor(oz) + 0.5], axis=1)
+        pos.append(b)
+    p = np.concatenate(pos).astype(np.float32)
+    out = np.zeros((len(p), 4), np.float32)
+    out[:, :3] = p
+    return out
+
+
+def solids_scene(fluid_shape=(64, 64, 64), n_boxes=8, box_shape=(16, 16, 32), box=128, seed=3):
+    """Fluid lattice in the low-x corner and static solid boxes in the high-x half.
+    Returns pos, vel, inverse mass (1 fluid, 0 solid)."""
+    fpos, fvel = lattice(*fluid_shape, seed=seed)
+    x0 = 2.5 + fluid_shape[0] + 2.0
+    spos = solid_boxes(n_boxes, box_shape, (x0, 1.5, 2.0), (box - 2.0, box - 2.0, box - 2.0), seed + 1000)
+    pos = np.concatenate([fpos, spos])
+    vel = np.zeros_like(pos)
+    w = np.concatenate([np.ones(len(fpos), np.float32), np.zeros(len(spos), np.float32)])
+    return pos, vel, w
+
+
 WORKLOADS = {
     "dam_break_32k": dict(shape=(32, 32, 32), box=64, seed=1, vorticity=0.0, viscosity=0.0),
     "fluid_1m": dict(shape=(100, 100, 100), box=128, seed=2, vorticity=0.0005, viscosity=0.01),
+    "solids_328k": dict(shape=(64, 64, 64), box=128, seed=3, vorticity=0.0, viscosity=0.0, solids=(8, (16, 16, 32))),
 }
