@@ -202,6 +202,44 @@ typedef struct pbd_kernel_stat {
 int pbd_profile_frames(pbd_sim* sim, int nsteps, void* stream, pbd_kernel_stat* stats,
                        uint32_t max_stats, uint32_t* n_stats);
 
+/* ---- tuning --------------------------------------------------------------------------- */
+/* No counterpart in the reference (threads per block is a config value there,
+ * Initialize.h:73).  Times the frame with 64, 128 and 256 threads per block for the neighbour
+ * passes (3 frames each after 2 warm-up frames -- this ADVANCES the simulation by 15 frames) and
+ * keeps the fastest.  With `cache_path` (a JSON-lines file) a result recorded for the same
+ * workload signature is reused without measuring, and new results are appended. */
+int pbd_autotune(pbd_sim* sim, const char* cache_path, void* stream, uint32_t* block);
+
+/* ---- batched scenes ------------------------------------------------------------------ */
+/* No counterpart in the reference (one scene per process there).  Many independent scenes
+ * advance together: every kernel of a frame covers all scenes, so a frame is one graph launch
+ * whatever the number of scenes.  Scenes share every parameter except the ones in
+ * pbd_scene_desc.  Each scene's particles are sorted by (scene, Morton key) and use their own
+ * 128^3-cell slice of the cell tables, so a scene evolves exactly as it would alone. */
+typedef struct pbd_scene_desc {
+    uint32_t capacity;          /* particles this scene may hold */
+    float    rest_density;      /* Density.restDensity of this scene */
+    float    gravity;           /* Forces.gravity of this scene */
+    float    bounds_min[3];     /* Enclosure.{X,Y,Z}.min of this scene */
+    float    bounds_max[3];     /* Enclosure.{X,Y,Z}.max of this scene */
+} pbd_scene_desc;
+typedef struct pbd_batch pbd_batch;
+int pbd_batch_create(const pbd_params* shared, uint32_t nscenes, const pbd_scene_desc* scenes,
+                     pbd_batch** out);
+int pbd_batch_destroy(pbd_batch* batch);
+int pbd_batch_add_particles(pbd_batch* batch, uint32_t scene, uint32_t n, const float* pos4,
+                            const float* vel4);
+int pbd_batch_step(pbd_batch* batch, int nsteps, void* stream);
+int pbd_batch_sync(pbd_batch* batch);
+int pbd_batch_num_particles(pbd_batch* batch, uint32_t scene, uint32_t* n);
+/* The scene's particles in their current (Morton-sorted) order; arrays of
+ * pbd_batch_num_particles float4.  Synchronous. */
+int pbd_batch_get_state(pbd_batch* batch, uint32_t scene, float* pos4, float* vel4);
+int pbd_batch_autotune(pbd_batch* batch, const char* cache_path, void* stream, uint32_t* block);
+int pbd_batch_launches_per_step(pbd_batch* batch, uint32_t* n);
+int pbd_batch_profile_frames(pbd_batch* batch, int nsteps, void* stream, pbd_kernel_stat* stats,
+                             uint32_t max_stats, uint32_t* n_stats);
+
 /* ---- sorting without allocation -------------------------------------------------- */
 /* No counterpart in the reference.  For hosts that cannot call cudaMalloc where they sort
  * (engines that own all device memory from start-up, frame loops that must not stall on an

@@ -15,6 +15,13 @@ namespace pbd {
 
 constexpr uint32_t kEmptyCell = 0xFFFFFFFFu;   // UINT_MAX start = empty cell (SortReorder.h:146)
 
+// Per-scene values of the batched form (one simulation holding many independent scenes).
+struct SceneParams {
+    float rho0;            // Density.restDensity of this scene
+    float gravity;         // Forces.gravity of this scene
+    float bmin[3], bmax[3];
+};
+
 struct DevParams {
     uint32_t N;            // numberOfParticles this frame
     uint32_t G;            // maxGrid (cells addressable by the tables)
@@ -42,7 +49,30 @@ struct DevParams {
     float inv_wq;          // 1 / wq
     float inv_spiky_den;   // 1 / spiky_den
     float cut2;            // max(hp, hs, d)^2: beyond it no kernel and no contact is non-zero
+    // batched form: scene of each particle (sorted order), each scene's [start, end) in the sorted
+    // arrays and its parameters; cells of scene s live at s * G + morton in the tables
+    uint32_t batched;
+    uint32_t nscenes;
+    uint32_t table_size;   // cells in the tables: G, or nscenes * G in the batched form
+    const SceneParams* scenes;
+    uint32_t* scene_of;
+    uint32_t* scene_range;
 };
+
+// The scene a particle belongs to, as the walk and the per-scene constants see it.
+struct SceneCtx {
+    uint32_t base;   // first table entry of the scene's cells (scene * G)
+    uint32_t end;    // one past the scene's last particle in the sorted arrays
+    uint32_t n;      // particles in the scene (the reference's numberOfParticles)
+    float rho0;
+};
+
+__device__ __forceinline__ SceneCtx scene_ctx(const DevParams& P, uint32_t i) {
+    if (!P.batched) return SceneCtx{0u, P.N, P.N, P.rho0};
+    const uint32_t sc = P.scene_of[i];
+    const uint32_t s = P.scene_range[2 * sc], e = P.scene_range[2 * sc + 1];
+    return SceneCtx{sc * P.G, e, e - s, P.scenes[sc].rho0};
+}
 
 // ---------------------------------------------------------------- Morton (Hash.h) -----
 __device__ __forceinline__ uint32_t expand_bits(uint32_t v) {

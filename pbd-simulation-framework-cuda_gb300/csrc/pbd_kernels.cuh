@@ -40,20 +40,32 @@ predict_key_kernel(DevParams P, float4* __restrict__ x, float4* __restrict__ v, 
     const uint32_t old_n = *table_n;            // sorted keys whose cells the tables still hold
     const uint32_t total = N > old_n ? N : old_n;
     const bool forces = (P.active & PBD_ACTIVE_APPLY_FORCES) != 0;
+    if (P.batched && blockIdx.x == 0)           // scene ranges are rebuilt by the re-order
+        for (uint32_t k = threadIdx.x; k < 2 * P.nscenes; k += blockDim.x) P.scene_range[k] = 0u;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         if (i < old_n) {                        // last frame's cell of slot i: mark empty
             const uint32_t oc = old_keys[i];
-            if (oc < P.G) cell_start[oc] = kEmptyCell;
+            if (oc < P.table_size) cell_start[oc] = kEmptyCell;
         }
         if (i >= N) continue;
         float4 pp;
+        uint32_t sc = 0;
+        float gravity = P.gravity;
+        const float* bmin = P.bmin;
+        const float* bmax = P.bmax;
+        if (P.batched) {                         // this particle's scene: own gravity and walls
+            sc = P.scene_of[i];
+            gravity = P.scenes[sc].gravity;
+            bmin = P.scenes[sc].bmin;
+            bmax = P.scenes[sc].bmax;
+        }
         if (forces) {
             float4 vv = v[i];
             float4 xx = x[i];
             const float dt = P.dt;
             if (!w || w[i] != 0.0f) {           // solids (inverse mass 0) take no forces
                 const float4 f = fext[i];
-                vv.y = __fmaf_rn(P.gravity, dt, vv.y);
+                vv.y = __fmaf_rn(gravity, dt, vv.y);
                 vv.x = __fmaf_rn(f.x, dt, vv.x);
                 vv.y = __fmaf_rn(f.y, dt, vv.y);
                 vv.z = __fmaf_rn(f.z, dt, vv.z);
@@ -63,12 +75,12 @@ predict_key_kernel(DevParams P, float4* __restrict__ x, float4* __restrict__ v, 
                              __fmaf_rn(vv.z, dt, xx.z), __fmaf_rn(vv.w, dt, xx.w));
             bool upd = false;
             // confineToBox (Forces.h:26-54)
-            if (pp.x < P.bmin[0]) { vv.x = __fmul_rn(P.vel_damp, vv.x); pp.x = __fadd_rn(P.bmin[0], 0.001f); upd = true; }
-            else if (pp.x > P.bmax[0]) { vv.x = __fmul_rn(P.vel_damp, vv.x); pp.x = __fsub_rn(P.bmax[0], 0.001f); upd = true; }
-            if (pp.y < P.bmin[1]) { vv.y = __fmul_rn(P.vel_damp, vv.y); pp.y = __fadd_rn(P.bmin[1], 0.001f); upd = true; }
-            else if (pp.y > P.bmax[1]) { vv.y = __fmul_rn(P.vel_damp, vv.y); pp.y = __fsub_rn(P.bmax[1], 0.001f); upd = true; }
-            if (pp.z < P.bmin[2]) { vv.z = __fmul_rn(P.vel_damp, vv.z); pp.z = __fadd_rn(P.bmin[2], 0.001f); upd = true; }
-            else if (pp.z > P.bmax[2]) { vv.z = __fmul_rn(P.vel_damp, vv.z); pp.z = __fsub_rn(P.bmax[2], 0.001f); upd = true; }
+            if (pp.x < bmin[0]) { vv.x = __fmul_rn(P.vel_damp, vv.x); pp.x = __fadd_rn(bmin[0], 0.001f); upd = true; }
+            else if (pp.x > bmax[0]) { vv.x = __fmul_rn(P.vel_damp, vv.x); pp.x = __fsub_rn(bmax[0], 0.001f); upd = true; }
+            if (pp.y < bmin[1]) { vv.y = __fmul_rn(P.vel_damp, vv.y); pp.y = __fadd_rn(bmin[1], 0.001f); upd = true; }
+            else if (pp.y > bmax[1]) { vv.y = __fmul_rn(P.vel_damp, vv.y); pp.y = __fsub_rn(bmax[1], 0.001f); upd = true; }
+            if (pp.z < bmin[2]) { vv.z = __fmul_rn(P.vel_damp, vv.z); pp.z = __fadd_rn(bmin[2], 0.001f); upd = true; }
+            else if (pp.z > bmax[2]) { vv.z = __fmul_rn(P.vel_damp, vv.z); pp.z = __fsub_rn(bmax[2], 0.001f); upd = true; }
             if (upd) {
                 const float pd = P.pos_damp;
                 xx.x = __fmaf_rn(pd, __fsub_rn(pp.x, xx.x), xx.x);
@@ -83,7 +95,11 @@ predict_key_kernel(DevParams P, float4* __restrict__ x, float4* __restrict__ v, 
         } else {
             pp = p[i];
         }
-        const uint32_t key = morton(pp.x, pp.y, pp.z);
+        uint32_t key = morton(pp.x, pp.y, pp.z);
+        if (P.batched) {                         // scene-major key: scenes sort apart
+            if (key >= P.G) { atomicOr(err, kErrKeyBits); key = P.G - 1u; }
+            key += sc * P.G;
+        }
         keys[i] = key;
         for (int ps = 0; ps < npasses; ++ps) atomicAdd(&sh[ps * kRadix + ((key >> (ps * kRadixBits)) & (kRadix - 1))], 1u);
         if (npasses < kMaxPasses && (key >> (npasses * kRadixBits)) != 0u) atomicOr(err, kErrKeyBits);
@@ -134,21 +150,31 @@ reorder_cells_kernel(DevParams P, ReorderArgs A, SortScratch S, int npasses, uin
         if (A.ido) A.ido[i] = A.idi[o];
         if (A.wo) A.wo[i] = A.wi[o];
         const uint32_t k = A.skeys[i];
-        if (k < P.G) {
+        if (k < P.table_size) {
             if (i == 0 || A.skeys[i - 1] != k) A.cell_start[k] = i;
             if (i == N - 1 || A.skeys[i + 1] != k) A.cell_end[k] = i + 1;
+        }
+        if (P.batched) {                         // scene of each sorted slot and each scene's range
+            const uint32_t sc = k / P.G;
+            P.scene_of[i] = sc;
+            if (i == 0 || A.skeys[i - 1] / P.G != sc) P.scene_range[2 * sc] = i;
+            if (i == N - 1 || A.skeys[i + 1] / P.G != sc) P.scene_range[2 * sc + 1] = i + 1;
         }
     }
 }
 
 // Mark empty every cell the tables hold (used when the sorted-key buffer moves).
 __global__ void clear_cells_kernel(const uint32_t* __restrict__ old_keys, const uint32_t* __restrict__ table_n,
-                                   uint32_t* __restrict__ cell_start, uint32_t G) {
+                                   uint32_t* __restrict__ cell_start, uint32_t table_size) {
     const uint32_t n = *table_n;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t oc = old_keys[i];
-        if (oc < G) cell_start[oc] = kEmptyCell;
+        if (oc < table_size) cell_start[oc] = kEmptyCell;
     }
+}
+
+__global__ void fill_u32_kernel(uint32_t* a, uint32_t value, uint32_t first, uint32_t n) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) a[first + k] = value;
 }
 
 __global__ void fill_float_kernel(float* a, float value, uint32_t n) {

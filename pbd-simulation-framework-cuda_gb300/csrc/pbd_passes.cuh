@@ -45,10 +45,10 @@ struct DeferList {
 // (findContacts/findNeighbours run before the solver loop, Fluid.cu:41-47); passes later in
 // the frame use the moved positions for the physics but the anchor's cells.
 template <class F, class G>
-__device__ __forceinline__ void for_each_range(const DevParams& P, float4 pi, const uint32_t* __restrict__ cs,
+__device__ __forceinline__ void for_each_range(const DevParams& P, const SceneCtx& S, float4 pi, const uint32_t* __restrict__ cs,
                                                const uint32_t* __restrict__ ce, F& f, G& end_contacts) {
-    const uint32_t N = P.N;
-    const bool quirk = (P.flags & PBD_FLAG_CELL_END_QUIRK) && N >= 2;
+    const uint32_t N = P.N;     // table starts >= N mark empty cells
+    const bool quirk = (P.flags & PBD_FLAG_CELL_END_QUIRK) && S.n >= 2;
     if (P.active & PBD_ACTIVE_FIND_CONTACTS) {
         uint32_t mz[3];
 #pragma unroll
@@ -63,10 +63,10 @@ __device__ __forceinline__ void for_each_range(const DevParams& P, float4 pi, co
                 for (int c = 0; c < 3; ++c) {
                     const uint32_t h = hxy + mz[c];
                     if (h >= P.G) continue;
-                    const uint32_t s = __ldg(cs + h);
+                    const uint32_t s = __ldg(cs + S.base + h);
                     if (s >= N) continue;
-                    uint32_t e = __ldg(ce + h);
-                    if ((quirk && h == N - 1) || e > N) e = N;   // entries >= N are skipped (Collision.h:59)
+                    uint32_t e = __ldg(ce + S.base + h);
+                    if ((quirk && h == S.n - 1) || e > S.end) e = S.end;   // entries >= N are skipped (Collision.h:59)
                     if (f(s, e, true)) return;
                 }
             }
@@ -89,10 +89,10 @@ __device__ __forceinline__ void for_each_range(const DevParams& P, float4 pi, co
                     for (int c = -sh; c <= sh; c += cstep) {
                         const uint32_t h = hx + hy + morton_axis(__fmaf_rn((float)c, P.d, pi.z));
                         if (h >= P.G) continue;
-                        const uint32_t s = __ldg(cs + h);
-                        uint32_t e = __ldg(ce + h);
-                        if (s == kEmptyCell) continue;
-                        if ((quirk && h == N - 1) || e > N) e = N;   // entries >= N are skipped (Collision.h:142)
+                        const uint32_t s = __ldg(cs + S.base + h);
+                        uint32_t e = __ldg(ce + S.base + h);
+                        if (s >= N) continue;
+                        if ((quirk && h == S.n - 1) || e > S.end) e = S.end;   // entries >= N are skipped (Collision.h:142)
                         if (f(s, e, false)) return;
                     }
                 }
@@ -105,9 +105,9 @@ __device__ __forceinline__ void for_each_range(const DevParams& P, float4 pi, co
 // range longer than kLongRange is met and `defer` is set.  `anchor` selects the cells, `p`
 // holds the current positions.
 template <class V>
-__device__ __forceinline__ uint32_t walk_seq(const DevParams& P, uint32_t i, float4 anchor, const float4* __restrict__ p,
-                                             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
-                                             V& vis, bool defer, bool* deferred) {
+__device__ __forceinline__ uint32_t walk_seq(const DevParams& P, const SceneCtx& S, uint32_t i, float4 anchor,
+                                             const float4* __restrict__ p, const uint32_t* __restrict__ cs,
+                                             const uint32_t* __restrict__ ce, V& vis, bool defer, bool* deferred) {
     const uint32_t M = P.M;
     uint32_t cnt = 0;
     if (M == 0) return 0;
@@ -121,14 +121,15 @@ __device__ __forceinline__ uint32_t walk_seq(const DevParams& P, uint32_t i, flo
         return false;
     };
     auto endc = [&]() -> bool { vis.end_contacts(cnt); return false; };
-    for_each_range(P, anchor, cs, ce, range, endc);
+    for_each_range(P, S, anchor, cs, ce, range, endc);
     return cnt;
 }
 
 // One warp per particle (all 32 lanes call it with the same i).  Same list, same order.
 template <class V>
-__device__ __forceinline__ uint32_t walk_coop(const DevParams& P, uint32_t i, float4 anchor, const float4* __restrict__ p,
-                                              const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, V& vis) {
+__device__ __forceinline__ uint32_t walk_coop(const DevParams& P, const SceneCtx& S, uint32_t i, float4 anchor,
+                                              const float4* __restrict__ p, const uint32_t* __restrict__ cs,
+                                              const uint32_t* __restrict__ ce, V& vis) {
     const uint32_t M = P.M;
     const uint32_t lane = lane_id(), lt = lanemask_lt_u();
     uint32_t cnt = 0;
@@ -155,7 +156,7 @@ __device__ __forceinline__ uint32_t walk_coop(const DevParams& P, uint32_t i, fl
         return false;
     };
     auto endc = [&]() -> bool { vis.end_contacts(cnt); return false; };
-    for_each_range(P, anchor, cs, ce, range, endc);
+    for_each_range(P, S, anchor, cs, ce, range, endc);
     return cnt;
 }
 
@@ -218,37 +219,39 @@ struct LambdaVisit {
         A += c.a; B += c.b;
         Cx += c.gx; Cy += c.gy; Cz += c.gz; Cw += c.gw;
     }
-    __device__ __forceinline__ float finish() const {
-        const float a = A / P.rho0 - 1.0f;
-        const float b = B / P.rho0;
-        const float c = (Cx * Cx + Cy * Cy + Cz * Cz + Cw * Cw) / P.rho0;
+    __device__ __forceinline__ float finish(float rho0) const {
+        const float a = A / rho0 - 1.0f;
+        const float b = B / rho0;
+        const float c = (Cx * Cx + Cy * Cy + Cz * Cz + Cw * Cw) / rho0;
         return -a / (b + c + P.lambda_eps);
     }
 };
 
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
               const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
+    const SceneCtx S = scene_ctx(P, i);
     LambdaVisit vis(P, p[i]);
     bool deferred = false;
-    walk_seq(P, i, pa[i], p, cs, ce, vis, true, &deferred);
+    walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
     if (deferred) {
         if (defer_particle(D, i)) return;
         vis.reset();
-        walk_seq(P, i, pa[i], p, cs, ce, vis, false, &deferred);
+        walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
-    lambda[i] = vis.finish();
+    lambda[i] = vis.finish(S.rho0);
 }
 
 __global__ void __launch_bounds__(128)
 lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
                    const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
+        const SceneCtx S = scene_ctx(P, i);
         LambdaVisit vis(P, p[i]);
-        walk_coop(P, i, pa[i], p, cs, ce, vis);
-        if (lane_id() == 0) lambda[i] = vis.finish();
+        walk_coop(P, S, i, pa[i], p, cs, ce, vis);
+        if (lane_id() == 0) lambda[i] = vis.finish(S.rho0);
     });
 }
 
@@ -335,13 +338,13 @@ struct DeltaVisit {
     }
 };
 
-__device__ __forceinline__ void delta_finish(const DevParams& P, uint32_t mode, uint32_t i, const DeltaVisit& vis,
+__device__ __forceinline__ void delta_finish(const DevParams& P, float rho0, uint32_t mode, uint32_t i, const DeltaVisit& vis,
                                              float4* __restrict__ pout, float4* __restrict__ x, float4* __restrict__ v,
                                              float4* __restrict__ delta) {
     // a solid (inverse mass 0) takes no density correction
     float4 pn = vis.pacc, xn = vis.xacc;
     float4 dp = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (mode & kDoDelta) dp = make_float4(vis.ax / P.rho0, vis.ay / P.rho0, vis.az / P.rho0, vis.aw / P.rho0);
+    if (mode & kDoDelta) dp = make_float4(vis.ax / rho0, vis.ay / rho0, vis.az / rho0, vis.aw / rho0);
     else if (mode & kLoadDelta) dp = delta[i];
     if (mode & kStoreDelta) delta[i] = dp;
     if (mode & kDoApply) {
@@ -357,7 +360,7 @@ __device__ __forceinline__ void delta_finish(const DevParams& P, uint32_t mode, 
     if (mode & (kDoCollide | kDoUpdate)) x[i] = xn;
 }
 
-__global__ void __launch_bounds__(128, 4)
+__global__ void __launch_bounds__(256, 2)
 delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const float4* __restrict__ pa, float4* __restrict__ pout,
              float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda, const float* __restrict__ w,
              float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
@@ -368,17 +371,18 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const f
     const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
     const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
+    const SceneCtx S = scene_ctx(P, i);
     DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
     if (mode & (kDoDelta | kDoCollide)) {
         bool deferred = false;
-        walk_seq(P, i, pa[i], pin, cs, ce, vis, true, &deferred);
+        walk_seq(P, S, i, pa[i], pin, cs, ce, vis, true, &deferred);
         if (deferred) {
             if (defer_particle(D, i)) return;
             vis.reset();
-            walk_seq(P, i, pa[i], pin, cs, ce, vis, false, &deferred);
+            walk_seq(P, S, i, pa[i], pin, cs, ce, vis, false, &deferred);
         }
     }
-    delta_finish(P, mode, i, vis, pout, x, v, delta);
+    delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
 }
 
 __global__ void __launch_bounds__(128)
@@ -391,9 +395,10 @@ delta_coop_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, co
         const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
         const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
+        const SceneCtx S = scene_ctx(P, i);
         DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
-        walk_coop(P, i, pa[i], pin, cs, ce, vis);
-        if (lane_id() == 0) delta_finish(P, mode, i, vis, pout, x, v, delta);
+        walk_coop(P, S, i, pa[i], pin, cs, ce, vis);
+        if (lane_id() == 0) delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
     });
 }
 
@@ -443,18 +448,19 @@ struct OmegaVisit {
     }
 };
 
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ v,
              const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega, DeferList D) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
+    const SceneCtx S = scene_ctx(P, i);
     OmegaVisit vis(P, v, p[i], v[i]);
     bool deferred = false;
-    walk_seq(P, i, pa[i], p, cs, ce, vis, true, &deferred);
+    walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
     if (deferred) {
         if (defer_particle(D, i)) return;
         vis.reset();
-        walk_seq(P, i, pa[i], p, cs, ce, vis, false, &deferred);
+        walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
     omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
 }
@@ -464,8 +470,9 @@ omega_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __res
                   const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega,
                   DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
+        const SceneCtx S = scene_ctx(P, i);
         OmegaVisit vis(P, v, p[i], v[i]);
-        walk_coop(P, i, pa[i], p, cs, ce, vis);
+        walk_coop(P, S, i, pa[i], p, cs, ce, vis);
         if (lane_id() == 0) omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
     });
 }
@@ -544,7 +551,7 @@ __device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i,
     }
 }
 
-__global__ void __launch_bounds__(128, 4)
+__global__ void __launch_bounds__(256, 2)
 vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ vin,
                  float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
@@ -552,13 +559,14 @@ vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const SceneCtx S = scene_ctx(P, i);
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
     bool deferred = false;
-    walk_seq(P, i, pa[i], p, cs, ce, vis, true, &deferred);
+    walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
     if (deferred) {
         if (defer_particle(D, i)) return;
         vis.reset();
-        walk_seq(P, i, pa[i], p, cs, ce, vis, false, &deferred);
+        walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
     vort_visc_finish(P, i, vis, vout, fext, w);
 }
@@ -570,8 +578,9 @@ vort_visc_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* _
                       const float* __restrict__ w, DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
         const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const SceneCtx S = scene_ctx(P, i);
         VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
-        walk_coop(P, i, pa[i], p, cs, ce, vis);
+        walk_coop(P, S, i, pa[i], p, cs, ce, vis);
         if (lane_id() == 0) vort_visc_finish(P, i, vis, vout, fext, w);
     });
 }
@@ -605,12 +614,12 @@ __global__ void list_kernel(DevParams P, const float4* __restrict__ p, const uin
     uint32_t n;
     if (coop) {
         ListVisit lv(lane_id() == 0 ? list + (size_t)i * cap : nullptr, lane_id() == 0 ? cap : 0u);
-        n = walk_coop(P, i, p[i], p, cs, ce, lv);
+        n = walk_coop(P, scene_ctx(P, i), i, p[i], p, cs, ce, lv);
         vis.contacts = lv.contacts;
         if (lane_id() != 0) return;
     } else {
         bool deferred = false;
-        n = walk_seq(P, i, p[i], p, cs, ce, vis, false, &deferred);
+        n = walk_seq(P, scene_ctx(P, i), i, p[i], p, cs, ce, vis, false, &deferred);
     }
     if (vis.contacts == 0xFFFFFFFFu) vis.contacts = n;   // cap reached inside the 27 cells
     count[i] = n;

@@ -39,7 +39,7 @@ struct Cur {
 constexpr int kMaxGraphs = 8;
 
 constexpr int kThreadsParticle = 256;
-constexpr int kThreadsNeighbour = 128;
+constexpr int kThreadsNeighbourDefault = 128;
 constexpr int kThreadsCoop = 128;         // 4 warps, one deferred particle per warp
 
 inline uint32_t div_up(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
@@ -55,6 +55,15 @@ struct pbd_sim {
     uint32_t* ids[2]{};
     float* w[2]{};                // inverse masses (solids = 0), carried through re-orders once used
     bool mass_used = false;
+    int tpb_nbr = kThreadsNeighbourDefault;   // block size of the neighbour passes (tunable)
+    // batched form
+    bool batched = false;
+    uint32_t nscenes = 0;
+    SceneParams* d_scenes = nullptr;
+    uint32_t* scene_of = nullptr;
+    uint32_t* scene_range = nullptr;
+    std::vector<uint32_t> scene_cap, scene_count;
+    std::vector<SceneParams> h_scenes;
     float4 *fext = nullptr, *omega = nullptr, *delta = nullptr;
     float* lambda = nullptr;
     uint32_t *keys[2]{}, *vals[2]{};
@@ -89,11 +98,19 @@ int cuda_fail(const char* what, cudaError_t e) {
         if (_e != cudaSuccess) return cuda_fail(#call, _e); \
     } while (0)
 
-int sort_passes(const pbd_params& p) {
+int sort_passes(const pbd_sim* s) {
     // With applyForces on, every key comes from a position clamped inside the enclosure, whose
     // limits are at most 126.5 (Communication.h:573-598): keys < 2^21, three 8-bit digits.
-    return (p.active & PBD_ACTIVE_APPLY_FORCES) ? 3 : 4;
+    // The batched form prefixes the scene number: 21 + log2(scenes) bits.
+    if (s->batched) {
+        uint32_t bits = 21;
+        while ((1u << (bits - 21)) < s->nscenes) ++bits;
+        return std::min(kMaxPasses, (int)((bits + kRadixBits - 1) / kRadixBits));
+    }
+    return (s->prm.active & PBD_ACTIVE_APPLY_FORCES) ? 3 : 4;
 }
+
+uint32_t table_size(const pbd_sim* s) { return s->prm.max_grid * (s->batched ? s->nscenes : 1u); }
 
 float powi_host(float x, int n) {
     float r = 1.0f;
@@ -144,6 +161,12 @@ DevParams make_dev_params(const pbd_sim* s) {
     P.inv_wq = wq != 0.0f ? 1.0f / wq : 0.0f;
     P.inv_spiky_den = 1.0f / P.spiky_den;
     P.far_pairs_zero = (wq > 0.0f && std::isfinite(wq) && p.n_scorr >= 0) ? 1u : 0u;
+    P.batched = s->batched ? 1u : 0u;
+    P.nscenes = s->nscenes;
+    P.table_size = table_size(s);
+    P.scenes = s->d_scenes;
+    P.scene_of = s->scene_of;
+    P.scene_range = s->scene_range;
     const float c = std::max(P.hp, std::max(P.hs, P.d));
     P.cut2 = c * c * 1.0001f;
     return P;
@@ -176,8 +199,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const DevParams P = make_dev_params(s);
     const pbd_params& prm = s->prm;
     const uint32_t N = s->N;
-    const int np = sort_passes(prm);
-    const uint32_t G = prm.max_grid;
+    const int np = sort_passes(s);
+    const int tn = s->tpb_nbr;
     SortScratch S{s->hist, s->status, s->tile_counter, s->err, s->max_tiles};
     nl = 0;
 
@@ -222,7 +245,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const float* wf = s->mass_used ? s->w[cur.x] : nullptr;   // after the re-order
     auto next_p = [&](int c) { return c == anchor ? (anchor + 1) % 3 : 3 - c - anchor; };
 
-    const uint32_t gn = div_up(N, kThreadsNeighbour);
+    const uint32_t gn = div_up(N, tn);
     const DeferList D{s->defer_items, s->defer_count, s->defer_done, s->defer_cap};
     const uint32_t gc = (uint32_t)s->num_sms * 2u;   // cooperative kernels: grid-stride over the deferred
     const uint32_t act = prm.active;
@@ -234,7 +257,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     for (uint32_t it = 0; it < I; ++it) {
         if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
             PROF_BEGIN("lambda");
-            lambda_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, s->lambda, D);
+            lambda_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, s->lambda, D);
             lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, s->lambda, D);
             PROF_END();
             nl += 2;
@@ -260,7 +283,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             if (final_pass && do_update) mode |= kDoUpdate;
             PROF_BEGIN("delta");
             const int pout = next_p(cur.p);
-            delta_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
+            delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
                                                             s->v[cur.v], s->lambda, wf, s->delta, s->cell_start, s->cell_end, D);
             delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
                                                            s->v[cur.v], s->lambda, wf, s->delta, s->cell_start, s->cell_end, D);
@@ -278,7 +301,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     }
     if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
         PROF_BEGIN("omega");
-        omega_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
+        omega_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
         omega_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
         PROF_END();
         nl += 2;
@@ -286,7 +309,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     if (vort || visc) {
         PROF_BEGIN("vort_visc");
-        vort_visc_kernel<<<gn, kThreadsNeighbour, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
+        vort_visc_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
                                                             s->fext, s->cell_start, s->cell_end, vort, visc, wf, D);
         vort_visc_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
                                                            s->fext, s->cell_start, s->cell_end, vort, visc, wf, D);
@@ -294,7 +317,6 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         nl += 2;
         if (visc) cur.v ^= 1;
     }
-    (void)G;
     return cudaGetLastError();
 }
 
@@ -319,10 +341,10 @@ int capture_one(pbd_sim* s, Cur& c, cudaGraphExec_t* out, uint32_t& nl) {
 
 // The sort's final buffer depends on the pass count; if it moved, clear the old cells now.
 int settle_tables(pbd_sim* s, cudaStream_t st) {
-    const int np = sort_passes(s->prm);
+    const int np = sort_passes(s);
     if (s->table_passes >= 0 && (s->table_passes % 2) != (np % 2)) {
         clear_cells_kernel<<<std::max(1u, std::min(div_up(s->table_hint, 256), (uint32_t)s->num_sms * 8u)), 256, 0, st>>>(
-            s->keys[s->table_passes % 2], s->table_n, s->cell_start, s->prm.max_grid);
+            s->keys[s->table_passes % 2], s->table_n, s->cell_start, table_size(s));
         CK(cudaGetLastError());
         CK(cudaMemsetAsync(s->table_n, 0, sizeof(uint32_t), st));
         s->table_hint = 0;
@@ -376,25 +398,35 @@ extern "C" {
 const char* pbd_last_error(void) { return g_last_error.c_str(); }
 uint32_t pbd_abi_version(void) { return PBD_ABI_VERSION; }
 
-int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
-    clear_error();
-    if (!prm || !out) { set_error("pbd_create: null argument"); return PBD_ERR_INVALID_ARG; }
+}  // extern "C"
+
+namespace {
+// Allocate a simulation: one arena for every buffer.  `scenes` is non-null for the batched form.
+int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<SceneParams>* scenes,
+               const std::vector<uint32_t>* caps, pbd_sim** out) {
     *out = nullptr;
     int rc = pbd_validate_params(prm);
     if (rc) return rc;
     if (prm->collision_type != 0) { set_error("collisionType 1 (batched contact claims) is not implemented"); return PBD_ERR_UNSUPPORTED; }
-    if (capacity == 0 || capacity > (1u << 30) - 1u) { set_error("pbd_create: capacity must be in [1, 2^30)"); return PBD_ERR_INVALID_ARG; }
+    if (capacity == 0 || capacity > (1u << 30) - 1u) { set_error("capacity must be in [1, 2^30)"); return PBD_ERR_INVALID_ARG; }
     pbd_sim* s = new (std::nothrow) pbd_sim();
-    if (!s) { set_error("pbd_create: host allocation"); return PBD_ERR_ALLOC; }
+    if (!s) { set_error("host allocation"); return PBD_ERR_ALLOC; }
     s->prm = *prm;
     s->cap = capacity;
+    if (scenes) {
+        s->batched = true;
+        s->nscenes = (uint32_t)scenes->size();
+        s->h_scenes = *scenes;
+        s->scene_cap = *caps;
+        s->scene_count.assign(s->nscenes, 0u);
+    }
     cudaError_t e = cudaGetDevice(&s->device);
     if (e != cudaSuccess) { delete s; return cuda_fail("cudaGetDevice", e); }
     e = cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device);
     if (e != cudaSuccess) { delete s; return cuda_fail("cudaDeviceGetAttribute", e); }
     s->max_tiles = div_up(capacity, kSortTile);
     // ---- one arena, 256-byte aligned slices
-    const size_t C = capacity, G = prm->max_grid;
+    const size_t C = capacity, T = table_size(s);
     std::vector<std::pair<void**, size_t>> parts;
     for (int b = 0; b < 2; ++b) {
         parts.push_back({(void**)&s->x[b], C * 16});
@@ -405,7 +437,7 @@ int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
     for (int b = 0; b < 3; ++b) parts.push_back({(void**)&s->p[b], C * 16});
     parts.push_back({(void**)&s->fext, C * 16}); parts.push_back({(void**)&s->omega, C * 16});
     parts.push_back({(void**)&s->delta, C * 16}); parts.push_back({(void**)&s->lambda, C * 4});
-    parts.push_back({(void**)&s->cell_start, G * 4}); parts.push_back({(void**)&s->cell_end, G * 4});
+    parts.push_back({(void**)&s->cell_start, T * 4}); parts.push_back({(void**)&s->cell_end, T * 4});
     parts.push_back({(void**)&s->hist, (size_t)kMaxPasses * kRadix * 4});
     parts.push_back({(void**)&s->status, (size_t)kMaxPasses * s->max_tiles * kRadix * 4});
     parts.push_back({(void**)&s->tile_counter, kMaxPasses * 4}); parts.push_back({(void**)&s->err, 4});
@@ -413,6 +445,11 @@ int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
     s->defer_cap = std::min<uint32_t>(capacity, 1u << 16);
     parts.push_back({(void**)&s->defer_items, (size_t)s->defer_cap * 4});
     parts.push_back({(void**)&s->defer_count, 4}); parts.push_back({(void**)&s->defer_done, 4});
+    if (s->batched) {
+        parts.push_back({(void**)&s->d_scenes, (size_t)s->nscenes * sizeof(SceneParams)});
+        parts.push_back({(void**)&s->scene_of, C * 4});
+        parts.push_back({(void**)&s->scene_range, (size_t)s->nscenes * 8});
+    }
     size_t total = 0;
     for (auto& pt : parts) total += (pt.second + 255) & ~size_t(255);
     e = cudaMalloc(&s->arena, total);
@@ -420,16 +457,27 @@ int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
     char* cur = static_cast<char*>(s->arena);
     for (auto& pt : parts) { *pt.first = cur; cur += (pt.second + 255) & ~size_t(255); }
     e = cudaMemset(s->arena, 0, total);
-    if (e == cudaSuccess) e = cudaMemset(s->cell_start, 0xFF, G * 4);   // all cells empty
+    if (e == cudaSuccess) e = cudaMemset(s->cell_start, 0xFF, T * 4);   // all cells empty
     if (e == cudaSuccess) {                                               // inverse mass 1 everywhere
         for (int b = 0; b < 2; ++b) fill_float_kernel<<<256, 256>>>(s->w[b], 1.0f, capacity);
         e = cudaGetLastError();
     }
+    if (e == cudaSuccess && s->batched)
+        e = cudaMemcpy(s->d_scenes, s->h_scenes.data(), s->nscenes * sizeof(SceneParams), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) { cudaFree(s->arena); delete s; return cuda_fail("pbd_create init", e); }
     *out = s;
     return PBD_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int pbd_create(const pbd_params* prm, uint32_t capacity, pbd_sim** out) {
+    clear_error();
+    if (!prm || !out) { set_error("pbd_create: null argument"); return PBD_ERR_INVALID_ARG; }
+    return create_sim(prm, capacity, nullptr, nullptr, out);
 }
 
 int pbd_destroy(pbd_sim* s) {
@@ -479,6 +527,7 @@ static int add_common(pbd_sim* s, uint32_t n, const float* pos4, const float* ve
     if (int rc = check_sim(s, "pbd_add_particles")) return rc;
     if (n == 0) return PBD_OK;
     if (!pos4 || !vel4) { set_error("pbd_add_particles: null position or velocity array"); return PBD_ERR_INVALID_ARG; }
+    if (s->batched) { set_error("a batch takes particles per scene: pbd_batch_add_particles"); return PBD_ERR_INVALID_ARG; }
     if ((uint64_t)s->N + n > s->cap) {
         set_error("pbd_add_particles: " + std::to_string(s->N) + " + " + std::to_string(n) + " exceeds capacity " + std::to_string(s->cap));
         return PBD_ERR_CAPACITY;
@@ -526,6 +575,7 @@ int pbd_add_particles_device(pbd_sim* s, uint32_t n, const float* d_pos4, const 
 int pbd_add_particle(pbd_sim* s, const float pos[3], const float dir[3]) {
     clear_error();
     if (int rc = check_sim(s, "pbd_add_particle")) return rc;
+    if (s->batched) { set_error("a batch takes particles per scene: pbd_batch_add_particles"); return PBD_ERR_INVALID_ARG; }
     if (!pos || !dir) { set_error("pbd_add_particle: null"); return PBD_ERR_INVALID_ARG; }
     if ((uint64_t)s->N + 1 > s->cap) { set_error("pbd_add_particle: capacity reached"); return PBD_ERR_CAPACITY; }
     add_one_kernel<<<1, 1, 0, s->last_stream>>>(s->x[s->cur.x], s->v[s->cur.v], s->col[s->cur.x], s->ids[s->cur.x],
@@ -540,6 +590,7 @@ int pbd_clear(pbd_sim* s) {
     clear_error();
     if (int rc = check_sim(s, "pbd_clear")) return rc;
     s->N = 0;   // Communication.h:657-660
+    std::fill(s->scene_count.begin(), s->scene_count.end(), 0u);
     return PBD_OK;
 }
 
@@ -549,7 +600,7 @@ int pbd_step(pbd_sim* s, int nsteps, void* stream) {
     if (nsteps < 0) { set_error("pbd_step: nsteps < 0"); return PBD_ERR_INVALID_ARG; }
     if (s->N == 0 || nsteps == 0) return PBD_OK;   // Fluid.cu:19
     cudaStream_t st = (cudaStream_t)stream;
-    if (s->dirty || s->graph_n != s->N || s->table_passes != sort_passes(s->prm)) {
+    if (s->dirty || s->graph_n != s->N || s->table_passes != sort_passes(s)) {
         if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
         if (int rc = settle_tables(s, st)) return rc;
         if (int rc = build_graphs(s)) return rc;
@@ -611,7 +662,7 @@ int pbd_debug_dump(pbd_sim* s, uint32_t* keys, uint32_t* perm, uint32_t* cell_st
     clear_error();
     if (int rc = check_sim(s, "pbd_debug_dump")) return rc;
     if (int rc = sync_last(s)) return rc;
-    const int fin = (s->table_passes >= 0 ? s->table_passes : sort_passes(s->prm)) % 2;
+    const int fin = (s->table_passes >= 0 ? s->table_passes : sort_passes(s)) % 2;
     const size_t n = s->N;
     if (keys) CK(cudaMemcpy(keys, s->keys[fin], n * 4, cudaMemcpyDeviceToHost));
     if (perm) CK(cudaMemcpy(perm, s->vals[fin], n * 4, cudaMemcpyDeviceToHost));
@@ -717,6 +768,185 @@ int pbd_launches_per_step(pbd_sim* s, uint32_t* n) {
     }
     *n = s->launches;
     return PBD_OK;
+}
+
+
+// ======================================================================================
+// Block-size tuning of the neighbour passes, with a JSON-lines cache
+// ======================================================================================
+namespace {
+std::string tune_signature(const pbd_sim* s) {
+    char buf[256];
+    std::snprintf(buf, sizeof(buf), "n=%u;scenes=%u;iters=%u;stab=%u;active=%u;M=%u;K=%u;hs=%g;hp=%g;d=%g;mass=%d",
+                  s->N, s->nscenes, s->prm.solver_iterations, s->prm.stabilization_iterations, s->prm.active,
+                  s->prm.max_neighbours_per_particle, s->prm.kernel_width_neighbours, s->prm.kernel_width_spiky,
+                  s->prm.kernel_width_poly, 2.0 * s->prm.particle_radius, s->mass_used ? 1 : 0);
+    return buf;
+}
+
+bool cache_lookup(const char* path, const std::string& sig, int* block) {
+    if (!path) return false;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return false;
+    char line[1024];
+    bool found = false;
+    const std::string key = "\"signature\": \"" + sig + "\"";
+    while (std::fgets(line, sizeof(line), f)) {
+        if (std::strstr(line, key.c_str())) {
+            const char* b = std::strstr(line, "\"block\": ");
+            if (b) { *block = std::atoi(b + 9); found = true; }
+        }
+    }
+    std::fclose(f);
+    return found && (*block == 64 || *block == 128 || *block == 256);
+}
+}  // namespace
+
+int pbd_autotune(pbd_sim* s, const char* cache_path, void* stream, uint32_t* block) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_autotune")) return rc;
+    if (s->N == 0) { set_error("pbd_autotune: no particles"); return PBD_ERR_INVALID_ARG; }
+    const std::string sig = tune_signature(s);
+    int best = 0;
+    if (!cache_lookup(cache_path, sig, &best)) {
+        cudaStream_t st = (cudaStream_t)stream;
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        float best_ms = 1e30f;
+        for (int tpb : {64, 128, 256}) {
+            s->tpb_nbr = tpb;
+            s->dirty = true;
+            if (int rc = pbd_step(s, 2, stream)) return rc;        // records the graphs, warms up
+            CK(cudaEventRecord(a, st));
+            if (int rc = pbd_step(s, 3, stream)) return rc;
+            CK(cudaEventRecord(b, st));
+            CK(cudaEventSynchronize(b));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, a, b));
+            if (ms < best_ms) { best_ms = ms; best = tpb; }
+        }
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        if (cache_path) {
+            FILE* f = std::fopen(cache_path, "a");
+            if (f) {
+                std::fprintf(f, "{\"signature\": \"%s\", \"block\": %d, \"frame_ms\": %.6f}\n", sig.c_str(), best, best_ms / 3.0f);
+                std::fclose(f);
+            }
+        }
+    }
+    s->tpb_nbr = best;
+    s->dirty = true;
+    if (block) *block = (uint32_t)best;
+    return PBD_OK;
+}
+
+// ======================================================================================
+// Batched scenes: one simulation whose particles carry a scene number
+// ======================================================================================
+static pbd_sim* as_sim(pbd_batch* b) { return reinterpret_cast<pbd_sim*>(b); }
+
+int pbd_batch_create(const pbd_params* shared, uint32_t nscenes, const pbd_scene_desc* scenes, pbd_batch** out) {
+    clear_error();
+    if (!shared || !scenes || !out || nscenes == 0) { set_error("pbd_batch_create: bad argument"); return PBD_ERR_INVALID_ARG; }
+    *out = nullptr;
+    if (shared->max_grid != 128u * 128u * 128u) { set_error("pbd_batch_create: scenes use the 128^3 grid (max_grid)"); return PBD_ERR_UNSUPPORTED; }
+    if ((uint64_t)nscenes * shared->max_grid > (1ull << 32) - 1) { set_error("pbd_batch_create: at most 2047 scenes"); return PBD_ERR_RANGE; }
+    std::vector<SceneParams> sp(nscenes);
+    std::vector<uint32_t> caps(nscenes);
+    uint64_t total = 0;
+    for (uint32_t k = 0; k < nscenes; ++k) {
+        pbd_params q = *shared;   // each scene's values are checked with the reference's ranges
+        q.rest_density = scenes[k].rest_density;
+        q.gravity = scenes[k].gravity;
+        for (int a = 0; a < 3; ++a) { q.bounds_min[a] = scenes[k].bounds_min[a]; q.bounds_max[a] = scenes[k].bounds_max[a]; }
+        if (int rc = pbd_validate_params(&q)) {
+            set_error("scene " + std::to_string(k) + ": " + pbd_last_error());
+            return rc;
+        }
+        sp[k].rho0 = scenes[k].rest_density;
+        sp[k].gravity = scenes[k].gravity;
+        for (int a = 0; a < 3; ++a) { sp[k].bmin[a] = scenes[k].bounds_min[a]; sp[k].bmax[a] = scenes[k].bounds_max[a]; }
+        caps[k] = scenes[k].capacity;
+        total += scenes[k].capacity;
+    }
+    if (total == 0 || total > (1u << 30) - 1u) { set_error("pbd_batch_create: total capacity must be in [1, 2^30)"); return PBD_ERR_INVALID_ARG; }
+    pbd_sim* s = nullptr;
+    int rc = create_sim(shared, (uint32_t)total, &sp, &caps, &s);
+    if (rc) return rc;
+    *out = reinterpret_cast<pbd_batch*>(s);
+    return PBD_OK;
+}
+
+int pbd_batch_destroy(pbd_batch* b) { return pbd_destroy(as_sim(b)); }
+
+int pbd_batch_add_particles(pbd_batch* b, uint32_t scene, uint32_t n, const float* pos4, const float* vel4) {
+    clear_error();
+    pbd_sim* s = as_sim(b);
+    if (int rc = check_sim(s, "pbd_batch_add_particles")) return rc;
+    if (scene >= s->nscenes) { set_error("pbd_batch_add_particles: scene out of range"); return PBD_ERR_INVALID_ARG; }
+    if (n == 0) return PBD_OK;
+    if (!pos4 || !vel4) { set_error("pbd_batch_add_particles: null array"); return PBD_ERR_INVALID_ARG; }
+    if ((uint64_t)s->scene_count[scene] + n > s->scene_cap[scene]) {
+        set_error("pbd_batch_add_particles: scene " + std::to_string(scene) + " capacity " + std::to_string(s->scene_cap[scene]) + " exceeded");
+        return PBD_ERR_CAPACITY;
+    }
+    cudaStream_t st = s->last_stream;
+    const size_t off = s->N, bytes = (size_t)n * 16;
+    CK(cudaMemcpyAsync(s->x[s->cur.x] + off, pos4, bytes, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(s->v[s->cur.v] + off, vel4, bytes, cudaMemcpyHostToDevice, st));
+    fill_new_kernel<<<div_up(n, 256), 256, 0, st>>>(s->ids[s->cur.x], s->w[s->cur.x], 0, s->N, n);
+    fill_u32_kernel<<<div_up(n, 256), 256, 0, st>>>(s->scene_of, scene, s->N, n);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    s->N += n;
+    s->scene_count[scene] += n;
+    return PBD_OK;
+}
+
+int pbd_batch_step(pbd_batch* b, int nsteps, void* stream) { return pbd_step(as_sim(b), nsteps, stream); }
+int pbd_batch_sync(pbd_batch* b) { return pbd_sync(as_sim(b)); }
+int pbd_batch_num_particles(pbd_batch* b, uint32_t scene, uint32_t* n) {
+    clear_error();
+    pbd_sim* s = as_sim(b);
+    if (int rc = check_sim(s, "pbd_batch_num_particles")) return rc;
+    if (!n || scene >= s->nscenes) { set_error("pbd_batch_num_particles: bad argument"); return PBD_ERR_INVALID_ARG; }
+    *n = s->scene_count[scene];
+    return PBD_OK;
+}
+
+int pbd_batch_get_state(pbd_batch* b, uint32_t scene, float* pos4, float* vel4) {
+    clear_error();
+    pbd_sim* s = as_sim(b);
+    if (int rc = check_sim(s, "pbd_batch_get_state")) return rc;
+    if (scene >= s->nscenes) { set_error("pbd_batch_get_state: scene out of range"); return PBD_ERR_INVALID_ARG; }
+    if (int rc = sync_last(s)) return rc;
+    const size_t N = s->N;
+    std::vector<float4> x(N), v(N);
+    std::vector<uint32_t> sc(N);
+    CK(cudaMemcpy(x.data(), s->x[s->cur.x], N * 16, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(v.data(), s->v[s->cur.v], N * 16, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(sc.data(), s->scene_of, N * 4, cudaMemcpyDeviceToHost));
+    size_t k = 0;
+    for (size_t i = 0; i < N; ++i) {
+        if (sc[i] != scene) continue;
+        if (pos4) std::memcpy(pos4 + 4 * k, &x[i], 16);
+        if (vel4) std::memcpy(vel4 + 4 * k, &v[i], 16);
+        ++k;
+    }
+    return PBD_OK;
+}
+
+int pbd_batch_autotune(pbd_batch* b, const char* cache_path, void* stream, uint32_t* block) {
+    return pbd_autotune(as_sim(b), cache_path, stream, block);
+}
+
+int pbd_batch_launches_per_step(pbd_batch* b, uint32_t* n) { return pbd_launches_per_step(as_sim(b), n); }
+
+int pbd_batch_profile_frames(pbd_batch* b, int nsteps, void* stream, pbd_kernel_stat* stats, uint32_t max_stats,
+                             uint32_t* n_stats) {
+    return pbd_profile_frames(as_sim(b), nsteps, stream, stats, max_stats, n_stats);
 }
 
 }  // extern "C"

@@ -28,6 +28,9 @@ EXPORTED = [
     "pbd_add_particles", "pbd_add_particles_mass", "pbd_add_particles_device", "pbd_add_particle", "pbd_clear", "pbd_step", "pbd_sync",
     "pbd_get_state", "pbd_get_device_state", "pbd_debug_dump", "pbd_debug_neighbours", "pbd_debug_front",
     "pbd_launches_per_step", "pbd_profile_frames", "pbd_sort_keys_noalloc", "pbd_last_error", "pbd_abi_version",
+    "pbd_autotune", "pbd_batch_create", "pbd_batch_destroy", "pbd_batch_add_particles", "pbd_batch_step",
+    "pbd_batch_sync", "pbd_batch_num_particles", "pbd_batch_get_state", "pbd_batch_autotune",
+    "pbd_batch_launches_per_step", "pbd_batch_profile_frames",
 ]
 
 
@@ -57,6 +60,12 @@ class Params(C.Structure):
             v = getattr(self, name)
             d[name] = list(v) if not isinstance(v, (int, float)) else v
         return d
+
+
+class SceneDesc(C.Structure):
+    """pbd_scene_desc (include/pbd.h): the per-scene values of a batch."""
+    _fields_ = [("capacity", C.c_uint32), ("rest_density", C.c_float), ("gravity", C.c_float),
+                ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3)]
 
 
 class KernelStat(C.Structure):
@@ -96,6 +105,13 @@ def lib():
             "pbd_launches_per_step": [vp, u32p],
             "pbd_profile_frames": [vp, i32, vp, C.POINTER(KernelStat), u32, u32p],
             "pbd_sort_keys_noalloc": [vp, vp, vp, u32, u32, vp],
+            "pbd_autotune": [vp, C.c_char_p, vp, u32p],
+            "pbd_batch_create": [P, u32, C.POINTER(SceneDesc), C.POINTER(vp)], "pbd_batch_destroy": [vp],
+            "pbd_batch_add_particles": [vp, u32, u32, fp, fp], "pbd_batch_step": [vp, i32, vp],
+            "pbd_batch_sync": [vp], "pbd_batch_num_particles": [vp, u32, u32p],
+            "pbd_batch_get_state": [vp, u32, fp, fp], "pbd_batch_autotune": [vp, C.c_char_p, vp, u32p],
+            "pbd_batch_launches_per_step": [vp, u32p],
+            "pbd_batch_profile_frames": [vp, i32, vp, C.POINTER(KernelStat), u32, u32p],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -248,3 +264,82 @@ class Sim:
         v = C.c_uint32()
         check(self.L.pbd_launches_per_step(self.h, C.byref(v)))
         return v.value
+
+
+class Batch:
+    """A pbd_batch: many independent scenes stepped together."""
+
+    def __init__(self, shared_params, scene_descs):
+        self.L = lib()
+        self.h = C.c_void_p()
+        arr = (SceneDesc * len(scene_descs))(*scene_descs)
+        check(self.L.pbd_batch_create(C.byref(shared_params), len(scene_descs), arr, C.byref(self.h)))
+        self.nscenes = len(scene_descs)
+
+    def close(self):
+        if self.h:
+            self.L.pbd_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_particles(self, scene, pos4, vel4):
+        pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+        vel4 = np.ascontiguousarray(vel4, dtype=np.float32)
+        check(self.L.pbd_batch_add_particles(self.h, scene, pos4.shape[0], _fp(pos4), _fp(vel4)))
+
+    def step(self, nsteps=1, stream=0):
+        check(self.L.pbd_batch_step(self.h, nsteps, C.c_void_p(stream)))
+
+    def sync(self):
+        check(self.L.pbd_batch_sync(self.h))
+
+    def count(self, scene):
+        v = C.c_uint32()
+        check(self.L.pbd_batch_num_particles(self.h, scene, C.byref(v)))
+        return v.value
+
+    def state(self, scene):
+        n = self.count(scene)
+        x = np.zeros((n, 4), np.float32)
+        v = np.zeros((n, 4), np.float32)
+        check(self.L.pbd_batch_get_state(self.h, scene, _fp(x), _fp(v)))
+        return {"x": x, "v": v}
+
+    def autotune(self, cache_path=None, stream=0):
+        b = C.c_uint32()
+        check(self.L.pbd_batch_autotune(self.h, None if cache_path is None else os.fsencode(cache_path),
+                                        C.c_void_p(stream), C.byref(b)))
+        return b.value
+
+    def launches_per_step(self):
+        v = C.c_uint32()
+        check(self.L.pbd_batch_launches_per_step(self.h, C.byref(v)))
+        return v.value
+
+    def profile(self, nsteps, stream=0):
+        stats = (KernelStat * 32)()
+        n = C.c_uint32()
+        check(self.L.pbd_batch_profile_frames(self.h, nsteps, C.c_void_p(stream), stats, 32, C.byref(n)))
+        return {stats[k].name.decode(): (stats[k].launches, stats[k].total_ms) for k in range(n.value)}
+
+
+def scene_desc(capacity, rest_density, gravity, box):
+    d = SceneDesc()
+    d.capacity = capacity
+    d.rest_density = rest_density
+    d.gravity = gravity
+    for a in range(3):
+        d.bounds_min[a] = 1.5
+        d.bounds_max[a] = float(box) - 1.5
+    return d

@@ -115,6 +115,32 @@ def solids_scene(fluid_shape=(64, 64, 64), n_boxes=8, box_shape=(16, 16, 32), bo
     return pos, vel, w
 
 
+def batched_scenes(nscenes=256, seed=4, n_range=(4096, 65536), rho_range=(900.0, 1100.0),
+                   g_range=(8.0, 11.0), box_range=(32, 96)):
+    """Seeded batch of dam breaks: per scene a particle count, rest density, gravity magnitude and
+    cubic domain (cells per side), each drawn uniformly; a domain too small to hold its count as a
+    unit lattice cube with room to fall is raised to cbrt(n) + 8 cells.  The fluid block is a
+    lattice cube of that count in the domain's lower corner."""
+    u = uniform01(seed, 4 * nscenes).reshape(nscenes, 4)
+    out = []
+    for k in range(nscenes):
+        n = int(n_range[0] + u[k, 0] * (n_range[1] - n_range[0] + 1))
+        box = int(box_range[0] + u[k, 3] * (box_range[1] - box_range[0] + 1))
+        box = min(box_range[1], max(box, int(np.ceil(n ** (1.0 / 3.0))) + 8))
+        rho = float(rho_range[0] + u[k, 1] * (rho_range[1] - rho_range[0]))
+        g = -float(g_range[0] + u[k, 2] * (g_range[1] - g_range[0]))
+        side = box - 4                       # lattice columns that fit between the walls
+        nx = min(side, max(1, int(round(n ** (1.0 / 3.0)))))
+        nz = nx
+        ny = -(-n // (nx * nz))
+        if ny > side:                         # too tall: widen the base
+            nx = nz = side
+            ny = -(-n // (nx * nz))
+        pos, vel = lattice(nx, ny, nz, seed=seed * 1000 + k)
+        out.append(dict(n=n, rest_density=rho, gravity=g, box=box, pos=pos[:n], vel=vel[:n]))
+    return out
+
+
 WORKLOADS = {
     "dam_break_32k": dict(shape=(32, 32, 32), box=64, seed=1, vorticity=0.0, viscosity=0.0),
     "fluid_1m": dict(shape=(100, 100, 100), box=128, seed=2, vorticity=0.0005, viscosity=0.01),
