@@ -153,6 +153,198 @@ def cpu_baseline(name, max_seconds, threads=None):
             "sample": f"{name}: {len(pos)} particles x {frames} frames (after 1 untimed), {el:.1f} s, FP32 OpenMP"}
 
 
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def run_batched(torch, pbd, scenes, stream, sh, frames):
+    """256 seeded dam-break scenes (4K-65K particles, rest density 900-1100, |g| 8-11, domains
+    32-96 cells): scenes/s advanced as one batch vs the same scenes stepped one by one."""
+    sl = scenes.batched_scenes()
+    shared = scenes.workload_params(pbd, 64, REST_DENSITY)
+    shared.lambda_epsilon = LAMBDA_EPS
+    descs = [pbd.scene_desc(sc["n"], sc["rest_density"], sc["gravity"], sc["box"]) for sc in sl]
+    total = sum(sc["n"] for sc in sl)
+    tune_cache = os.environ.get("PBD_TUNE_CACHE", os.path.join(ROOT, "gpurun_out", "autotune.jsonl"))
+    os.makedirs(os.path.dirname(tune_cache), exist_ok=True)
+    with pbd.Batch(shared, descs) as tb:            # tuning copy: the autotuner advances frames
+        for k, sc in enumerate(sl):
+            tb.add_particles(k, sc["pos"], sc["vel"])
+        block = tb.autotune(tune_cache, stream=sh)
+        stream.synchronize()
+        tb.sync()
+    b = pbd.Batch(shared, descs)
+    for k, sc in enumerate(sl):
+        b.add_particles(k, sc["pos"], sc["vel"])
+    b.autotune(tune_cache, stream=sh)              # served from the cache: no frames consumed
+    b.step(3, stream=sh)
+    stream.synchronize()
+    e0, e1 = _events(torch)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    b.step(frames, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    b.sync()
+    ms_batch = e0.elapsed_time(e1) / frames
+    launches = b.launches_per_step()
+    b.close()
+    sims = []
+    for sc in sl:
+        p = shared.copy()
+        p.rest_density = sc["rest_density"]
+        p.gravity = sc["gravity"]
+        for a in range(3):
+            p.bounds_min[a] = 1.5
+            p.bounds_max[a] = sc["box"] - 1.5
+        x = pbd.Sim(p, sc["n"])
+        x.add_particles(sc["pos"], sc["vel"])
+        sims.append(x)
+    for x in sims:
+        x.step(3, stream=sh)
+    one_frames = max(5, frames // 4)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(one_frames):
+        for x in sims:
+            x.step(1, stream=sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_one = e0.elapsed_time(e1) / one_frames
+    for x in sims:
+        x.sync()
+        x.close()
+    return {"workload": "batched_256", "scenes": len(sl), "particles": total, "frames": frames,
+            "ms_per_frame": ms_batch, "scenes_per_s": len(sl) * 1e3 / ms_batch,
+            "particle_steps_per_s": total * 1e3 / ms_batch, "launches_per_frame": launches,
+            "neighbour_block": block, "one_by_one_ms_per_frame": ms_one,
+            "one_by_one_scenes_per_s": len(sl) * 1e3 / ms_one, "speedup_vs_one_by_one": ms_one / ms_batch}
+
+
+def run_solids(torch, pbd, scenes, stream, sh, frames):
+    """64^3 fluid + 8 static solid boxes (65,536 solids), 128^3 domain: particle-steps/s."""
+    pos, vel, w = scenes.solids_scene()
+    p = scenes.workload_params(pbd, 128, REST_DENSITY)
+    p.lambda_epsilon = LAMBDA_EPS
+    with pbd.Sim(p, len(pos)) as sim:
+        sim.add_particles_mass(pos, vel, w)
+        sim.step(3, stream=sh)
+        stream.synchronize()
+        e0, e1 = _events(torch)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.step(frames, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sim.sync()
+        ms = e0.elapsed_time(e1) / frames
+        st = sim.state()
+    solid_ids = np.nonzero(w == 0)[0]
+    return {"workload": "solids_328k", "particles": len(pos), "solid_particles": int(len(solid_ids)), "frames": frames,
+            "ms_per_frame": ms, "particle_steps_per_s": len(pos) * 1e3 / ms}
+
+
+def run_adjoint(torch, pbd, scenes, stream, sh, frames=60, every=10, fd_check=True, short=10):
+    """Differentiable dam break (65,536 particles, 60 frames x 4 iterations, checkpoints every
+    10): device time of forward+adjoint against the forward alone, and the gradient of
+    L = mean |x_final - target|^2 along a seeded direction of v0 and for rest density and eps,
+    against central differences of the FP64 oracle (the step 1e-3, and a step near the FP32
+    resolution of the parameter), at the full horizon and at a short one."""
+    pos, vel, target = scenes.adjoint_dam_break()
+    n = len(pos)
+    p = scenes.workload_params(pbd, 72, REST_DENSITY)
+    p.lambda_epsilon = LAMBDA_EPS
+    p.flags &= ~pbd.FLAG_CELL_END_QUIRK
+    p.flags |= pbd.FLAG_TRACK_IDS
+
+    def dl_dx(state):
+        g = np.zeros((n, 4), np.float32)
+        g[:, :3] = 2.0 * (state["x"][:, :3] - target[state["ids"]]) / n
+        return g
+
+    def gradients(sim, horizon):
+        sim.clear()
+        sim.add_particles(pos, vel)
+        sim.adjoint_forward(horizon, every, stream=sh)
+        fin = sim.state()
+        loss = float(np.mean(np.sum((fin["x"][:, :3] - target[fin["ids"]]) ** 2, axis=1)))
+        gv, gx, gr, ge = sim.adjoint_backward(dl_dx(fin), stream=sh)
+        return loss, gv, gr, ge
+
+    e0, e1 = _events(torch)
+    e2 = torch.cuda.Event(enable_timing=True)
+    with pbd.Sim(p, n) as sim:
+        loss, gv, gr, ge = gradients(sim, frames)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.step(frames, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_fwd = e0.elapsed_time(e1)
+        g = dl_dx(sim.state())
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.adjoint_forward(frames, every, stream=sh)
+        e2.record(stream)
+        sim.adjoint_backward(g, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_adj = e0.elapsed_time(e1)
+        ms_adj_fwd = e0.elapsed_time(e2)
+        short_grads = gradients(sim, short) if fd_check else None
+        sim.sync()
+    out = {"workload": "adjoint_64k", "particles": n, "frames": frames, "iterations": p.solver_iterations,
+           "checkpoint_every": every, "loss": loss, "forward_ms": ms_fwd, "forward_plus_adjoint_ms": ms_adj,
+           "adjoint_forward_ms": ms_adj_fwd, "adjoint_backward_ms": ms_adj - ms_adj_fwd,
+           "cost_ratio": ms_adj / ms_fwd, "dL_drest_density": gr, "dL_deps": ge,
+           "dL_dv0_norm": float(np.linalg.norm(gv[:, :3]))}
+    if fd_check:
+        from oracle import oracle as orc_mod
+        rng = np.random.default_rng(5)
+        dirn = rng.normal(size=(n, 3))
+
+        def oloss(prm, vel0, horizon):
+            o = orc_mod.Oracle(prm, n, "f64")
+            o.add_particles(pos, vel0)
+            o.step(horizon)
+            s2 = o.state()
+            o.close()
+            return float(np.mean(np.sum((s2["x"][:, :3] - target[s2["ids"]]) ** 2, axis=1)))
+
+        def fd_param(field, h, horizon):
+            pp, pm = p.copy(), p.copy()
+            setattr(pp, field, getattr(p, field) + h)
+            setattr(pm, field, getattr(p, field) - h)
+            step = float(np.float32(getattr(pp, field))) - float(np.float32(getattr(pm, field)))   # FP32 fields
+            return (oloss(pp, vel, horizon) - oloss(pm, vel, horizon)) / step
+
+        def fd_v0(h, horizon, gvh):
+            vp, vm = vel.copy(), vel.copy()
+            vp[:, :3] += (h * dirn).astype(np.float32)
+            vm[:, :3] -= (h * dirn).astype(np.float32)
+            step = vp[:, :3].astype(np.float64) - vm[:, :3].astype(np.float64)
+            return (oloss(p, vp, horizon) - oloss(p, vm, horizon)), float(np.sum(gvh[:, :3].astype(np.float64) * step))
+
+        def rel(a, b):
+            return abs(a - b) / max(abs(b), 1e-30)
+
+        t0 = time.perf_counter()
+        checks = {}
+        for horizon, (lo, gvh, grh, geh) in ((frames, (loss, gv, gr, ge)), (short, short_grads)):
+            c = {"loss": lo}
+            for name, field, ad, small in (("rest_density", "rest_density", grh, 1.25e-4), ("eps", "lambda_epsilon", geh, 1e-7)):
+                for h in (1e-3, small):
+                    fd = fd_param(field, h, horizon)
+                    c[f"{name}@h={h:g}"] = {"adjoint": ad, "fd_fp64": fd, "rel": rel(ad, fd)}
+            for h in (1e-3, 1e-6):
+                fd, ad = fd_v0(h, horizon, gvh)
+                c[f"v0_direction@h={h:g}"] = {"adjoint": ad, "fd_fp64": fd, "rel": rel(ad, fd)}
+            checks[f"{horizon}_frames"] = c
+        out["gradient_check"] = checks
+        out["gradient_check_s"] = time.perf_counter() - t0
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -279,6 +471,19 @@ def run_ours(args):
     e2e_value = n * e2e_steps * world / t_e2e
     sim.sync()
 
+    sim.close()
+    # ---- batched scenes and unified solids (same GPU, after the headline measurement)
+    def leg(fn, *a, **k):
+        # a failing secondary leg is reported in the line instead of losing the headline number
+        try:
+            return fn(*a, **k)
+        except Exception as e:  # noqa: BLE001
+            return {"error": f"{type(e).__name__}: {e}"}
+
+    batched = leg(run_batched, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 60)))
+    solids = leg(run_solids, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 100)))
+    adjoint = leg(run_adjoint, torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check)
+
     working_set = n * (16 * 3 + 16 * 3 + 4 + 16 + 16 * 2) + 2 * params.max_grid * 4
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -299,12 +504,14 @@ def run_ours(args):
                           "achieved_gbs": algorithmic_bytes_per_particle_step() * value / world / 1e9,
                           "frac": algorithmic_bytes_per_particle_step() * value / world / 1e9 / peak},
         "kernel_ms_per_frame": {k: v[1] / args.steps for k, v in prof.items()},
+        "batched": batched,
+        "solids": solids,
+        "adjoint": adjoint,
     }
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    sim.close()
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
@@ -319,6 +526,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fluid_1m")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-fd-check", action="store_true", help="skip the FP64 finite-difference check of the adjoint")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

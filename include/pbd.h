@@ -240,6 +240,25 @@ int pbd_batch_launches_per_step(pbd_batch* batch, uint32_t* n);
 int pbd_batch_profile_frames(pbd_batch* batch, int nsteps, void* stream, pbd_kernel_stat* stats,
                              uint32_t max_stats, uint32_t* n_stats);
 
+/* ---- adjoint ------------------------------------------------------------------------ */
+/* No counterpart in the reference.  Gradients of a loss on the final positions of a rollout
+ * with respect to the initial velocities and positions, the rest density and the relaxation
+ * eps of lambda (pbd_params.lambda_epsilon).
+ * pbd_adjoint_forward advances `nsteps` frames exactly as pbd_step does and keeps the state
+ * every `ckpt_every` frames (device memory allocated here, not in the frame).
+ * pbd_adjoint_backward takes dL/dx_final (host, N float4, in the order pbd_get_state returns
+ * after the forward) and returns dL/dv0 and dL/dx0 (host, N float4, in the order of the state
+ * before the forward; either may be NULL), dL/drest_density and dL/deps.  It recomputes each
+ * segment from its checkpoint (the last one is taped by the forward itself) with the neighbour
+ * lists, permutations and wall contacts of the forward held fixed (they are piecewise constant),
+ * and leaves the simulation as the forward left it; it may be called again for another loss on
+ * the same forward.  Supported: the density solve, contacts, walls and integration (vorticity,
+ * viscosity, solids, stabilizationIterations != 1 and enclosurePositionDamping != 0 return
+ * PBD_ERR_UNSUPPORTED). */
+int pbd_adjoint_forward(pbd_sim* sim, int nsteps, int ckpt_every, void* stream);
+int pbd_adjoint_backward(pbd_sim* sim, const float* dL_dx_final, float* dL_dv0, float* dL_dx0,
+                         double* dL_drest_density, double* dL_deps, void* stream);
+
 /* ---- sorting without allocation -------------------------------------------------- */
 /* No counterpart in the reference.  For hosts that cannot call cudaMalloc where they sort
  * (engines that own all device memory from start-up, frame loops that must not stall on an

@@ -1,0 +1,227 @@
+"""FP64 NumPy restatement of the frame and of its reverse pass (test infrastructure only).
+
+Only tests/ and bench.py's checks import this module; the shipped library never does.  It
+restates, for the adjoint's supported configuration (applyForces, the density solve with
+stabilizationIterations = 1, solveCollisions, updatePositions; no vorticity or viscosity,
+enclosurePositionDamping = 0, unit cell width, the cell-end quirk off), the frame that
+Fluid::compute runs (src/app/simulation/Fluid.cu:14-97):
+
+  applyForces     v* = v + g dt (y), p = x + v* dt, clamped to the walls  (kernel/Forces.h:65-101)
+  lists           j is a candidate of i when their anchor cells are adjacent (27 cells,
+                  kernel/Collision.h:11-66); the anchor is p right after the re-order
+  computeLambda   (kernel/Density.h:48-93)
+  computeDelta    (kernel/Density.h:104-145), solveCollisions (kernel/Collision.h:171-242),
+  applyDelta      p <- p + c - Delta, x <- x + c (Jacobi: all reads from the iteration's snapshot)
+  updatePositions v = (p - x)/dt, x = p (kernel/Update.h:11-32)
+
+Particles stay in id order here (the re-order is a permutation: it changes summation order
+only).  `rollout` runs frames and can keep a tape; `backward` returns dL/dv0, dL/dx0,
+dL/drest_density and dL/deps for L = sum(c . x_final) and is checked against central
+differences of `rollout` itself and against the C oracle's FP64 trajectory.
+"""
+import numpy as np
+
+PI = 3.14159265359    # Globals.h:122
+
+
+class Consts:
+    def __init__(self, prm):
+        d = 2.0 * prm.particle_radius
+        if abs(d - 1.0) > 1e-12:
+            raise ValueError("the restatement assumes a unit cell width (particle radius 0.5)")
+        self.d = d
+        self.dt = float(prm.delta_t)
+        self.g = float(prm.gravity)
+        self.rho0 = float(prm.rest_density)
+        self.eps = float(prm.lambda_epsilon)
+        self.hs = d * float(prm.kernel_width_spiky)
+        self.hp = float(prm.kernel_width_poly)
+        self.k = float(prm.k_scorr)
+        self.n = int(prm.n_scorr)
+        self.ac = 0.5 * (1.0 - float(prm.stiffness))
+        self.bmin = np.array([prm.bounds_min[a] for a in range(3)], np.float64)
+        self.bmax = np.array([prm.bounds_max[a] for a in range(3)], np.float64)
+        self.iters = int(prm.solver_iterations)
+        self.M = int(prm.max_neighbours_per_particle)
+        self.collide = prm.collision_type == 0
+        self.poly_inv_den = 1.0 / (0.001 + 64.0 * PI * self.hp ** 9)
+        self.spiky_k = 15.0 / (PI * self.hs ** 6)
+        q = self.hs * float(prm.q_scorr)
+        self.wq = self.poly6(np.array([q]))[0][0]
+        c = max(self.hp, self.hs, d)
+        self.cut2 = c * c * 1.0001
+
+    def poly6(self, L):
+        inside = (L > 0.001) & (L < self.hp - 0.001)
+        t = np.where(inside, self.hp * self.hp - L * L, 0.0)
+        W = 315.0 * t ** 6 * self.poly_inv_den
+        dW = -12.0 * L * 315.0 * t ** 5 * self.poly_inv_den
+        return np.where(inside, W, 0.0), np.where(inside, dW, 0.0)
+
+    def spiky(self, L):
+        inside = (L > 0.0001) & (self.hs - L > 0.0001)
+        a = np.where(inside, self.hs - L, 0.0)
+        return self.spiky_k * a * a, -2.0 * self.spiky_k * a
+
+
+def candidate_pairs(anchor, M):
+    """Directed pairs (i, j), i != j, whose anchor cells are adjacent (trunc of the clamped
+    position, Hash.h:21-29).  Raises if a list would reach the cap M (the cap cuts lists in
+    the reference's cell order, which this restatement does not follow)."""
+    cell = np.clip(anchor, 0.0, 1023.0).astype(np.int64)
+    n = len(cell)
+    key = (cell[:, 0] << 20) | (cell[:, 1] << 10) | cell[:, 2]
+    order = np.argsort(key, kind="stable")
+    skey = key[order]
+    I, J = [], []
+    for a in (-1, 0, 1):
+        for b in (-1, 0, 1):
+            for c in (-1, 0, 1):
+                nk = ((cell[:, 0] + a) << 20) | ((cell[:, 1] + b) << 10) | (cell[:, 2] + c)
+                ok = np.all((cell + np.array([a, b, c])) >= 0, axis=1) & np.all((cell + np.array([a, b, c])) <= 1023, axis=1)
+                lo = np.searchsorted(skey, nk, "left")
+                hi = np.searchsorted(skey, nk, "right")
+                cnt = np.where(ok, hi - lo, 0)
+                ii = np.repeat(np.arange(n), cnt)
+                start = np.repeat(lo - np.concatenate([[0], np.cumsum(cnt)[:-1]]), cnt)
+                jj = order[start + np.arange(len(ii))]
+                I.append(ii); J.append(jj)
+    I = np.concatenate(I); J = np.concatenate(J)
+    keep = I != J
+    I, J = I[keep], J[keep]
+    if n and np.bincount(I, minlength=n).max() >= M:
+        raise ValueError("a neighbour list reaches the cap")
+    return I, J
+
+
+def _pair_geometry(C, P, I, J):
+    r = P[I] - P[J]
+    r2 = np.einsum("ij,ij->i", r, r)
+    m = (r2 < C.cut2) & (r2 > 0.0)
+    I, J, r, r2 = I[m], J[m], r[m], r2[m]
+    L = np.sqrt(r2)
+    rh = r / L[:, None]
+    return I, J, r, L, rh
+
+
+def _sum(I, vals, n):
+    if vals.ndim == 1:
+        return np.bincount(I, weights=vals, minlength=n)
+    return np.stack([np.bincount(I, weights=vals[:, a], minlength=n) for a in range(vals.shape[1])], axis=1)
+
+
+def _lambda(C, n, I, L, rh):
+    W, dW = C.poly6(L)
+    g, dg = C.spiky(L)
+    rho = _sum(I, W, n)
+    B = _sum(I, g * g, n)
+    S = _sum(I, g[:, None] * rh, n)
+    s2 = np.einsum("ij,ij->i", S, S)
+    Cc = rho / C.rho0 - 1.0
+    D = (B + s2) / C.rho0 + C.eps
+    return -Cc / D, dict(W=W, dW=dW, g=g, dg=dg, rho=rho, B=B, S=S, s2=s2, C=Cc, D=D)
+
+
+def _predict(C, x, v):
+    vv = v.copy()
+    vv[:, 1] += C.g * C.dt
+    p = x + vv * C.dt
+    lo, hi = p < C.bmin, p > C.bmax
+    p = np.where(lo, C.bmin + 0.001, np.where(hi, C.bmax - 0.001, p))
+    return p, ~(lo | hi)
+
+
+def frame(C, x, v, tape=None):
+    """One frame on (n, 3) float64 positions and velocities; returns (x', v')."""
+    n = len(x)
+    p, _ = _predict(C, x, v)
+    I0, J0 = candidate_pairs(p, C.M)
+    if tape is not None:
+        tape.append(dict(x=x.copy(), v=v.copy(), I=I0, J=J0, p=[]))
+    x = x.copy()
+    for _ in range(C.iters):
+        if tape is not None:
+            tape[-1]["p"].append(p.copy())
+        I, J, r, L, rh = _pair_geometry(C, p, I0, J0)
+        lam, q = _lambda(C, n, I, L, rh)
+        sc = -C.k * (q["W"] / C.wq) ** C.n
+        coef = lam[I] + lam[J] + sc
+        delta = _sum(I, (coef * q["g"])[:, None] * rh, n) / C.rho0
+        c = np.zeros_like(p)
+        if C.collide:
+            ov = C.d - L
+            cm = (ov > 0.0) & (L > 0.00001)
+            c = _sum(I[cm], (C.ac * ov[cm])[:, None] * rh[cm], n)
+        p = p + c - delta
+        x = x + c
+    v = (p - x) / C.dt
+    return p.copy(), v
+
+
+def rollout(C, x, v, frames, tape=None):
+    for _ in range(frames):
+        x, v = frame(C, x, v, tape)
+    return x, v
+
+
+def _hess_mul(g, dg, L, rh, a):
+    ra = np.einsum("ij,ij->i", rh, a)
+    return dg[:, None] * ra[:, None] * rh + (g / L)[:, None] * (a - ra[:, None] * rh)
+
+
+def frame_backward(C, rec, gxo, gvo, acc):
+    """Reverse of `frame` for the taped record `rec`: (dL/dx', dL/dv') -> (dL/dx, dL/dv)."""
+    n = len(gxo)
+    gp = gxo + gvo / C.dt
+    gx = -gvo / C.dt
+    I0, J0 = rec["I"], rec["J"]
+    for it in range(C.iters - 1, -1, -1):
+        p = rec["p"][it]
+        I, J, r, L, rh = _pair_geometry(C, p, I0, J0)
+        lam, q = _lambda(C, n, I, L, rh)
+        W, dW, g, dg = q["W"], q["dW"], q["g"], q["dg"]
+        qq = W / C.wq
+        sc = -C.k * qq ** C.n
+        dsc = -C.k * C.n * qq ** (C.n - 1) * dW / C.wq if C.n != 0 else np.zeros_like(W)
+        coef = lam[I] + lam[J] + sc
+        G = g[:, None] * rh
+        # Delta and contacts
+        a = -gp / C.rho0
+        gd = np.einsum("ij,ij->i", G, a[I])
+        glam = _sum(I, gd, n) + _sum(J, gd, n)
+        rbar = coef[:, None] * _hess_mul(g, dg, L, rh, a[I]) + (gd * dsc)[:, None] * rh
+        if C.collide:
+            cbar = (gp + gx)[I]
+            ov = C.d - L
+            cm = ((ov > 0.0) & (L > 0.00001)).astype(np.float64)
+            rc = np.einsum("ij,ij->i", rh, cbar)
+            ol = ov / L
+            rbar += (C.ac * cm)[:, None] * (-rc[:, None] * rh + ol[:, None] * (cbar - rc[:, None] * rh))
+        sdelta = _sum(I, coef[:, None] * G, n)
+        acc[0] += float(np.sum(gp * sdelta)) / (C.rho0 * C.rho0)
+        gnew = gp + _sum(I, rbar, n) - _sum(J, rbar, n)
+        # lambda
+        Cbar = -glam / q["D"]
+        Dbar = glam * q["C"] / q["D"] ** 2
+        acc[0] += float(np.sum(Cbar * (-q["rho"] / C.rho0 ** 2) + Dbar * (-(q["B"] + q["s2"]) / C.rho0 ** 2)))
+        acc[1] += float(np.sum(Dbar))
+        S = q["S"]
+        rbar2 = (Cbar[I] / C.rho0 * dW)[:, None] * rh + (2.0 * Dbar[I] / C.rho0)[:, None] * _hess_mul(g, dg, L, rh, G + S[I])
+        gnew += _sum(I, rbar2, n) - _sum(J, rbar2, n)
+        gp = gnew
+    _, mask = _predict(C, rec["x"], rec["v"])
+    gx_in = gx + mask * gp
+    gv_in = mask * gp * C.dt
+    return gx_in, gv_in
+
+
+def backward(C, x0, v0, frames, weights):
+    """Gradients of L = sum(weights . x_final) (all (n, 3)); returns (dL/dv0, dL/dx0, dL/drho0, dL/deps)."""
+    tape = []
+    rollout(C, np.asarray(x0, np.float64), np.asarray(v0, np.float64), frames, tape)
+    gx = np.asarray(weights, np.float64).copy()
+    gv = np.zeros_like(gx)
+    acc = [0.0, 0.0]
+    for rec in reversed(tape):
+        gx, gv = frame_backward(C, rec, gx, gv, acc)
+    return gv, gx, acc[0], acc[1]

@@ -1,0 +1,297 @@
+// pbd_adjoint.cuh -- reverse-mode kernels of the frame (no counterpart in the reference).
+//
+// The frame's map (x, v) -> (x', v') with the neighbour list, the sort permutation and the wall
+// clamps held fixed (they are piecewise constant in the inputs):
+//   predict   p = x + (v + g dt + f dt) dt, clamped per component to the walls   (Forces.h:65-101)
+//   reorder   gather by the permutation                                           (SortReorder.h:86-115)
+//   I times   lambda_i = -(rho_i/rho0 - 1) / (B_i + |S_i|^2/rho0 + eps)             (Density.h:48-93)
+//             Delta_i = (1/rho0) sum_j (lambda_i + lambda_j + s_corr_ij) G_ij        (Density.h:104-145)
+//             c_i = sum_contacts 0.5 (1 - stiffness) (d - |r|) r_hat              (Collision.h:171-242)
+//             p <- p + c - Delta ;  x <- x + c
+//   update    v' = (p - x)/dt ; x' = p                                              (Update.h:11-32)
+// with r = p_i - p_j, G = spiky gradient g(|r|) r_hat, W = poly6.  The reverse passes scatter the
+// pair terms with atomic adds (so the neighbour relation need not be symmetric) and accumulate
+// dL/drest_density and dL/deps in double.
+#pragma once
+#include "pbd_passes.cuh"
+
+namespace pbd {
+
+// spiky magnitude g(L) = 15 (h - L)^2 / (pi h^6) and its derivative, inside the support
+__device__ __forceinline__ void spiky_g(const DevParams& P, float L, float& g, float& dg) {
+    if (L > 0.0001f && (P.hs - L) > 0.0001f) {
+        const float a = P.hs - L;
+        const float k = 15.0f * P.inv_spiky_den;
+        g = k * a * a;
+        dg = -2.0f * k * a;
+    } else {
+        g = 0.0f;
+        dg = 0.0f;
+    }
+}
+
+// poly6 W(L) = 315 (hp^2 - L^2)^6 / den and dW/dL, inside the support
+__device__ __forceinline__ void poly6_w(const DevParams& P, float L, float& W, float& dW) {
+    if (L > 0.001f && L < P.hp - 0.001f) {
+        const float t = P.hp2 - L * L;
+        const float t2 = t * t, t5 = t2 * t2 * t;
+        W = 315.0f * t5 * t * P.poly_inv_den;
+        dW = -12.0f * L * 315.0f * t5 * P.poly_inv_den;
+    } else {
+        W = 0.0f;
+        dW = 0.0f;
+    }
+}
+
+// H v for H = dG/dr = dg rhat rhat^T + (g/L)(I - rhat rhat^T)
+__device__ __forceinline__ float3 spiky_hess_mul(float g, float dg, float L, float3 rh, float3 v) {
+    const float rv = rh.x * v.x + rh.y * v.y + rh.z * v.z;
+    const float gl = g / L;
+    return make_float3(dg * rv * rh.x + gl * (v.x - rv * rh.x), dg * rv * rh.y + gl * (v.y - rv * rh.y),
+                       dg * rv * rh.z + gl * (v.z - rv * rh.z));
+}
+
+__device__ __forceinline__ void atomic_sub3(float4* a, float3 v) {
+    atomicAdd(&a->x, -v.x);
+    atomicAdd(&a->y, -v.y);
+    atomicAdd(&a->z, -v.z);
+}
+
+// Block-reduce two doubles and add them to the accumulators.
+__device__ __forceinline__ void block_add2(double a, double b, double* acc) {
+    __shared__ double sa[32], sb[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sa[warp] = a; sb[warp] = b; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) { ta += sa[w]; tb += sb[w]; }
+        if (ta != 0.0) atomicAdd(acc, ta);
+        if (tb != 0.0) atomicAdd(acc + 1, tb);
+    }
+}
+
+// update backward: pbar = xbar + vbar/dt, xbar = -vbar/dt   (sorted order of the frame)
+__global__ void adj_update_kernel(const DevParams P, const float4* __restrict__ gx_out, const float4* __restrict__ gv_out,
+                                  float4* __restrict__ gp, float4* __restrict__ gx) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const float4 a = gx_out[i], b = gv_out[i];
+    const float r = P.inv_dt;
+    gp[i] = make_float4(a.x + b.x * r, a.y + b.y * r, a.z + b.z * r, 0.f);
+    gx[i] = make_float4(-b.x * r, -b.y * r, -b.z * r, 0.f);
+}
+
+// Delta + contact backward for one iteration.  gp_in = dL/dp^{it+1}, gx = dL/dx^{it+1};
+// gp_out (pre-filled with gp_in) receives J^T terms; glam receives dL/dlambda (pre-zeroed).
+struct AdjDeltaVisit {
+    struct Contrib { int dummy; };
+    const DevParams& P;
+    const float* __restrict__ lambda;
+    float4 pi;
+    float li;
+    float3 a;          // Delta-bar / rho0
+    float3 cbar;       // dL/dc_i = gp_in + gx
+    float4* gp_out;
+    float* glam;
+    float3 gpi;        // this particle's own accumulated term
+    float3 sdelta;     // sum coef * G (for the rho0 term)
+    float glami;
+    bool collide;      // solveCollisions runs (collisionType 0)
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ static Contrib zero() { return Contrib{0}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool contact) {
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (r2 >= P.cut2 || r2 <= 0.0f) return zero();
+        const float L = sqrtf(r2);
+        const float3 rh = make_float3(rx / L, ry / L, rz / L);
+        float3 rbar = make_float3(0.f, 0.f, 0.f);
+        float g, dg;
+        spiky_g(P, L, g, dg);
+        if (g != 0.0f) {
+            float W, dW;
+            poly6_w(P, L, W, dW);
+            const float q = W * P.inv_wq;
+            const float sc = -P.k_scorr * powi(q, P.n_scorr);
+            const float dsc = P.n_scorr != 0 ? -P.k_scorr * (float)P.n_scorr * powi(q, P.n_scorr - 1) * dW * P.inv_wq : 0.0f;
+            const float lj = __ldg(lambda + j);
+            const float coef = li + lj + sc;
+            const float3 G = make_float3(g * rh.x, g * rh.y, g * rh.z);
+            const float gd = G.x * a.x + G.y * a.y + G.z * a.z;
+            glami += gd;
+            atomicAdd(glam + j, gd);
+            const float3 Ha = spiky_hess_mul(g, dg, L, rh, a);
+            rbar.x += coef * Ha.x + gd * dsc * rh.x;
+            rbar.y += coef * Ha.y + gd * dsc * rh.y;
+            rbar.z += coef * Ha.z + gd * dsc * rh.z;
+            sdelta.x += coef * G.x; sdelta.y += coef * G.y; sdelta.z += coef * G.z;
+        }
+        if (contact && collide) {
+            const float overlap = P.d - L;
+            if (overlap > 0.0f && L > 0.00001f) {
+                // f = ac (d - L) rhat, df/dr = ac [ -rhat rhat^T + (d - L)/L (I - rhat rhat^T) ]
+                const float ac = 0.5f * P.one_minus_stiffness;
+                const float rc = rh.x * cbar.x + rh.y * cbar.y + rh.z * cbar.z;
+                const float ol = overlap / L;
+                rbar.x += ac * (-rc * rh.x + ol * (cbar.x - rc * rh.x));
+                rbar.y += ac * (-rc * rh.y + ol * (cbar.y - rc * rh.y));
+                rbar.z += ac * (-rc * rh.z + ol * (cbar.z - rc * rh.z));
+            }
+        }
+        gpi.x += rbar.x; gpi.y += rbar.y; gpi.z += rbar.z;
+        atomic_sub3(gp_out + j, rbar);
+        return zero();
+    }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
+};
+
+__global__ void __launch_bounds__(128)
+adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float* __restrict__ lambda,
+                 const float4* __restrict__ gp_in, const float4* __restrict__ gx, float4* __restrict__ gp_out,
+                 float* __restrict__ glam, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, double* acc,
+                 bool collide) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double drho = 0.0;
+    if (i < P.N) {
+        const SceneCtx S = scene_ctx(P, i);
+        const float4 gpin = gp_in[i], gxi = gx[i];
+        const float inv = 1.0f / S.rho0;
+        AdjDeltaVisit vis{P, lambda, p[i], lambda[i],
+                          make_float3(-gpin.x * inv, -gpin.y * inv, -gpin.z * inv),
+                          make_float3(gpin.x + gxi.x, gpin.y + gxi.y, gpin.z + gxi.z), gp_out, glam,
+                          make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), 0.f, collide};
+        bool deferred = false;
+        walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
+        atomicAdd(&gp_out[i].x, vis.gpi.x);
+        atomicAdd(&gp_out[i].y, vis.gpi.y);
+        atomicAdd(&gp_out[i].z, vis.gpi.z);
+        atomicAdd(glam + i, vis.glami);
+        // Delta_i = sdelta / rho0: d/drho0 = -sdelta / rho0^2, Delta-bar = -gp_in
+        drho = (double)(gpin.x * vis.sdelta.x + gpin.y * vis.sdelta.y + gpin.z * vis.sdelta.z) * (double)(inv * inv);
+    }
+    block_add2(drho, 0.0, acc);
+}
+
+// lambda backward for one iteration: glam complete; adds J^T terms to gp_out, d/drho0, d/deps.
+// rho, B and S come from the forward's own sums (LambdaVisit::store_aux), so only the scatter
+// walk remains.
+struct AdjLambdaBwd {
+    struct Contrib { int dummy; };
+    const DevParams& P;
+    float4 pi;
+    float cbar_w;      // Cbar / rho0
+    float dbar2;       // 2 Dbar / rho0
+    float3 Sg;
+    float4* gp_out;
+    float3 gpi;
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ static Contrib zero() { return Contrib{0}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool) {
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (r2 >= P.cut2 || r2 <= 0.0f) return zero();
+        const float L = sqrtf(r2);
+        const float3 rh = make_float3(rx / L, ry / L, rz / L);
+        float g, dg, W, dW;
+        spiky_g(P, L, g, dg);
+        poly6_w(P, L, W, dW);
+        float3 rbar = make_float3(cbar_w * dW * rh.x, cbar_w * dW * rh.y, cbar_w * dW * rh.z);
+        if (g != 0.0f) {
+            const float3 v = make_float3(g * rh.x + Sg.x, g * rh.y + Sg.y, g * rh.z + Sg.z);
+            const float3 Hv = spiky_hess_mul(g, dg, L, rh, v);
+            rbar.x += dbar2 * Hv.x; rbar.y += dbar2 * Hv.y; rbar.z += dbar2 * Hv.z;
+        }
+        gpi.x += rbar.x; gpi.y += rbar.y; gpi.z += rbar.z;
+        atomic_sub3(gp_out + j, rbar);
+        return zero();
+    }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
+};
+
+__global__ void __launch_bounds__(128)
+adj_lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ aux,
+                  const float* __restrict__ glam, float4* __restrict__ gp_out, const uint32_t* __restrict__ cs,
+                  const uint32_t* __restrict__ ce, double* acc) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double drho = 0.0, deps = 0.0;
+    if (i < P.N) {
+        const SceneCtx S = scene_ctx(P, i);
+        const float lb = glam[i];
+        const float4 s0 = aux[i], s1 = aux[P.N + i];   // (rho, B, S.x, S.y), (S.z, S.w, 0, 0)
+        const float rho0 = S.rho0;
+        const float C = s0.x / rho0 - 1.0f;
+        const float BS = s0.y + (s0.z * s0.z + s0.w * s0.w + s1.x * s1.x + s1.y * s1.y);
+        const float D = BS / rho0 + P.lambda_eps;
+        const float Cbar = -lb / D;
+        const float Dbar = lb * C / (D * D);
+        const double r02 = (double)rho0 * rho0;
+        drho = (double)Cbar * (-(double)s0.x / r02) + (double)Dbar * (-(double)BS / r02);
+        deps = (double)Dbar;
+        if (lb != 0.0f) {
+            AdjLambdaBwd b{P, p[i], Cbar / rho0, 2.0f * Dbar / rho0, make_float3(s0.z, s0.w, s1.x), gp_out,
+                           make_float3(0.f, 0.f, 0.f)};
+            bool deferred = false;
+            walk_seq(P, S, i, pa[i], p, cs, ce, b, false, &deferred);
+            atomicAdd(&gp_out[i].x, b.gpi.x);
+            atomicAdd(&gp_out[i].y, b.gpi.y);
+            atomicAdd(&gp_out[i].z, b.gpi.z);
+        }
+    }
+    block_add2(drho, deps, acc);
+}
+
+// re-order + applyForces backward, fused: sorted slot i came from pre-sort slot o = perm[i];
+// x_pred = x (no positional damping), p = x + v* dt unless the wall clamp fired on that axis.
+__global__ void adj_predict_kernel(DevParams P, const uint32_t* __restrict__ perm, const float4* __restrict__ x_in,
+                                   const float4* __restrict__ v_in, const float4* __restrict__ fext,
+                                   const float4* __restrict__ gp, const float4* __restrict__ gxp,
+                                   float4* __restrict__ gx_out, float4* __restrict__ gv_out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const uint32_t o = perm[i];
+    const float4 xx = x_in[o], f = fext[o];
+    float4 vv = v_in[o];
+    const float dt = P.dt;
+    vv.y = __fmaf_rn(P.gravity, dt, vv.y);
+    vv.x = __fmaf_rn(f.x, dt, vv.x);
+    vv.y = __fmaf_rn(f.y, dt, vv.y);
+    vv.z = __fmaf_rn(f.z, dt, vv.z);
+    const float px = __fmaf_rn(vv.x, dt, xx.x), py = __fmaf_rn(vv.y, dt, xx.y), pz = __fmaf_rn(vv.z, dt, xx.z);
+    const float mx = (px < P.bmin[0] || px > P.bmax[0]) ? 0.f : 1.f;
+    const float my = (py < P.bmin[1] || py > P.bmax[1]) ? 0.f : 1.f;
+    const float mz = (pz < P.bmin[2] || pz > P.bmax[2]) ? 0.f : 1.f;
+    const float4 g = gp[i], gx = gxp[i];
+    gx_out[o] = make_float4(gx.x + mx * g.x, gx.y + my * g.y, gx.z + mz * g.z, 0.f);
+    gv_out[o] = make_float4(mx * g.x * dt, my * g.y * dt, mz * g.z * dt, 0.f);
+}
+
+// Rebuild the cell tables of a taped frame from its sorted keys (computeCellInfo,
+// SortReorder.h:160-188).  clear_keys/clear_n: the keys whose cells the tables hold now.
+__global__ void adj_clear_cells_kernel(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ cs,
+                                       uint32_t table_size) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = keys[i];
+        if (k < table_size) cs[k] = kEmptyCell;
+    }
+}
+
+__global__ void adj_set_cells_kernel(const uint32_t* __restrict__ skeys, uint32_t n, uint32_t* __restrict__ cs,
+                                     uint32_t* __restrict__ ce, uint32_t table_size) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t k = skeys[i];
+        if (k >= table_size) continue;
+        if (i == 0 || skeys[i - 1] != k) cs[k] = i;
+        if (i == n - 1 || skeys[i + 1] != k) ce[k] = i + 1;
+    }
+}
+
+}  // namespace pbd

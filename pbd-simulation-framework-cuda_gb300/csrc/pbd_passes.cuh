@@ -219,6 +219,11 @@ struct LambdaVisit {
         A += c.a; B += c.b;
         Cx += c.gx; Cy += c.gy; Cz += c.gz; Cw += c.gw;
     }
+    // the sums the reverse pass needs: aux[i] = (rho, B, S.x, S.y), aux[N + i] = (S.z, S.w, 0, 0)
+    __device__ __forceinline__ void store_aux(float4* __restrict__ aux, uint32_t N, uint32_t i) const {
+        aux[i] = make_float4(A, B, Cx, Cy);
+        aux[N + i] = make_float4(Cz, Cw, 0.f, 0.f);
+    }
     __device__ __forceinline__ float finish(float rho0) const {
         const float a = A / rho0 - 1.0f;
         const float b = B / rho0;
@@ -229,7 +234,7 @@ struct LambdaVisit {
 
 __global__ void __launch_bounds__(256)
 lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
-              const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D) {
+              const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D, float4* __restrict__ aux) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
@@ -242,16 +247,20 @@ lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restric
         walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
     lambda[i] = vis.finish(S.rho0);
+    if (aux) vis.store_aux(aux, P.N, i);
 }
 
 __global__ void __launch_bounds__(128)
 lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
-                   const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D) {
+                   const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D, float4* __restrict__ aux) {
     for_each_deferred(D, [&](uint32_t i) {
         const SceneCtx S = scene_ctx(P, i);
         LambdaVisit vis(P, p[i]);
         walk_coop(P, S, i, pa[i], p, cs, ce, vis);
-        if (lane_id() == 0) lambda[i] = vis.finish(S.rho0);
+        if (lane_id() == 0) {
+            lambda[i] = vis.finish(S.rho0);
+            if (aux) vis.store_aux(aux, P.N, i);
+        }
     });
 }
 

@@ -21,6 +21,7 @@
 
 #include "pbd_internal.h"
 #include "pbd_kernels.cuh"
+#include "pbd_adjoint.cuh"
 
 namespace pbd {
 thread_local std::string g_last_error;
@@ -46,6 +47,18 @@ inline uint32_t div_up(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) /
 
 }  // namespace
 
+// What the adjoint keeps of one frame (device buffers of N entries each).
+constexpr int kMaxTapeIters = 16;
+struct Tape {
+    float4* x_in;                  // state before applyForces (pre-sort order)
+    float4* v_in;
+    uint32_t* perm;                // sort permutation of the frame
+    uint32_t* keys;                // sorted keys (rebuild the frame's cell tables)
+    float4* p_it[kMaxTapeIters];   // p* entering each solver iteration (sorted order)
+    float* lam[kMaxTapeIters];     // lambda of each iteration
+    float4* aux[kMaxTapeIters];    // the lambda pass's sums (2N float4: rho, B, S)
+};
+
 struct pbd_sim {
     pbd_params prm{};
     uint32_t cap = 0, N = 0;
@@ -62,6 +75,21 @@ struct pbd_sim {
     SceneParams* d_scenes = nullptr;
     uint32_t* scene_of = nullptr;
     uint32_t* scene_range = nullptr;
+    // adjoint workspace (allocated by pbd_adjoint_forward)
+    void* adj_arena = nullptr;
+    size_t adj_bytes = 0;
+    int adj_steps = 0, adj_every = 0, adj_nck = 0;
+    uint32_t adj_n = 0;
+    float4 *adj_ck_x = nullptr, *adj_ck_v = nullptr, *adj_fin_x = nullptr, *adj_fin_v = nullptr;
+    uint32_t* adj_fin_keys = nullptr;
+    float4 *adj_fin_p = nullptr, *adj_fin_col = nullptr;
+    uint32_t* adj_fin_ids = nullptr;
+    std::vector<Tape> adj_tape;
+    float4 *adj_g[5]{};            // gradient buffers
+    float* adj_glam = nullptr;
+    bool adj_last_taped = false;   // the tape holds the forward's last segment
+    uint64_t gen = 0, adj_gen = 0; // bumped by every call that changes the state or parameters
+    double* adj_acc = nullptr;
     std::vector<uint32_t> scene_cap, scene_count;
     std::vector<SceneParams> h_scenes;
     float4 *fext = nullptr, *omega = nullptr, *delta = nullptr;
@@ -195,7 +223,7 @@ struct Profiler {
 
 // Record (or run) one frame of Fluid::compute (Fluid.cu:14-97) on `st`.
 cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only, uint32_t& nl,
-                          Profiler* prof = nullptr) {
+                          Profiler* prof = nullptr, const Tape* tape = nullptr) {
     const DevParams P = make_dev_params(s);
     const pbd_params& prm = s->prm;
     const uint32_t N = s->N;
@@ -207,6 +235,10 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     // applyForces + initializeCellIds (+ histograms, + clearing last frame's cells)
     const uint32_t total = std::max(N, s->table_hint);
     const uint32_t gpred = std::max(1u, std::min(div_up(total, kThreadsParticle), (uint32_t)s->num_sms * 8u));
+    if (tape) {
+        cudaMemcpyAsync(tape->x_in, s->x[cur.x], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(tape->v_in, s->v[cur.v], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
+    }
     PROF_BEGIN("predict_key");
     const float* wcur = s->mass_used ? s->w[cur.x] : nullptr;
     predict_key_kernel<<<gpred, kThreadsParticle, 0, st>>>(P, s->x[cur.x], s->v[cur.v], s->p[cur.p], s->fext, wcur,
@@ -228,6 +260,10 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     }
     // copy + reorder + computeCellInfo
     const int fin = np % 2;
+    if (tape) {
+        cudaMemcpyAsync(tape->perm, s->vals[fin], (size_t)N * 4, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(tape->keys, s->keys[fin], (size_t)N * 4, cudaMemcpyDeviceToDevice, st);
+    }
     const bool cols = (prm.flags & PBD_FLAG_COLORS) != 0, ids = (prm.flags & PBD_FLAG_TRACK_IDS) != 0;
     const int anchor = (cur.p + 1) % 3;   // this frame's anchor: never written again in the frame
     ReorderArgs A{s->keys[fin], s->vals[fin], s->x[cur.x], s->p[cur.p], s->v[cur.v], s->col[cur.x],
@@ -255,10 +291,16 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const bool collide = prm.collision_type == 0;
     bool last_was_delta = false;
     for (uint32_t it = 0; it < I; ++it) {
+        if (tape && it < (uint32_t)kMaxTapeIters)
+            cudaMemcpyAsync(tape->p_it[it], s->p[cur.p], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
+        // a taped frame keeps each iteration's lambda (and the sums behind it) for the reverse pass
+        const bool taped = tape && it < (uint32_t)kMaxTapeIters;
+        float* lam = taped ? tape->lam[it] : s->lambda;
+        float4* aux = taped ? tape->aux[it] : nullptr;
         if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
             PROF_BEGIN("lambda");
-            lambda_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, s->lambda, D);
-            lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, s->lambda, D);
+            lambda_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux);
+            lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux);
             PROF_END();
             nl += 2;
             last_was_delta = false;
@@ -284,9 +326,9 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             PROF_BEGIN("delta");
             const int pout = next_p(cur.p);
             delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
-                                                            s->v[cur.v], s->lambda, wf, s->delta, s->cell_start, s->cell_end, D);
+                                                            s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
             delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
-                                                           s->v[cur.v], s->lambda, wf, s->delta, s->cell_start, s->cell_end, D);
+                                                           s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
             PROF_END();
             nl += 2;
             cur.p = pout;
@@ -485,6 +527,7 @@ int pbd_destroy(pbd_sim* s) {
     if (!s) return PBD_OK;
     cudaDeviceSynchronize();
     destroy_graphs(s);
+    if (s->adj_arena) cudaFree(s->adj_arena);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     cudaError_t e = cudaFree(s->arena);
     delete s;
@@ -495,6 +538,7 @@ int pbd_destroy(pbd_sim* s) {
 int pbd_set_params(pbd_sim* s, const pbd_params* prm) {
     clear_error();
     if (int rc = check_sim(s, "pbd_set_params")) return rc;
+    ++s->gen;
     if (!prm) { set_error("pbd_set_params: null"); return PBD_ERR_INVALID_ARG; }
     if (int rc = pbd_validate_params(prm)) return rc;
     if (prm->collision_type != 0) { set_error("collisionType 1 (batched contact claims) is not implemented"); return PBD_ERR_UNSUPPORTED; }
@@ -524,6 +568,7 @@ int pbd_capacity(const pbd_sim* s, uint32_t* c) {
 
 static int add_common(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4,
                       const float* inv_mass, cudaMemcpyKind kind, cudaStream_t st, bool sync) {
+    ++s->gen;
     if (int rc = check_sim(s, "pbd_add_particles")) return rc;
     if (n == 0) return PBD_OK;
     if (!pos4 || !vel4) { set_error("pbd_add_particles: null position or velocity array"); return PBD_ERR_INVALID_ARG; }
@@ -575,6 +620,7 @@ int pbd_add_particles_device(pbd_sim* s, uint32_t n, const float* d_pos4, const 
 int pbd_add_particle(pbd_sim* s, const float pos[3], const float dir[3]) {
     clear_error();
     if (int rc = check_sim(s, "pbd_add_particle")) return rc;
+    ++s->gen;
     if (s->batched) { set_error("a batch takes particles per scene: pbd_batch_add_particles"); return PBD_ERR_INVALID_ARG; }
     if (!pos || !dir) { set_error("pbd_add_particle: null"); return PBD_ERR_INVALID_ARG; }
     if ((uint64_t)s->N + 1 > s->cap) { set_error("pbd_add_particle: capacity reached"); return PBD_ERR_CAPACITY; }
@@ -589,6 +635,7 @@ int pbd_add_particle(pbd_sim* s, const float pos[3], const float dir[3]) {
 int pbd_clear(pbd_sim* s) {
     clear_error();
     if (int rc = check_sim(s, "pbd_clear")) return rc;
+    ++s->gen;
     s->N = 0;   // Communication.h:657-660
     std::fill(s->scene_count.begin(), s->scene_count.end(), 0u);
     return PBD_OK;
@@ -597,6 +644,7 @@ int pbd_clear(pbd_sim* s) {
 int pbd_step(pbd_sim* s, int nsteps, void* stream) {
     clear_error();
     if (int rc = check_sim(s, "pbd_step")) return rc;
+    ++s->gen;
     if (nsteps < 0) { set_error("pbd_step: nsteps < 0"); return PBD_ERR_INVALID_ARG; }
     if (s->N == 0 || nsteps == 0) return PBD_OK;   // Fluid.cu:19
     cudaStream_t st = (cudaStream_t)stream;
@@ -706,6 +754,7 @@ int pbd_debug_neighbours(pbd_sim* s, uint32_t max_entries, uint32_t* list, uint3
 int pbd_debug_front(pbd_sim* s, void* stream) {
     clear_error();
     if (int rc = check_sim(s, "pbd_debug_front")) return rc;
+    ++s->gen;
     if (s->N == 0) return PBD_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
@@ -723,6 +772,7 @@ int pbd_profile_frames(pbd_sim* s, int nsteps, void* stream, pbd_kernel_stat* st
                        uint32_t* n_stats) {
     clear_error();
     if (int rc = check_sim(s, "pbd_profile_frames")) return rc;
+    ++s->gen;
     if (!stats || !n_stats || nsteps < 0) { set_error("pbd_profile_frames: bad argument"); return PBD_ERR_INVALID_ARG; }
     *n_stats = 0;
     if (s->N == 0 || nsteps == 0) return PBD_OK;
@@ -805,6 +855,7 @@ bool cache_lookup(const char* path, const std::string& sig, int* block) {
 int pbd_autotune(pbd_sim* s, const char* cache_path, void* stream, uint32_t* block) {
     clear_error();
     if (int rc = check_sim(s, "pbd_autotune")) return rc;
+    ++s->gen;
     if (s->N == 0) { set_error("pbd_autotune: no particles"); return PBD_ERR_INVALID_ARG; }
     const std::string sig = tune_signature(s);
     int best = 0;
@@ -949,4 +1000,196 @@ int pbd_batch_profile_frames(pbd_batch* b, int nsteps, void* stream, pbd_kernel_
     return pbd_profile_frames(as_sim(b), nsteps, stream, stats, max_stats, n_stats);
 }
 
+
+// ======================================================================================
+// Adjoint (no counterpart in the reference): checkpointed forward, taped recompute, reverse
+// ======================================================================================
+static int adjoint_supported(const pbd_sim* s) {
+    const pbd_params& p = s->prm;
+    const uint32_t need = PBD_ACTIVE_APPLY_FORCES | PBD_ACTIVE_FIND_CONTACTS | PBD_ACTIVE_COMPUTE_LAMBDA |
+                          PBD_ACTIVE_COMPUTE_DELTA_POSITIONS | PBD_ACTIVE_APPLY_DELTA_POSITIONS | PBD_ACTIVE_UPDATE_POSITIONS;
+    if ((p.active & need) != need) { set_error("adjoint: applyForces, findContacts, computeLambda, computeDeltaPositions, applyDeltaPositions and updatePositions must be active"); return PBD_ERR_UNSUPPORTED; }
+    if (p.active & (PBD_ACTIVE_COMPUTE_VORTICITY | PBD_ACTIVE_COMPUTE_VISCOSITY)) { set_error("adjoint: vorticity and viscosity have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
+    if (p.stabilization_iterations != 1 || p.solver_iterations == 0 || p.solver_iterations > (uint32_t)kMaxTapeIters) { set_error("adjoint: stabilizationIterations must be 1 and solverIterations 1..16"); return PBD_ERR_UNSUPPORTED; }
+    if (p.enclosure_position_damping != 0.0f) { set_error("adjoint: enclosurePositionDamping must be 0"); return PBD_ERR_UNSUPPORTED; }
+    if (s->mass_used || s->batched) { set_error("adjoint: solids and batches have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
+    return PBD_OK;
+}
+
+// Run `nf` frames with direct launches, keeping the tape of each (the cell tables must be
+// settled, as pbd_step leaves them).
+static int run_taped(pbd_sim* s, cudaStream_t st, int nf) {
+    for (int t = 0; t < nf; ++t) {
+        uint32_t nl = 0;
+        cudaError_t e = enqueue_frame(s, st, s->cur, false, nl, nullptr, &s->adj_tape[t]);
+        if (e != cudaSuccess) return cuda_fail("adjoint frame", e);
+        s->table_hint = s->N;
+    }
+    return PBD_OK;
+}
+
+int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_adjoint_forward")) return rc;
+    if (nsteps < 1 || ckpt_every < 1) { set_error("pbd_adjoint_forward: nsteps and ckpt_every must be >= 1"); return PBD_ERR_INVALID_ARG; }
+    if (s->N == 0) { set_error("pbd_adjoint_forward: no particles"); return PBD_ERR_INVALID_ARG; }
+    if (int rc = adjoint_supported(s)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
+    const size_t N = s->N;
+    const int k = std::min(ckpt_every, nsteps);
+    const int nck = (nsteps + k - 1) / k;
+    const uint32_t I = s->prm.solver_iterations;
+    // workspace: checkpoints, the final state, k frames of tape, gradient buffers
+    const size_t per_tape = N * (16 + 16 + 4 + 4) + (size_t)I * N * (16 + 4 + 32);
+    const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + 64 +
+                        (size_t)(16 + (4 + 3 * I) * k) * 256;
+    if (need > s->adj_bytes) {
+        if (s->adj_arena) CK(cudaStreamSynchronize(st));
+        if (s->adj_arena) cudaFree(s->adj_arena);
+        s->adj_arena = nullptr;
+        cudaError_t e = cudaMalloc(&s->adj_arena, need);
+        if (e != cudaSuccess) { s->adj_bytes = 0; set_error(std::string("adjoint workspace: ") + cudaGetErrorString(e)); return PBD_ERR_ALLOC; }
+        s->adj_bytes = need;
+    }
+    char* c = static_cast<char*>(s->adj_arena);
+    auto take = [&](size_t bytes) { char* r = c; c += (bytes + 255) & ~size_t(255); return r; };
+    s->adj_ck_x = (float4*)take((size_t)nck * N * 16);
+    s->adj_ck_v = (float4*)take((size_t)nck * N * 16);
+    s->adj_fin_x = (float4*)take(N * 16);
+    s->adj_fin_v = (float4*)take(N * 16);
+    s->adj_fin_p = (float4*)take(N * 16);
+    s->adj_fin_col = (float4*)take(N * 16);
+    s->adj_fin_keys = (uint32_t*)take(N * 4);
+    s->adj_fin_ids = (uint32_t*)take(N * 4);
+    s->adj_tape.assign(k, Tape{});
+    for (int t = 0; t < k; ++t) {
+        Tape& T = s->adj_tape[t];
+        T.x_in = (float4*)take(N * 16);
+        T.v_in = (float4*)take(N * 16);
+        T.perm = (uint32_t*)take(N * 4);
+        T.keys = (uint32_t*)take(N * 4);
+        for (uint32_t it = 0; it < I; ++it) {
+            T.p_it[it] = (float4*)take(N * 16);
+            T.lam[it] = (float*)take(N * 4);
+            T.aux[it] = (float4*)take(N * 32);
+        }
+    }
+    for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
+    s->adj_glam = (float*)take(N * 4);
+    s->adj_acc = (double*)take(64);
+    s->adj_steps = nsteps;
+    s->adj_every = k;
+    s->adj_nck = nck;
+    s->adj_n = s->N;
+    s->adj_last_taped = false;
+    for (int ck = 0; ck < nck; ++ck) {
+        const int nf = std::min(k, nsteps - ck * k);
+        CK(cudaMemcpyAsync(s->adj_ck_x + (size_t)ck * N, s->x[s->cur.x], N * 16, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(s->adj_ck_v + (size_t)ck * N, s->v[s->cur.v], N * 16, cudaMemcpyDeviceToDevice, st));
+        if (ck + 1 < nck) {
+            if (int rc = pbd_step(s, nf, stream)) return rc;
+        } else {
+            // the last segment keeps its tape now, so the reverse pass need not recompute it
+            if (s->dirty || s->graph_n != s->N || s->table_passes != sort_passes(s)) {
+                if (int rc = settle_tables(s, st)) return rc;
+                if (int rc = build_graphs(s)) return rc;
+            }
+            if (int rc = run_taped(s, st, nf)) return rc;
+        }
+    }
+    s->adj_last_taped = true;
+    s->adj_gen = s->gen;
+    const int fin = sort_passes(s) % 2;
+    CK(cudaMemcpyAsync(s->adj_fin_x, s->x[s->cur.x], N * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->adj_fin_v, s->v[s->cur.v], N * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->adj_fin_keys, s->keys[fin], N * 4, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->adj_fin_p, s->p[s->cur.p], N * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->adj_fin_col, s->col[s->cur.x], N * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->adj_fin_ids, s->ids[s->cur.x], N * 4, cudaMemcpyDeviceToDevice, st));
+    s->last_stream = st;
+    return PBD_OK;
+}
+
+// Make the cell tables hold the cells of `keys` (n sorted keys); `held` are the keys they hold now.
+static void retable(pbd_sim* s, cudaStream_t st, const uint32_t* held, const uint32_t* keys, uint32_t n) {
+    const uint32_t T = table_size(s);
+    const uint32_t g = std::max(1u, std::min(div_up(n, 256), (uint32_t)s->num_sms * 8u));
+    adj_clear_cells_kernel<<<g, 256, 0, st>>>(held, n, s->cell_start, T);
+    adj_set_cells_kernel<<<g, 256, 0, st>>>(keys, n, s->cell_start, s->cell_end, T);
+}
+
+int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, float* dL_dx0, double* dL_drho0,
+                         double* dL_deps, void* stream) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_adjoint_backward")) return rc;
+    if (!s->adj_arena || s->adj_steps == 0) { set_error("pbd_adjoint_backward: run pbd_adjoint_forward first"); return PBD_ERR_INVALID_ARG; }
+    if (s->N != s->adj_n || s->gen != s->adj_gen) { set_error("pbd_adjoint_backward: the state or the parameters changed since pbd_adjoint_forward"); return PBD_ERR_INVALID_ARG; }
+    if (!dL_dx_final) { set_error("pbd_adjoint_backward: null dL/dx"); return PBD_ERR_INVALID_ARG; }
+    if (int rc = adjoint_supported(s)) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
+    const uint32_t N = s->N, I = s->prm.solver_iterations;
+    const int fin = sort_passes(s) % 2;
+    float4 *gx_out = s->adj_g[0], *gv_out = s->adj_g[1], *gx = s->adj_g[2];
+    CK(cudaMemcpyAsync(gx_out, dL_dx_final, (size_t)N * 16, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(gv_out, 0, (size_t)N * 16, st));
+    CK(cudaMemsetAsync(s->adj_acc, 0, 64, st));
+    const bool collide = s->prm.collision_type == 0;
+    const uint32_t gn = div_up(N, 128), ge = div_up(N, 256);
+    const DevParams P = make_dev_params(s);
+    const uint32_t* held = s->keys[fin];       // the tables hold the cells of the last frame run
+    for (int ck = s->adj_nck - 1; ck >= 0; --ck) {
+        const int f0 = ck * s->adj_every;
+        const int nf = std::min(s->adj_every, s->adj_steps - f0);
+        if (ck + 1 < s->adj_nck || !s->adj_last_taped) {
+            // recompute the segment from its checkpoint, keeping the tape
+            CK(cudaMemcpyAsync(s->x[s->cur.x], s->adj_ck_x + (size_t)ck * N, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
+            CK(cudaMemcpyAsync(s->v[s->cur.v], s->adj_ck_v + (size_t)ck * N, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
+            if (int rc = run_taped(s, st, nf)) return rc;
+        }
+        held = s->adj_tape[nf - 1].keys;       // same contents as keys[fin] now
+        for (int t = nf - 1; t >= 0; --t) {
+            const Tape& T = s->adj_tape[t];
+            if (T.keys != held) { retable(s, st, held, T.keys, N); held = T.keys; }
+            // adj_update writes all of gp: each frame starts from the same pair of buffers
+            float4 *gp = s->adj_g[3], *gp2 = s->adj_g[4];
+            adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
+            for (int it = (int)I - 1; it >= 0; --it) {
+                const float4* p = T.p_it[it];
+                const float4* pa = T.p_it[0];
+                CK(cudaMemcpyAsync(gp2, gp, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
+                CK(cudaMemsetAsync(s->adj_glam, 0, (size_t)N * 4, st));
+                adj_delta_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.lam[it], gp, gx, gp2, s->adj_glam, s->cell_start,
+                                                     s->cell_end, s->adj_acc, collide);
+                adj_lambda_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.aux[it], s->adj_glam, gp2, s->cell_start, s->cell_end,
+                                                      s->adj_acc);
+                std::swap(gp, gp2);
+            }
+            adj_predict_kernel<<<ge, 256, 0, st>>>(P, T.perm, T.x_in, T.v_in, s->fext, gp, gx, gx_out, gv_out);
+            CK(cudaGetLastError());
+        }
+        // back to the tables the next recompute's predict expects: the cells of keys[fin]
+        retable(s, st, held, s->keys[fin], N);
+        held = s->keys[fin];
+    }
+    // restore the state after the forward: tables, sorted keys, x, v, p, colours and ids
+    retable(s, st, s->keys[fin], s->adj_fin_keys, N);
+    CK(cudaMemcpyAsync(s->keys[fin], s->adj_fin_keys, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->x[s->cur.x], s->adj_fin_x, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->v[s->cur.v], s->adj_fin_v, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->p[s->cur.p], s->adj_fin_p, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->col[s->cur.x], s->adj_fin_col, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(s->ids[s->cur.x], s->adj_fin_ids, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
+    s->adj_last_taped = s->adj_nck == 1;       // else the tape now holds the first segment
+    double acc[2] = {0.0, 0.0};
+    CK(cudaMemcpyAsync(acc, s->adj_acc, 16, cudaMemcpyDeviceToHost, st));
+    if (dL_dv0) CK(cudaMemcpyAsync(dL_dv0, gv_out, (size_t)N * 16, cudaMemcpyDeviceToHost, st));
+    if (dL_dx0) CK(cudaMemcpyAsync(dL_dx0, gx_out, (size_t)N * 16, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (dL_drho0) *dL_drho0 = acc[0];
+    if (dL_deps) *dL_deps = acc[1];
+    s->last_stream = st;
+    return PBD_OK;
+}
 }  // extern "C"

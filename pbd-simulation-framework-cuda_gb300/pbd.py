@@ -30,7 +30,7 @@ EXPORTED = [
     "pbd_launches_per_step", "pbd_profile_frames", "pbd_sort_keys_noalloc", "pbd_last_error", "pbd_abi_version",
     "pbd_autotune", "pbd_batch_create", "pbd_batch_destroy", "pbd_batch_add_particles", "pbd_batch_step",
     "pbd_batch_sync", "pbd_batch_num_particles", "pbd_batch_get_state", "pbd_batch_autotune",
-    "pbd_batch_launches_per_step", "pbd_batch_profile_frames",
+    "pbd_batch_launches_per_step", "pbd_batch_profile_frames", "pbd_adjoint_forward", "pbd_adjoint_backward",
 ]
 
 
@@ -112,6 +112,8 @@ def lib():
             "pbd_batch_get_state": [vp, u32, fp, fp], "pbd_batch_autotune": [vp, C.c_char_p, vp, u32p],
             "pbd_batch_launches_per_step": [vp, u32p],
             "pbd_batch_profile_frames": [vp, i32, vp, C.POINTER(KernelStat), u32, u32p],
+            "pbd_adjoint_forward": [vp, i32, i32, vp],
+            "pbd_adjoint_backward": [vp, fp, fp, fp, C.POINTER(C.c_double), C.POINTER(C.c_double), vp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -264,6 +266,19 @@ class Sim:
         v = C.c_uint32()
         check(self.L.pbd_launches_per_step(self.h, C.byref(v)))
         return v.value
+
+    def adjoint_forward(self, nsteps, ckpt_every, stream=0):
+        check(self.L.pbd_adjoint_forward(self.h, nsteps, ckpt_every, C.c_void_p(stream)))
+
+    def adjoint_backward(self, dl_dx_final, stream=0):
+        """Returns (dL/dv0, dL/dx0, dL/drest_density, dL/deps); arrays in the pre-forward order."""
+        g = np.ascontiguousarray(dl_dx_final, dtype=np.float32)
+        n = self.n
+        dv = np.zeros((n, 4), np.float32)
+        dx = np.zeros((n, 4), np.float32)
+        dr, de = C.c_double(), C.c_double()
+        check(self.L.pbd_adjoint_backward(self.h, _fp(g), _fp(dv), _fp(dx), C.byref(dr), C.byref(de), C.c_void_p(stream)))
+        return dv, dx, dr.value, de.value
 
 
 class Batch:

@@ -10,6 +10,7 @@ Workloads (kernel radius h = 1 = particle diameter, dt = 1/60, 4 solver iteratio
   fluid_1m        100^3 fluid particles in a 128^3-cell domain, vorticity 5e-4, XSPH 0.01, seed 2
   solids_328k     64^3 fluid particles + 8 static solid boxes of 8,192 particles (inverse mass 0)
                   in a 128^3-cell domain, seed 3
+  adjoint_64k     32 x 64 x 32 fluid column in a 72^3-cell box with a seeded target, seed 5
 """
 import numpy as np
 
@@ -139,6 +140,19 @@ def batched_scenes(nscenes=256, seed=4, n_range=(4096, 65536), rho_range=(900.0,
         pos, vel = lattice(nx, ny, nz, seed=seed * 1000 + k)
         out.append(dict(n=n, rest_density=rho, gravity=g, box=box, pos=pos[:n], vel=vel[:n]))
     return out
+
+
+def adjoint_dam_break(shape=(32, 64, 32), box=72, seed=5):
+    """Differentiable dam break: a unit lattice column of 65,536 particles (32 x 64 x 32) at rest
+    in a 72^3-cell box and a seeded target configuration (uniform in the lower half of the box
+    between the walls).  Returns pos, vel, target (n, 3) float64."""
+    pos, vel = lattice(*shape, seed=seed)
+    n = len(pos)
+    u = uniform01(seed + 7000, 3 * n).reshape(n, 3)
+    lo, hi = 2.0, box - 2.0
+    target = lo + u * (hi - lo)
+    target[:, 1] = lo + u[:, 1] * (box / 2.0 - lo)
+    return pos, vel, target
 
 
 WORKLOADS = {

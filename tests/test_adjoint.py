@@ -1,0 +1,218 @@
+"""Adjoint of the frame: dL/dv0, dL/dx0, dL/drest_density and dL/deps of L = sum(c . x_final).
+
+CPU: the FP64 restatement (oracle/adjoint.py) is pinned to the C oracle's FP64 trajectory and
+its reverse pass to central differences of its own forward.
+GPU: pbd_adjoint_forward/backward through the C ABI against that FP64 reverse pass on the same
+seeded scene, with several checkpoint spacings, and the state the forward left restored.
+Tolerance of the GPU gradients (FP32 forward and reverse, atomic scatter order): 2% of the
+largest component for the arrays, 2% for the scalars."""
+import copy
+
+import numpy as np
+import pytest
+
+from helpers import maxdiff
+
+FRAMES = 8
+
+
+def adjoint_scene(pbd, scenes, shape=(7, 7, 7), box=14, spacing=0.75, iterations=3, seed=5, vel_sigma=1.0):
+    prm = scenes.workload_params(pbd, box, 1000.0, iterations=iterations)
+    prm.lambda_epsilon = 0.1
+    prm.flags &= ~pbd.FLAG_CELL_END_QUIRK
+    prm.flags |= pbd.FLAG_TRACK_IDS
+    pos, vel = scenes.lattice(*shape, spacing=spacing, seed=seed)
+    rng = np.random.default_rng(seed)
+    vel[:, :3] = rng.normal(0, vel_sigma, size=(len(vel), 3)).astype(np.float32)
+    weights = rng.normal(size=(len(pos), 3))
+    return prm, pos, vel, weights
+
+
+@pytest.fixture(scope="module")
+def adj():
+    from oracle import adjoint as m
+    return m
+
+
+def test_restatement_follows_oracle(pbd, scenes, oracle_mod, adj):
+    prm, pos, vel, _ = adjoint_scene(pbd, scenes)
+    C = adj.Consts(prm)
+    o = oracle_mod.Oracle(prm, len(pos), "f64")
+    o.add_particles(pos, vel)
+    x, v = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+    for _ in range(FRAMES):
+        o.step(1)
+        x, v = adj.frame(C, x, v)
+    s = o.state()
+    order = np.argsort(s["ids"])
+    assert maxdiff(s["x"][order, :3], x) < 1e-8
+    assert maxdiff(s["v"][order, :3], v) < 1e-6
+
+
+def _loss(adj, C, x0, v0, w):
+    x, _ = adj.rollout(C, x0, v0, FRAMES)
+    return float(np.sum(w * x))
+
+
+def test_reverse_pass_matches_central_differences(pbd, scenes, adj):
+    prm, pos, vel, w = adjoint_scene(pbd, scenes)
+    C = adj.Consts(prm)
+    x0, v0 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+    gv, gx, gr, ge = adj.backward(C, x0, v0, FRAMES, w)
+    rng = np.random.default_rng(11)
+    dirn = rng.normal(size=x0.shape)
+    h = 1e-6
+    fd_v = (_loss(adj, C, x0, v0 + h * dirn, w) - _loss(adj, C, x0, v0 - h * dirn, w)) / (2 * h)
+    assert abs(fd_v - np.sum(gv * dirn)) <= 1e-4 * abs(fd_v)
+    fd_x = (_loss(adj, C, x0 + h * dirn, v0, w) - _loss(adj, C, x0 - h * dirn, v0, w)) / (2 * h)
+    assert abs(fd_x - np.sum(gx * dirn)) <= 1e-3 * abs(fd_x)
+    for attr, g in (("rho0", gr), ("eps", ge)):
+        base = getattr(C, attr)
+        hh = 1e-4 * base
+        cp, cm = copy.copy(C), copy.copy(C)
+        setattr(cp, attr, base + hh)
+        setattr(cm, attr, base - hh)
+        fd = (_loss(adj, cp, x0, v0, w) - _loss(adj, cm, x0, v0, w)) / (2 * hh)
+        assert abs(fd - g) <= 1e-3 * abs(fd), (attr, fd, g)
+
+
+def test_adjoint_symbols_and_argument_checks_declared(pbd):
+    L = pbd.lib()
+    assert hasattr(L, "pbd_adjoint_forward") and hasattr(L, "pbd_adjoint_backward")
+
+
+# ---------------------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------------------
+
+def _gpu_grads(pbd, prm, pos, vel, weights, frames, every):
+    sim = pbd.Sim(prm, len(pos))
+    sim.add_particles(pos, vel)
+    sim.adjoint_forward(frames, every)
+    fin = sim.state()
+    dl = np.zeros((len(pos), 4), np.float32)
+    dl[:, :3] = weights[fin["ids"]]
+    gv, gx, gr, ge = sim.adjoint_backward(dl)
+    after = sim.state()
+    return sim, fin, after, gv[:, :3], gx[:, :3], gr, ge
+
+
+def _close(a, b, rel=0.02):
+    return maxdiff(a, b) <= rel * max(1e-30, float(np.max(np.abs(b))))
+
+
+def _close_l2(a, b, rel=0.02):
+    """relative L2 error: robust to the few particles whose FP32 and FP64 trajectories meet a
+    wall clamp on different frames (the clamp zeroes that particle's gradient on that axis)"""
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b)) <= rel * float(np.linalg.norm(b))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("every", [FRAMES, 3, 1])
+def test_gpu_adjoint_matches_fp64(need_gpu, pbd, scenes, adj, every):
+    prm, pos, vel, w = adjoint_scene(pbd, scenes)
+    C = adj.Consts(prm)
+    rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), FRAMES, w)
+    sim, fin, after, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, FRAMES, every)
+    assert _close(gv, rv) and _close(gx, rx)
+    assert abs(gr - rr) <= 0.02 * abs(rr) and abs(ge - re) <= 0.02 * abs(re)
+    # the backward leaves the simulation as the forward left it
+    for k in ("x", "v", "p", "ids"):
+        assert np.array_equal(fin[k], after[k]), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("iterations", [1, 4])
+def test_gpu_adjoint_one_frame_exact(need_gpu, pbd, scenes, adj, iterations):
+    """one frame: the FP32 reverse pass equals the FP64 one up to FP32 rounding"""
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(12, 10, 12), box=20, iterations=iterations, seed=7)
+    C = adj.Consts(prm)
+    rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), 1, w)
+    _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, 1, 1)
+    assert _close_l2(gv, rv, 2e-5) and _close_l2(gx, rx, 2e-5)
+    assert abs(gr - rr) <= 2e-5 * abs(rr) and abs(ge - re) <= 2e-5 * abs(re)
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_larger_scene(need_gpu, pbd, scenes, adj):
+    """1,440 particles with random velocities: FP32 and FP64 trajectories drift apart quickly
+    here (5e-4 by frame 12), so the comparison stays at 5 frames (3 checkpoint segments)"""
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(12, 10, 12), box=20, iterations=4, seed=7)
+    C = adj.Consts(prm)
+    frames = 5
+    rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), frames, w)
+    sim, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, frames, 2)
+    assert _close_l2(gv, rv) and _close_l2(gx, rx)
+    assert abs(gr - rr) <= 0.02 * abs(rr) and abs(ge - re) <= 0.02 * abs(re)
+    # a second reverse pass on the same forward recomputes every segment: same gradients
+    fin = sim.state()
+    dl = np.zeros((len(pos), 4), np.float32)
+    dl[:, :3] = w[fin["ids"]]
+    gv2, gx2, gr2, ge2 = sim.adjoint_backward(dl)
+    assert _close(gv2[:, :3], gv, 1e-4) and _close(gx2[:, :3], gx, 1e-4)
+    assert abs(gr2 - gr) <= 1e-4 * abs(gr) and abs(ge2 - ge) <= 1e-4 * abs(ge)
+
+
+@pytest.mark.gpu
+def test_gpu_step_after_backward_is_unchanged(need_gpu, pbd, scenes):
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(10, 10, 10), box=18)
+    a = pbd.Sim(prm, len(pos)); a.add_particles(pos, vel)
+    b = pbd.Sim(prm, len(pos)); b.add_particles(pos, vel)
+    a.adjoint_forward(6, 4)
+    b.step(6)
+    dl = np.ones((len(pos), 4), np.float32)
+    a.adjoint_backward(dl)
+    a.step(3)
+    b.step(3)
+    sa, sb = a.state(), b.state()
+    for k in ("x", "v", "ids"):
+        assert np.array_equal(sa[k], sb[k]), k
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_rejects_unsupported(need_gpu, pbd, scenes):
+    prm, pos, vel, _ = adjoint_scene(pbd, scenes)
+    sim = pbd.Sim(prm, len(pos))
+    sim.add_particles(pos, vel)
+    with pytest.raises(pbd.PBDError) as e:
+        sim.adjoint_backward(np.zeros((len(pos), 4), np.float32))
+    assert e.value.code == pbd.ERR_INVALID_ARG
+    # a frame between the forward and the reverse pass invalidates the tape
+    sim.adjoint_forward(2, 1)
+    sim.step(1)
+    with pytest.raises(pbd.PBDError) as e:
+        sim.adjoint_backward(np.zeros((len(pos), 4), np.float32))
+    assert e.value.code == pbd.ERR_INVALID_ARG
+    p2 = pbd.Params.from_buffer_copy(prm)
+    p2.e_vorticity = 0.01
+    p2.active |= pbd.ACTIVE["computeOmegas"] | pbd.ACTIVE["computeVorticity"]
+    sim.set_params(p2)
+    with pytest.raises(pbd.PBDError) as e:
+        sim.adjoint_forward(2, 1)
+    assert e.value.code == pbd.ERR_UNSUPPORTED
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_through_torch_autograd(need_gpu, pbd, scenes, adj):
+    """mean squared distance to a seeded target, differentiated by torch through the shim"""
+    import torch
+    from adjoint_autograd import rollout
+    prm, pos, vel, _ = adjoint_scene(pbd, scenes, shape=(8, 8, 8), box=16, seed=9)
+    rng = np.random.default_rng(9)
+    target = rng.uniform(2.0, 14.0, size=(len(pos), 3))
+    sim = pbd.Sim(prm, len(pos))
+    v0 = torch.tensor(vel[:, :3], requires_grad=True)
+    rho0 = torch.tensor(float(prm.rest_density), dtype=torch.float64, requires_grad=True)
+    eps = torch.tensor(float(prm.lambda_epsilon), dtype=torch.float64, requires_grad=True)
+    x = rollout(sim, pos, v0, rho0, eps, FRAMES, 4)
+    loss = ((x.double() - torch.from_numpy(target)) ** 2).sum(dim=1).mean()
+    loss.backward()
+    C = adj.Consts(prm)
+    x0, vv0 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+    xf, _ = adj.rollout(C, x0, vv0, FRAMES)
+    w = 2.0 * (xf - target) / len(pos)
+    rv, _, rr, re = adj.backward(C, x0, vv0, FRAMES, w)
+    assert _close(v0.grad.numpy(), rv)
+    assert abs(float(rho0.grad) - rr) <= 0.02 * abs(rr)
+    assert abs(float(eps.grad) - re) <= 0.02 * abs(re)
