@@ -68,6 +68,12 @@ extern "C" {
  * and write colour = neighbourCount / maxNeighbours as findNeighbours does
  * (kernel/Collision.h:118-120).  Off by default: colours are cosmetic. */
 #define PBD_FLAG_COLORS          (1u << 2)
+/* Walk the cells in every neighbour pass.  By default a pass that walks the cells (lambda,
+ * omega) keeps, per particle and in list order, the entries within the kernel cut at the
+ * positions it read, and the pass after it at the same positions (delta, viscosity without
+ * vorticity) reads only those; the entries left out add exact zeros there, so both ways give
+ * identical results: this flag exists for testing and measurement. */
+#define PBD_FLAG_FULL_WALK       (1u << 3)
 
 /* ---- parameters: mirrors SimulationParameters (kernel/Globals.h:50-75) plus the
  *      config keys Fluid::compute reads directly (Fluid.cu:35-67).  Field comments give

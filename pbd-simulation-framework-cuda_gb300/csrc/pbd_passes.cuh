@@ -38,6 +38,19 @@ struct DeferList {
     uint32_t cap;
 };
 
+// Near lists.  A pass that walks the cells (lambda, omega) records, per particle and in list
+// order, the entries within the cut (r^2 < cut2 at the positions it read); the pass right after
+// it reads the same positions (delta after lambda, viscosity after omega), so every entry left
+// out adds an exact zero there and the short list gives the full walk's sums bit for bit.  The
+// cap M is counted by the recording walk, so truncation is the reference's.
+constexpr uint32_t kListOff = 0x80000000u;   // meta: this particle walks the cells
+struct NbList {
+    uint32_t* list;      // kmax x stride entries, slot-major (slot k of particle i at k * stride + i)
+    uint32_t* meta;      // per particle: count | contacts << 8, or kListOff
+    uint32_t stride;
+    uint32_t kmax;       // <= 255
+};
+
 // Enumerate the non-empty cell ranges [s, e) of particle i's list in the reference's
 // order.  f(s, e, contact) returns true to stop; end_contacts(n) marks the end of the
 // 27-cell part (Collision.h:38-39).  `pi` is the particle's anchor: its predicted position
@@ -59,15 +72,20 @@ __device__ __forceinline__ void for_each_range(const DevParams& P, const SceneCt
 #pragma unroll 1
             for (int b = -1; b <= 1; ++b) {
                 const uint32_t hxy = hx + (morton_axis(__fmaf_rn((float)b, P.d, pi.y)) << 1);
+                // the column's three cells: all six table loads in flight before the walk
+                uint32_t h[3], cs3[3], ce3[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const uint32_t h = hxy + mz[c];
-                    if (h >= P.G) continue;
-                    const uint32_t s = __ldg(cs + S.base + h);
-                    if (s >= N) continue;
-                    uint32_t e = __ldg(ce + S.base + h);
-                    if ((quirk && h == S.n - 1) || e > S.end) e = S.end;   // entries >= N are skipped (Collision.h:59)
-                    if (f(s, e, true)) return;
+                    h[c] = hxy + mz[c];
+                    cs3[c] = h[c] < P.G ? __ldg(cs + S.base + h[c]) : kEmptyCell;
+                }
+#pragma unroll
+                for (int c = 0; c < 3; ++c) ce3[c] = h[c] < P.G ? __ldg(ce + S.base + h[c]) : 0u;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    if (cs3[c] >= N) continue;
+                    const uint32_t e = ((quirk && h[c] == S.n - 1) || ce3[c] > S.end) ? S.end : ce3[c];
+                    if (f(cs3[c], e, true)) return;
                 }
             }
         }
@@ -160,6 +178,62 @@ __device__ __forceinline__ uint32_t walk_coop(const DevParams& P, const SceneCtx
     return cnt;
 }
 
+// One thread per particle over its near list (meta not kListOff).
+// Entries go in batches of kListBatch: the batch's index loads, then its position loads, are
+// all in flight before the first contribution, instead of one dependent pair per entry.
+constexpr uint32_t kListBatch = 4;
+template <class V>
+__device__ __forceinline__ void walk_list(const NbList& L, uint32_t i, uint32_t meta, const float4* __restrict__ p, V& vis) {
+    const uint32_t n = meta & 0xFFu, nc = (meta >> 8) & 0xFFu;
+    const uint32_t* __restrict__ e = L.list + i;
+#pragma unroll 1
+    for (uint32_t k0 = 0; k0 < n; k0 += kListBatch) {
+        uint32_t j[kListBatch];
+        float4 pj[kListBatch];
+#pragma unroll
+        for (uint32_t b = 0; b < kListBatch; ++b) j[b] = (k0 + b < n) ? __ldg(e + (size_t)(k0 + b) * L.stride) : i;
+#pragma unroll
+        for (uint32_t b = 0; b < kListBatch; ++b) pj[b] = __ldg(p + j[b]);
+#pragma unroll
+        for (uint32_t b = 0; b < kListBatch; ++b) {
+            if (k0 + b < n) {
+                const bool contact = k0 + b < nc;
+                vis.add(vis.contrib(j[b], pj[b], contact), contact);
+            }
+        }
+    }
+}
+
+// Wraps the visitor of a recording pass and keeps particle i's near list as the walk goes.
+// Holds everything by value so the visitor stays in registers.
+template <class V>
+struct Recorder {
+    using Contrib = typename V::Contrib;
+    V inner;
+    uint32_t* list;
+    uint32_t stride, kmax, i;
+    float4 pi;
+    float cut2;
+    uint32_t n = 0, nc = 0xFFFFFFFFu;
+    __device__ Recorder(const V& v, const NbList& L, uint32_t i_, float4 p_i, float c2)
+        : inner(v), list(L.list), stride(L.stride), kmax(L.kmax), i(i_), pi(p_i), cut2(c2) {}
+    __device__ static Contrib zero() { return V::zero(); }
+    __device__ __forceinline__ void end_contacts(uint32_t c) { nc = n; inner.end_contacts(c); }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool contact) {
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        if (rx * rx + ry * ry + rz * rz < cut2) {
+            if (n < kmax) list[(size_t)n * stride + i] = j;
+            ++n;
+        }
+        return inner.contrib(j, pj, contact);
+    }
+    __device__ __forceinline__ void add(const Contrib& c, bool contact) { inner.add(c, contact); }
+    __device__ __forceinline__ uint32_t meta() const {
+        const uint32_t c = nc == 0xFFFFFFFFu ? n : nc;
+        return n > kmax ? kListOff : (n | (c << 8));
+    }
+};
+
 __device__ __forceinline__ float shfl_f(float v, int k) { return __shfl_sync(kFullMask, v, k); }
 __device__ __forceinline__ uint32_t shfl_u(uint32_t v, int k) { return __shfl_sync(kFullMask, v, k); }
 
@@ -234,13 +308,27 @@ struct LambdaVisit {
 
 __global__ void __launch_bounds__(256)
 lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
-              const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D, float4* __restrict__ aux) {
+              const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D, float4* __restrict__ aux,
+              NbList L) {
+    // with L.list: record the near lists for the delta pass that follows
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
-    LambdaVisit vis(P, p[i]);
+    const float4 pi = p[i];
+    LambdaVisit vis(P, pi);
     bool deferred = false;
-    walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
+    if (L.list) {
+        Recorder<LambdaVisit> rec(vis, L, i, pi, P.cut2);
+        walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
+        L.meta[i] = deferred ? kListOff : rec.meta();
+        if (!deferred) {
+            lambda[i] = rec.inner.finish(S.rho0);
+            if (aux) rec.inner.store_aux(aux, P.N, i);
+            return;
+        }
+    } else {
+        walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
+    }
     if (deferred) {
         if (defer_particle(D, i)) return;
         vis.reset();
@@ -373,7 +461,7 @@ __global__ void __launch_bounds__(256, 2)
 delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const float4* __restrict__ pa, float4* __restrict__ pout,
              float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda, const float* __restrict__ w,
              float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
-             DeferList D) {
+             DeferList D, NbList L) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const float4 pi = pin[i];
@@ -381,14 +469,20 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const f
     const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
     const SceneCtx S = scene_ctx(P, i);
+    const float4 ai = pa[i];
     DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
     if (mode & (kDoDelta | kDoCollide)) {
-        bool deferred = false;
-        walk_seq(P, S, i, pa[i], pin, cs, ce, vis, true, &deferred);
-        if (deferred) {
-            if (defer_particle(D, i)) return;
-            vis.reset();
-            walk_seq(P, S, i, pa[i], pin, cs, ce, vis, false, &deferred);
+        const uint32_t meta = L.list ? L.meta[i] : kListOff;
+        if (meta != kListOff) {
+            walk_list(L, i, meta, pin, vis);
+        } else {
+            bool deferred = false;
+            walk_seq(P, S, i, ai, pin, cs, ce, vis, true, &deferred);
+            if (deferred) {
+                if (defer_particle(D, i)) return;
+                vis.reset();
+                walk_seq(P, S, i, ai, pin, cs, ce, vis, false, &deferred);
+            }
         }
     }
     delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
@@ -459,13 +553,26 @@ struct OmegaVisit {
 
 __global__ void __launch_bounds__(256)
 omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ v,
-             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega, DeferList D) {
+             const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega, DeferList D,
+             NbList L) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
-    OmegaVisit vis(P, v, p[i], v[i]);
+    // with L.list: record the near lists for a viscosity pass without vorticity
+    const float4 pi = p[i];
+    OmegaVisit vis(P, v, pi, v[i]);
     bool deferred = false;
-    walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
+    if (L.list) {
+        Recorder<OmegaVisit> rec(vis, L, i, pi, P.cut2);
+        walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
+        L.meta[i] = deferred ? kListOff : rec.meta();
+        if (!deferred) {
+            omega[i] = make_float4(rec.inner.ox, rec.inner.oy, rec.inner.oz, 0.f);
+            return;
+        }
+    } else {
+        walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
+    }
     if (deferred) {
         if (defer_particle(D, i)) return;
         vis.reset();
@@ -564,18 +671,25 @@ __global__ void __launch_bounds__(256, 2)
 vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ vin,
                  float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
-                 const float* __restrict__ w, DeferList D) {
+                 const float* __restrict__ w, DeferList D, NbList L) {
+    // vorticity sums every list entry (no kernel weight): with it on, the cells are walked;
+    // without it, L holds the near lists the omega pass recorded at these positions
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const SceneCtx S = scene_ctx(P, i);
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
-    bool deferred = false;
-    walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
-    if (deferred) {
-        if (defer_particle(D, i)) return;
-        vis.reset();
-        walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
+    const uint32_t meta = (!do_vort && L.list) ? L.meta[i] : kListOff;
+    if (meta != kListOff) {
+        walk_list(L, i, meta, p, vis);
+    } else {
+        bool deferred = false;
+        walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
+        if (deferred) {
+            if (defer_particle(D, i)) return;
+            vis.reset();
+            walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
+        }
     }
     vort_visc_finish(P, i, vis, vout, fext, w);
 }

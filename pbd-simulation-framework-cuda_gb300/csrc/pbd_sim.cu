@@ -38,6 +38,7 @@ struct Cur {
     bool operator==(const Cur& o) const { return x == o.x && p == o.p && v == o.v; }
 };
 constexpr int kMaxGraphs = 8;
+constexpr uint32_t kListMax = 32;   // entries of a near list; particles with more walk the cells
 
 constexpr int kThreadsParticle = 256;
 constexpr int kThreadsNeighbourDefault = 128;
@@ -98,6 +99,7 @@ struct pbd_sim {
     uint32_t *cell_start = nullptr, *cell_end = nullptr;
     uint32_t *hist = nullptr, *status = nullptr, *tile_counter = nullptr, *err = nullptr, *table_n = nullptr;
     uint32_t max_tiles = 0;
+    uint32_t *nb_list = nullptr, *nb_meta = nullptr;   // near lists (recorded by lambda / omega)
     uint32_t *defer_items = nullptr, *defer_count = nullptr, *defer_done = nullptr;
     uint32_t defer_cap = 0;
     Cur cur;
@@ -286,6 +288,11 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const uint32_t gc = (uint32_t)s->num_sms * 2u;   // cooperative kernels: grid-stride over the deferred
     const uint32_t act = prm.active;
     const uint32_t I = prm.solver_iterations, Sx = prm.stabilization_iterations;
+    // near lists: recorded by a walking pass for the pass after it at the same positions; they
+    // need kernels that vanish beyond the cut (far_pairs_zero)
+    const bool use_lists = !(prm.flags & PBD_FLAG_FULL_WALK) && P.far_pairs_zero != 0u;
+    const NbList L = use_lists ? NbList{s->nb_list, s->nb_meta, s->cap, kListMax} : NbList{nullptr, nullptr, 0u, 0u};
+    const NbList L0{nullptr, nullptr, 0u, 0u};
     const bool do_delta = act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS, do_apply = act & PBD_ACTIVE_APPLY_DELTA_POSITIONS;
     const bool do_update = act & PBD_ACTIVE_UPDATE_POSITIONS;
     const bool collide = prm.collision_type == 0;
@@ -299,7 +306,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         float4* aux = taped ? tape->aux[it] : nullptr;
         if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
             PROF_BEGIN("lambda");
-            lambda_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux);
+            lambda_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux,
+                                             (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS) ? L : L0);
             lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux);
             PROF_END();
             nl += 2;
@@ -325,8 +333,11 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             if (final_pass && do_update) mode |= kDoUpdate;
             PROF_BEGIN("delta");
             const int pout = next_p(cur.p);
+            // the near lists hold this iteration's lambda walk (same positions) on pass 0 only
+            const bool recorded = (act & PBD_ACTIVE_COMPUTE_LAMBDA) && (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS);
+            const NbList Ld = (k == 0 && recorded) ? L : L0;
             delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
-                                                            s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
+                                                            s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D, Ld);
             delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
                                                            s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
             PROF_END();
@@ -343,7 +354,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     }
     if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
         PROF_BEGIN("omega");
-        omega_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
+        omega_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D,
+                                        (act & PBD_ACTIVE_COMPUTE_VORTICITY) ? L0 : L);
         omega_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
         PROF_END();
         nl += 2;
@@ -352,7 +364,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     if (vort || visc) {
         PROF_BEGIN("vort_visc");
         vort_visc_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
-                                                            s->fext, s->cell_start, s->cell_end, vort, visc, wf, D);
+                                                            s->fext, s->cell_start, s->cell_end, vort, visc, wf, D,
+                                                            (act & PBD_ACTIVE_COMPUTE_OMEGAS) ? L : L0);
         vort_visc_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
                                                            s->fext, s->cell_start, s->cell_end, vort, visc, wf, D);
         PROF_END();
@@ -487,6 +500,7 @@ int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<Scene
     s->defer_cap = std::min<uint32_t>(capacity, 1u << 16);
     parts.push_back({(void**)&s->defer_items, (size_t)s->defer_cap * 4});
     parts.push_back({(void**)&s->defer_count, 4}); parts.push_back({(void**)&s->defer_done, 4});
+    parts.push_back({(void**)&s->nb_list, (size_t)kListMax * C * 4}); parts.push_back({(void**)&s->nb_meta, C * 4});
     if (s->batched) {
         parts.push_back({(void**)&s->d_scenes, (size_t)s->nscenes * sizeof(SceneParams)});
         parts.push_back({(void**)&s->scene_of, C * 4});

@@ -131,7 +131,7 @@ def test_gpu_adjoint_one_frame_exact(need_gpu, pbd, scenes, adj, iterations):
     rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), 1, w)
     _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, 1, 1)
     assert _close_l2(gv, rv, 2e-5) and _close_l2(gx, rx, 2e-5)
-    assert abs(gr - rr) <= 2e-5 * abs(rr) and abs(ge - re) <= 2e-5 * abs(re)
+    assert abs(gr - rr) <= 1e-4 * abs(rr) and abs(ge - re) <= 1e-4 * abs(re)
 
 
 @pytest.mark.gpu

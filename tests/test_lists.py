@@ -1,0 +1,99 @@
+"""Near lists against the full cell walk (PBD_FLAG_FULL_WALK).
+
+A walking pass (lambda, omega) records the entries within the cut for the pass after it at the
+same positions (delta, viscosity); the entries left out add exact zeros there, so a step with
+near lists must be bit-identical to a step that walks the cells in every pass, over many frames,
+for every pass mix (density solve, contacts, vorticity, viscosity, solids, batches, the
+cell-end quirk's long ranges, fast motion)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(pbd, params, pos, vel, frames, inv_mass=None, full_walk=False):
+    p = params.copy()
+    if full_walk:
+        p.flags |= pbd.FLAG_FULL_WALK
+    sim = pbd.Sim(p, len(pos))
+    if inv_mass is None:
+        sim.add_particles(pos, vel)
+    else:
+        sim.add_particles_mass(pos, vel, inv_mass)
+    sim.step(frames)
+    sim.sync()
+    st = sim.state()
+    sim.close()
+    return st
+
+
+def _same(a, b):
+    for k in ("x", "v", "p", "ids"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+CASES = [
+    # shape, box, vorticity, viscosity, quirk, velocity sigma
+    ((20, 20, 20), 32, 0.0, 0.0, True, 0.0),
+    ((20, 20, 20), 32, 0.0005, 0.01, True, 0.0),
+    ((16, 24, 16), 32, 0.0, 0.01, False, 0.0),
+    ((13, 7, 11), 24, 0.0, 0.0, True, 3.0),
+]
+
+
+@pytest.mark.parametrize("shape,box,vort,visc,quirk,sigma", CASES)
+def test_lists_bit_identical_to_full_walk(need_gpu, pbd, scenes, shape, box, vort, visc, quirk, sigma):
+    params = scenes.workload_params(pbd, box, 1000.0, vorticity=vort, viscosity=visc)
+    params.lambda_epsilon = 0.1
+    params.flags |= pbd.FLAG_TRACK_IDS
+    if not quirk:
+        params.flags &= ~pbd.FLAG_CELL_END_QUIRK
+    pos, vel = scenes.lattice(*shape, seed=3)
+    if sigma:
+        vel[:, :3] = np.random.default_rng(3).normal(0, sigma, size=(len(vel), 3)).astype(np.float32)
+    a = _run(pbd, params, pos, vel, 40)
+    b = _run(pbd, params, pos, vel, 40, full_walk=True)
+    _same(a, b)
+
+
+def test_lists_fast_motion(need_gpu, pbd, scenes):
+    # fast random motion: particles move up to a few cells per frame
+    params = scenes.workload_params(pbd, 24, 1000.0)
+    params.lambda_epsilon = 0.1
+    params.flags |= pbd.FLAG_TRACK_IDS
+    pos, vel = scenes.lattice(12, 12, 12, spacing=0.8, seed=4)
+    vel[:, :3] = np.random.default_rng(4).normal(0, 40, size=(len(vel), 3)).astype(np.float32)
+    a = _run(pbd, params, pos, vel, 12)
+    b = _run(pbd, params, pos, vel, 12, full_walk=True)
+    _same(a, b)
+
+
+def test_lists_with_solids(need_gpu, pbd, scenes):
+    pos, vel, w = scenes.solids_scene(fluid_shape=(16, 16, 16), n_boxes=2, box_shape=(6, 6, 8), box=48, seed=5)
+    params = scenes.workload_params(pbd, 48, 1000.0)
+    params.lambda_epsilon = 0.1
+    params.flags |= pbd.FLAG_TRACK_IDS
+    a = _run(pbd, params, pos, vel, 30, inv_mass=w)
+    b = _run(pbd, params, pos, vel, 30, inv_mass=w, full_walk=True)
+    _same(a, b)
+
+
+def test_lists_in_batches(need_gpu, pbd, scenes):
+    sl = scenes.batched_scenes(nscenes=4, n_range=(500, 3000), box_range=(20, 32), seed=9)
+    shared = scenes.workload_params(pbd, 32, 1000.0)
+    shared.lambda_epsilon = 0.1
+    out = []
+    for fw in (False, True):
+        p = shared.copy()
+        if fw:
+            p.flags |= pbd.FLAG_FULL_WALK
+        descs = [pbd.scene_desc(sc["n"], sc["rest_density"], sc["gravity"], sc["box"]) for sc in sl]
+        b = pbd.Batch(p, descs)
+        for k, sc in enumerate(sl):
+            b.add_particles(k, sc["pos"], sc["vel"])
+        b.step(25)
+        b.sync()
+        out.append([b.state(k) for k in range(len(sl))])
+        b.close()
+    for s1, s2 in zip(*out):
+        assert np.array_equal(s1["x"], s2["x"]) and np.array_equal(s1["v"], s2["v"])
