@@ -56,6 +56,9 @@ KERNEL_BYTES = {
     "vort_visc": 80,        # read p*, v, omega (48), write f_ext, v (32)
     "update": 64,
 }
+# the same passes over the stored lists (full or near) do the same algorithmic work
+for _k in ("lambda", "delta", "omega", "vort_visc"):
+    KERNEL_BYTES[_k + "_list"] = KERNEL_BYTES[_k]
 
 
 def dist_env():
@@ -420,7 +423,7 @@ def run_ours(args):
     launches, total_ms = prof[top]
     per_launch_s = total_ms / launches / 1e3
     bytes_per = KERNEL_BYTES.get(top, 0) * n
-    if top == "delta":
+    if top in ("delta", "delta_list"):
         # one of I delta launches also writes v: average the extra 16 B over the I launches
         bytes_per += 16 * n / params.solver_iterations
     achieved = bytes_per / per_launch_s / 1e9

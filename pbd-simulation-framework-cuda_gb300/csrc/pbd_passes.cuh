@@ -38,11 +38,15 @@ struct DeferList {
     uint32_t cap;
 };
 
-// Near lists.  A pass that walks the cells (lambda, omega) records, per particle and in list
-// order, the entries within the cut (r^2 < cut2 at the positions it read); the pass right after
-// it reads the same positions (delta after lambda, viscosity after omega), so every entry left
-// out adds an exact zero there and the short list gives the full walk's sums bit for bit.  The
-// cap M is counted by the recording walk, so truncation is the reference's.
+// Stored lists, both in the reference's list order, slot-major.
+//  - The full list: the frame's first lambda pass walks the cells once (the cells come from the
+//    frame's anchors, so the list is fixed for the frame) and stores every entry, up to the cap
+//    M; the later lambda passes, omega and vorticity read it instead of the cell tables.
+//  - The near list: a lambda or omega pass keeps the entries within the cut (r^2 < cut2 at the
+//    positions it read); the pass right after it reads the same positions (delta after lambda,
+//    viscosity after omega), so every entry left out adds an exact zero there and the short
+//    list gives the full walk's sums bit for bit.
+// A particle whose list does not fit (or whose walk met a long cell range) walks the cells.
 constexpr uint32_t kListOff = 0x80000000u;   // meta: this particle walks the cells
 struct NbList {
     uint32_t* list;      // kmax x stride entries, slot-major (slot k of particle i at k * stride + i)
@@ -178,52 +182,65 @@ __device__ __forceinline__ uint32_t walk_coop(const DevParams& P, const SceneCtx
     return cnt;
 }
 
-// One thread per particle over its near list (meta not kListOff).
-// Entries go in batches of kListBatch: the batch's index loads, then its position loads, are
-// all in flight before the first contribution, instead of one dependent pair per entry.
+// One thread per particle over a stored list (meta not kListOff): the contact entries, then
+// end_contacts, then the rest.  Entries go in batches of kListBatch: the batch's index loads,
+// then its position loads, are all in flight before the first contribution, instead of one
+// dependent pair per entry.
 constexpr uint32_t kListBatch = 4;
 template <class V>
-__device__ __forceinline__ void walk_list(const NbList& L, uint32_t i, uint32_t meta, const float4* __restrict__ p, V& vis) {
-    const uint32_t n = meta & 0xFFu, nc = (meta >> 8) & 0xFFu;
+__device__ __forceinline__ void walk_list_part(const NbList& L, uint32_t i, uint32_t k0, uint32_t k1, bool contact,
+                                               const float4* __restrict__ p, V& vis) {
     const uint32_t* __restrict__ e = L.list + i;
 #pragma unroll 1
-    for (uint32_t k0 = 0; k0 < n; k0 += kListBatch) {
+    for (uint32_t kb = k0; kb < k1; kb += kListBatch) {
         uint32_t j[kListBatch];
         float4 pj[kListBatch];
 #pragma unroll
-        for (uint32_t b = 0; b < kListBatch; ++b) j[b] = (k0 + b < n) ? __ldg(e + (size_t)(k0 + b) * L.stride) : i;
+        for (uint32_t b = 0; b < kListBatch; ++b) j[b] = (kb + b < k1) ? __ldg(e + (size_t)(kb + b) * L.stride) : i;
 #pragma unroll
         for (uint32_t b = 0; b < kListBatch; ++b) pj[b] = __ldg(p + j[b]);
 #pragma unroll
-        for (uint32_t b = 0; b < kListBatch; ++b) {
-            if (k0 + b < n) {
-                const bool contact = k0 + b < nc;
-                vis.add(vis.contrib(j[b], pj[b], contact), contact);
-            }
-        }
+        for (uint32_t b = 0; b < kListBatch; ++b)
+            if (kb + b < k1) vis.add(vis.contrib(j[b], pj[b], contact), contact);
     }
 }
+template <class V>
+__device__ __forceinline__ void walk_list(const NbList& L, uint32_t i, uint32_t meta, const float4* __restrict__ p, V& vis) {
+    const uint32_t n = meta & 0xFFu, nc = (meta >> 8) & 0xFFu;
+    walk_list_part(L, i, 0u, nc, true, p, vis);
+    vis.end_contacts(nc);
+    walk_list_part(L, i, nc, n, false, p, vis);
+}
 
-// Wraps the visitor of a recording pass and keeps particle i's near list as the walk goes.
-// Holds everything by value so the visitor stays in registers.
+// Wraps the visitor of a walking pass and keeps particle i's near list (when `list` is set)
+// and its full list (when `flist` is set) as the walk goes.  Holds everything by value so the
+// visitor stays in registers.
 template <class V>
 struct Recorder {
     using Contrib = typename V::Contrib;
     V inner;
     uint32_t* list;
-    uint32_t stride, kmax, i;
+    uint32_t* flist;
+    uint32_t stride, kmax, fkmax, i;
     float4 pi;
     float cut2;
-    uint32_t n = 0, nc = 0xFFFFFFFFu;
-    __device__ Recorder(const V& v, const NbList& L, uint32_t i_, float4 p_i, float c2)
-        : inner(v), list(L.list), stride(L.stride), kmax(L.kmax), i(i_), pi(p_i), cut2(c2) {}
+    uint32_t n = 0, nc = 0xFFFFFFFFu, fn = 0, fnc = 0xFFFFFFFFu;
+    __device__ Recorder(const V& v, const NbList& L, const NbList& F, bool full, uint32_t i_, float4 p_i, float c2)
+        : inner(v), list(L.list), flist(full ? F.list : nullptr), stride(L.list ? L.stride : F.stride), kmax(L.kmax),
+          fkmax(F.kmax), i(i_), pi(p_i), cut2(c2) {}
     __device__ static Contrib zero() { return V::zero(); }
-    __device__ __forceinline__ void end_contacts(uint32_t c) { nc = n; inner.end_contacts(c); }
+    __device__ __forceinline__ void end_contacts(uint32_t c) { nc = n; fnc = fn; inner.end_contacts(c); }
     __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool contact) {
-        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        if (rx * rx + ry * ry + rz * rz < cut2) {
-            if (n < kmax) list[(size_t)n * stride + i] = j;
-            ++n;
+        if (flist) {
+            if (fn < fkmax) flist[(size_t)fn * stride + i] = j;
+            ++fn;
+        }
+        if (list) {
+            const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            if (rx * rx + ry * ry + rz * rz < cut2) {
+                if (n < kmax) list[(size_t)n * stride + i] = j;
+                ++n;
+            }
         }
         return inner.contrib(j, pj, contact);
     }
@@ -231,6 +248,10 @@ struct Recorder {
     __device__ __forceinline__ uint32_t meta() const {
         const uint32_t c = nc == 0xFFFFFFFFu ? n : nc;
         return n > kmax ? kListOff : (n | (c << 8));
+    }
+    __device__ __forceinline__ uint32_t fmeta() const {
+        const uint32_t c = fnc == 0xFFFFFFFFu ? fn : fnc;
+        return fn > fkmax ? kListOff : (fn | (c << 8));
     }
 };
 
@@ -309,18 +330,20 @@ struct LambdaVisit {
 __global__ void __launch_bounds__(256)
 lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
               const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D, float4* __restrict__ aux,
-              NbList L) {
-    // with L.list: record the near lists for the delta pass that follows
+              NbList L, NbList F) {
+    // walks the cells; L.list: record the near lists for the delta pass that follows;
+    // F.list: store the full lists (the frame's first lambda pass)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
     const float4 pi = p[i];
     LambdaVisit vis(P, pi);
     bool deferred = false;
-    if (L.list) {
-        Recorder<LambdaVisit> rec(vis, L, i, pi, P.cut2);
+    if (L.list || F.list) {
+        Recorder<LambdaVisit> rec(vis, L, F, F.list != nullptr, i, pi, P.cut2);
         walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
-        L.meta[i] = deferred ? kListOff : rec.meta();
+        if (L.list) L.meta[i] = deferred ? kListOff : rec.meta();
+        if (F.list) F.meta[i] = deferred ? kListOff : rec.fmeta();
         if (!deferred) {
             lambda[i] = rec.inner.finish(S.rho0);
             if (aux) rec.inner.store_aux(aux, P.N, i);
@@ -350,6 +373,37 @@ lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __re
             if (aux) vis.store_aux(aux, P.N, i);
         }
     });
+}
+
+// The frame's later lambda passes: read the full list (no cell tables), record the near list.
+// A particle without a stored list is handed to lambda_coop_kernel (the deferral list holds
+// every particle, so the hand-off cannot fail).  Kept apart from lambda_kernel so that its
+// register budget is the list walk's alone.
+__global__ void __launch_bounds__(256)
+lambda_list_kernel(DevParams P, const float4* __restrict__ p, float* __restrict__ lambda, DeferList D,
+                   float4* __restrict__ aux, NbList L, NbList F) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const uint32_t fm = F.meta[i];
+    if (fm == kListOff) {
+        if (L.list) L.meta[i] = kListOff;
+        defer_particle(D, i);
+        return;
+    }
+    const SceneCtx S = scene_ctx(P, i);
+    const float4 pi = p[i];
+    if (L.list) {
+        Recorder<LambdaVisit> rec(LambdaVisit(P, pi), L, F, false, i, pi, P.cut2);
+        walk_list(F, i, fm, p, rec);
+        L.meta[i] = rec.meta();
+        lambda[i] = rec.inner.finish(S.rho0);
+        if (aux) rec.inner.store_aux(aux, P.N, i);
+    } else {
+        LambdaVisit vis(P, pi);
+        walk_list(F, i, fm, p, vis);
+        lambda[i] = vis.finish(S.rho0);
+        if (aux) vis.store_aux(aux, P.N, i);
+    }
 }
 
 // ======================================================================================
@@ -461,7 +515,7 @@ __global__ void __launch_bounds__(256, 2)
 delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const float4* __restrict__ pa, float4* __restrict__ pout,
              float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda, const float* __restrict__ w,
              float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
-             DeferList D, NbList L) {
+             DeferList D) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const float4 pi = pin[i];
@@ -469,22 +523,39 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const f
     const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
     const SceneCtx S = scene_ctx(P, i);
-    const float4 ai = pa[i];
     DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
     if (mode & (kDoDelta | kDoCollide)) {
-        const uint32_t meta = L.list ? L.meta[i] : kListOff;
-        if (meta != kListOff) {
-            walk_list(L, i, meta, pin, vis);
-        } else {
-            bool deferred = false;
-            walk_seq(P, S, i, ai, pin, cs, ce, vis, true, &deferred);
-            if (deferred) {
-                if (defer_particle(D, i)) return;
-                vis.reset();
-                walk_seq(P, S, i, ai, pin, cs, ce, vis, false, &deferred);
-            }
+        bool deferred = false;
+        walk_seq(P, S, i, pa[i], pin, cs, ce, vis, true, &deferred);
+        if (deferred) {
+            if (defer_particle(D, i)) return;
+            vis.reset();
+            walk_seq(P, S, i, pa[i], pin, cs, ce, vis, false, &deferred);
         }
     }
+    delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
+}
+
+// delta pass 0 of an iteration over the near lists its lambda pass recorded; particles
+// without one go to delta_coop_kernel.
+__global__ void __launch_bounds__(256)
+delta_list_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, float4* __restrict__ pout,
+                  float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
+                  const float* __restrict__ w, float4* __restrict__ delta, DeferList D, NbList L) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const uint32_t meta = L.meta[i];
+    if (meta == kListOff) {
+        defer_particle(D, i);
+        return;
+    }
+    const float4 pi = pin[i];
+    const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
+    const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
+    const SceneCtx S = scene_ctx(P, i);
+    DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
+    walk_list(L, i, meta, pin, vis);
     delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
 }
 
@@ -558,12 +629,12 @@ omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
-    // with L.list: record the near lists for a viscosity pass without vorticity
+    // walks the cells; L.list: record the near lists for a viscosity pass without vorticity
     const float4 pi = p[i];
     OmegaVisit vis(P, v, pi, v[i]);
     bool deferred = false;
     if (L.list) {
-        Recorder<OmegaVisit> rec(vis, L, i, pi, P.cut2);
+        Recorder<OmegaVisit> rec(vis, L, L, false, i, pi, P.cut2);
         walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
         L.meta[i] = deferred ? kListOff : rec.meta();
         if (!deferred) {
@@ -579,6 +650,32 @@ omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict
         walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
     omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
+}
+
+// omega over the full list (recording the near list when L.list); particles without one go to
+// omega_coop_kernel.
+__global__ void __launch_bounds__(256)
+omega_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ v, float4* __restrict__ omega,
+                  DeferList D, NbList L, NbList F) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const uint32_t fm = F.meta[i];
+    if (fm == kListOff) {
+        if (L.list) L.meta[i] = kListOff;
+        defer_particle(D, i);
+        return;
+    }
+    const float4 pi = p[i];
+    if (L.list) {
+        Recorder<OmegaVisit> rec(OmegaVisit(P, v, pi, v[i]), L, F, false, i, pi, P.cut2);
+        walk_list(F, i, fm, p, rec);
+        L.meta[i] = rec.meta();
+        omega[i] = make_float4(rec.inner.ox, rec.inner.oy, rec.inner.oz, 0.f);
+    } else {
+        OmegaVisit vis(P, v, pi, v[i]);
+        walk_list(F, i, fm, p, vis);
+        omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
+    }
 }
 
 __global__ void __launch_bounds__(128)
@@ -671,26 +768,38 @@ __global__ void __launch_bounds__(256, 2)
 vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ vin,
                  float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
-                 const float* __restrict__ w, DeferList D, NbList L) {
-    // vorticity sums every list entry (no kernel weight): with it on, the cells are walked;
-    // without it, L holds the near lists the omega pass recorded at these positions
+                 const float* __restrict__ w, DeferList D) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const SceneCtx S = scene_ctx(P, i);
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
-    const uint32_t meta = (!do_vort && L.list) ? L.meta[i] : kListOff;
-    if (meta != kListOff) {
-        walk_list(L, i, meta, p, vis);
-    } else {
-        bool deferred = false;
-        walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
-        if (deferred) {
-            if (defer_particle(D, i)) return;
-            vis.reset();
-            walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
-        }
+    bool deferred = false;
+    walk_seq(P, S, i, pa[i], p, cs, ce, vis, true, &deferred);
+    if (deferred) {
+        if (defer_particle(D, i)) return;
+        vis.reset();
+        walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
+    vort_visc_finish(P, i, vis, vout, fext, w);
+}
+
+// vorticity + viscosity over a stored list (the full list with vorticity, else the omega pass's
+// near list); particles without one go to vort_visc_coop_kernel.
+__global__ void __launch_bounds__(256)
+vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ vin,
+                      float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
+                      int do_vort, int do_visc, const float* __restrict__ w, DeferList D, NbList Lv) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const uint32_t meta = Lv.meta[i];
+    if (meta == kListOff) {
+        defer_particle(D, i);
+        return;
+    }
+    const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
+    walk_list(Lv, i, meta, p, vis);
     vort_visc_finish(P, i, vis, vout, fext, w);
 }
 

@@ -38,7 +38,10 @@ struct Cur {
     bool operator==(const Cur& o) const { return x == o.x && p == o.p && v == o.v; }
 };
 constexpr int kMaxGraphs = 8;
-constexpr uint32_t kListMax = 32;   // entries of a near list; particles with more walk the cells
+// Stored list capacities (slot-major, only the used slots are touched).  A particle whose list
+// is longer goes to the warp-cooperative cell walk.
+constexpr uint32_t kListMax = 64;    // near list: entries within the cut
+constexpr uint32_t kFullMax = 128;   // full list: every entry of the frame's list
 
 constexpr int kThreadsParticle = 256;
 constexpr int kThreadsNeighbourDefault = 128;
@@ -100,6 +103,7 @@ struct pbd_sim {
     uint32_t *hist = nullptr, *status = nullptr, *tile_counter = nullptr, *err = nullptr, *table_n = nullptr;
     uint32_t max_tiles = 0;
     uint32_t *nb_list = nullptr, *nb_meta = nullptr;   // near lists (recorded by lambda / omega)
+    uint32_t *fl_list = nullptr, *fl_meta = nullptr;   // full lists (recorded by the frame's first lambda)
     uint32_t *defer_items = nullptr, *defer_count = nullptr, *defer_done = nullptr;
     uint32_t defer_cap = 0;
     Cur cur;
@@ -293,6 +297,9 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const bool use_lists = !(prm.flags & PBD_FLAG_FULL_WALK) && P.far_pairs_zero != 0u;
     const NbList L = use_lists ? NbList{s->nb_list, s->nb_meta, s->cap, kListMax} : NbList{nullptr, nullptr, 0u, 0u};
     const NbList L0{nullptr, nullptr, 0u, 0u};
+    // full lists: stored by the first lambda pass of the frame (its walk of the anchor cells)
+    const bool use_full = !(prm.flags & PBD_FLAG_FULL_WALK) && (act & PBD_ACTIVE_COMPUTE_LAMBDA) && I > 0;
+    const NbList F = use_full ? NbList{s->fl_list, s->fl_meta, s->cap, kFullMax} : L0;
     const bool do_delta = act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS, do_apply = act & PBD_ACTIVE_APPLY_DELTA_POSITIONS;
     const bool do_update = act & PBD_ACTIVE_UPDATE_POSITIONS;
     const bool collide = prm.collision_type == 0;
@@ -305,9 +312,13 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         float* lam = taped ? tape->lam[it] : s->lambda;
         float4* aux = taped ? tape->aux[it] : nullptr;
         if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
-            PROF_BEGIN("lambda");
-            lambda_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux,
-                                             (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS) ? L : L0);
+            PROF_BEGIN((use_full && it > 0) ? "lambda_list" : "lambda");
+            const NbList Lr = (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS) ? L : L0;
+            if (use_full && it > 0)
+                lambda_list_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], lam, D, aux, Lr, F);
+            else
+                lambda_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux, Lr,
+                                                 use_full ? F : L0);
             lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux);
             PROF_END();
             nl += 2;
@@ -331,13 +342,17 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             if (mode == 0) continue;
             const bool final_pass = last && (it + 1 == I);
             if (final_pass && do_update) mode |= kDoUpdate;
-            PROF_BEGIN("delta");
+            const bool recorded = (act & PBD_ACTIVE_COMPUTE_LAMBDA) && (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS);
+            const bool by_list = k == 0 && recorded && use_lists;
+            PROF_BEGIN(by_list ? "delta_list" : "delta");
             const int pout = next_p(cur.p);
             // the near lists hold this iteration's lambda walk (same positions) on pass 0 only
-            const bool recorded = (act & PBD_ACTIVE_COMPUTE_LAMBDA) && (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS);
-            const NbList Ld = (k == 0 && recorded) ? L : L0;
-            delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
-                                                            s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D, Ld);
+            if (by_list)
+                delta_list_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                                     s->delta, D, L);
+            else
+                delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                                s->delta, s->cell_start, s->cell_end, D);
             delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
                                                            s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
             PROF_END();
@@ -353,19 +368,27 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         ++nl;
     }
     if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
-        PROF_BEGIN("omega");
-        omega_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D,
-                                        (act & PBD_ACTIVE_COMPUTE_VORTICITY) ? L0 : L);
+        PROF_BEGIN(use_full ? "omega_list" : "omega");
+        const NbList Lo = (act & PBD_ACTIVE_COMPUTE_VORTICITY) ? L0 : L;   // near lists for viscosity alone
+        if (use_full)
+            omega_list_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->omega, D, Lo, F);
+        else
+            omega_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D, Lo);
         omega_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
         PROF_END();
         nl += 2;
     }
     const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     if (vort || visc) {
-        PROF_BEGIN("vort_visc");
-        vort_visc_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
-                                                            s->fext, s->cell_start, s->cell_end, vort, visc, wf, D,
-                                                            (act & PBD_ACTIVE_COMPUTE_OMEGAS) ? L : L0);
+        // vorticity sums every list entry: the full list; viscosity alone: the omega pass's near list
+        const NbList Lv = vort ? F : ((act & PBD_ACTIVE_COMPUTE_OMEGAS) ? L : L0);
+        PROF_BEGIN(Lv.list ? "vort_visc_list" : "vort_visc");
+        if (Lv.list)
+            vort_visc_list_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->v[cur.v ^ 1], s->omega, s->fext,
+                                                     vort, visc, wf, D, Lv);
+        else
+            vort_visc_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega, s->fext,
+                                                s->cell_start, s->cell_end, vort, visc, wf, D);
         vort_visc_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
                                                            s->fext, s->cell_start, s->cell_end, vort, visc, wf, D);
         PROF_END();
@@ -497,10 +520,11 @@ int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<Scene
     parts.push_back({(void**)&s->status, (size_t)kMaxPasses * s->max_tiles * kRadix * 4});
     parts.push_back({(void**)&s->tile_counter, kMaxPasses * 4}); parts.push_back({(void**)&s->err, 4});
     parts.push_back({(void**)&s->table_n, 4});
-    s->defer_cap = std::min<uint32_t>(capacity, 1u << 16);
+    s->defer_cap = capacity;   // every particle can be handed to the cooperative kernels
     parts.push_back({(void**)&s->defer_items, (size_t)s->defer_cap * 4});
     parts.push_back({(void**)&s->defer_count, 4}); parts.push_back({(void**)&s->defer_done, 4});
     parts.push_back({(void**)&s->nb_list, (size_t)kListMax * C * 4}); parts.push_back({(void**)&s->nb_meta, C * 4});
+    parts.push_back({(void**)&s->fl_list, (size_t)kFullMax * C * 4}); parts.push_back({(void**)&s->fl_meta, C * 4});
     if (s->batched) {
         parts.push_back({(void**)&s->d_scenes, (size_t)s->nscenes * sizeof(SceneParams)});
         parts.push_back({(void**)&s->scene_of, C * 4});
