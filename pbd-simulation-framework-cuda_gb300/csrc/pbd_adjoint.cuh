@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(128)
 adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float* __restrict__ lambda,
                  const float4* __restrict__ gp_in, const float4* __restrict__ gx, float4* __restrict__ gp_out,
                  float* __restrict__ glam, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, double* acc,
-                 bool collide) {
+                 bool collide, NbList Lt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double drho = 0.0;
     if (i < P.N) {
@@ -167,8 +167,11 @@ adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
                           make_float3(-gpin.x * inv, -gpin.y * inv, -gpin.z * inv),
                           make_float3(gpin.x + gxi.x, gpin.y + gxi.y, gpin.z + gxi.z), gp_out, glam,
                           make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), 0.f, collide};
+        // the forward's near list of this iteration (the pairs within the cut), else the cells
+        const uint32_t meta = Lt.list ? Lt.meta[i] : kListOff;
         bool deferred = false;
-        walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
+        if (meta != kListOff) walk_list(Lt, i, meta, p, vis);
+        else walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
         atomicAdd(&gp_out[i].x, vis.gpi.x);
         atomicAdd(&gp_out[i].y, vis.gpi.y);
         atomicAdd(&gp_out[i].z, vis.gpi.z);
@@ -220,7 +223,7 @@ struct AdjLambdaBwd {
 __global__ void __launch_bounds__(128)
 adj_lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ aux,
                   const float* __restrict__ glam, float4* __restrict__ gp_out, const uint32_t* __restrict__ cs,
-                  const uint32_t* __restrict__ ce, double* acc) {
+                  const uint32_t* __restrict__ ce, double* acc, NbList Lt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double drho = 0.0, deps = 0.0;
     if (i < P.N) {
@@ -239,8 +242,10 @@ adj_lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __res
         if (lb != 0.0f) {
             AdjLambdaBwd b{P, p[i], Cbar / rho0, 2.0f * Dbar / rho0, make_float3(s0.z, s0.w, s1.x), gp_out,
                            make_float3(0.f, 0.f, 0.f)};
+            const uint32_t meta = Lt.list ? Lt.meta[i] : kListOff;
             bool deferred = false;
-            walk_seq(P, S, i, pa[i], p, cs, ce, b, false, &deferred);
+            if (meta != kListOff) walk_list(Lt, i, meta, p, b);
+            else walk_seq(P, S, i, pa[i], p, cs, ce, b, false, &deferred);
             atomicAdd(&gp_out[i].x, b.gpi.x);
             atomicAdd(&gp_out[i].y, b.gpi.y);
             atomicAdd(&gp_out[i].z, b.gpi.z);

@@ -221,18 +221,18 @@ struct Recorder {
     V inner;
     uint32_t* list;
     uint32_t* flist;
-    uint32_t stride, kmax, fkmax, i;
+    uint32_t stride, fstride, kmax, fkmax, i;
     float4 pi;
     float cut2;
     uint32_t n = 0, nc = 0xFFFFFFFFu, fn = 0, fnc = 0xFFFFFFFFu;
     __device__ Recorder(const V& v, const NbList& L, const NbList& F, bool full, uint32_t i_, float4 p_i, float c2)
-        : inner(v), list(L.list), flist(full ? F.list : nullptr), stride(L.list ? L.stride : F.stride), kmax(L.kmax),
+        : inner(v), list(L.list), flist(full ? F.list : nullptr), stride(L.stride), fstride(F.stride), kmax(L.kmax),
           fkmax(F.kmax), i(i_), pi(p_i), cut2(c2) {}
     __device__ static Contrib zero() { return V::zero(); }
     __device__ __forceinline__ void end_contacts(uint32_t c) { nc = n; fnc = fn; inner.end_contacts(c); }
     __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool contact) {
         if (flist) {
-            if (fn < fkmax) flist[(size_t)fn * stride + i] = j;
+            if (fn < fkmax) flist[(size_t)fn * fstride + i] = j;
             ++fn;
         }
         if (list) {

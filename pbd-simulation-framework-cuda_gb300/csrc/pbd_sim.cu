@@ -61,6 +61,8 @@ struct Tape {
     float4* p_it[kMaxTapeIters];   // p* entering each solver iteration (sorted order)
     float* lam[kMaxTapeIters];     // lambda of each iteration
     float4* aux[kMaxTapeIters];    // the lambda pass's sums (2N float4: rho, B, S)
+    uint32_t* near[kMaxTapeIters];       // each iteration's near lists (kListMax x N, slot-major)
+    uint32_t* near_meta[kMaxTapeIters];  // and their counts
 };
 
 struct pbd_sim {
@@ -93,6 +95,11 @@ struct pbd_sim {
     float* adj_glam = nullptr;
     bool adj_last_taped = false;   // the tape holds the forward's last segment
     uint64_t gen = 0, adj_gen = 0; // bumped by every call that changes the state or parameters
+    uint64_t pgen = 0;             // bumped by every call that changes the parameters, N or the block size
+    struct AdjGraph { Cur start; int nf; int kind; Cur end; cudaGraphExec_t exec; };   // kind: see adj_segment
+    std::vector<AdjGraph> adj_graphs;   // recorded segments of the adjoint
+    uint64_t adj_graphs_pgen = ~0ull;
+    void* adj_graphs_arena = nullptr;
     double* adj_acc = nullptr;
     std::vector<uint32_t> scene_cap, scene_count;
     std::vector<SceneParams> h_scenes;
@@ -227,6 +234,11 @@ struct Profiler {
 #define PROF_BEGIN(name) do { if (prof) prof->begin(name); } while (0)
 #define PROF_END() do { if (prof) prof->end(); } while (0)
 
+// Near lists need kernels that vanish beyond the cut (far_pairs_zero).
+static bool near_lists_on(const pbd_sim* s, const DevParams& P) {
+    return !(s->prm.flags & PBD_FLAG_FULL_WALK) && P.far_pairs_zero != 0u;
+}
+
 // Record (or run) one frame of Fluid::compute (Fluid.cu:14-97) on `st`.
 cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only, uint32_t& nl,
                           Profiler* prof = nullptr, const Tape* tape = nullptr) {
@@ -294,8 +306,9 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const uint32_t I = prm.solver_iterations, Sx = prm.stabilization_iterations;
     // near lists: recorded by a walking pass for the pass after it at the same positions; they
     // need kernels that vanish beyond the cut (far_pairs_zero)
-    const bool use_lists = !(prm.flags & PBD_FLAG_FULL_WALK) && P.far_pairs_zero != 0u;
-    const NbList L = use_lists ? NbList{s->nb_list, s->nb_meta, s->cap, kListMax} : NbList{nullptr, nullptr, 0u, 0u};
+    const bool use_lists = near_lists_on(s, P);
+    const NbList Lf = use_lists ? NbList{s->nb_list, s->nb_meta, s->cap, kListMax} : NbList{nullptr, nullptr, 0u, 0u};
+    const NbList L = Lf;
     const NbList L0{nullptr, nullptr, 0u, 0u};
     // full lists: stored by the first lambda pass of the frame (its walk of the anchor cells)
     const bool use_full = !(prm.flags & PBD_FLAG_FULL_WALK) && (act & PBD_ACTIVE_COMPUTE_LAMBDA) && I > 0;
@@ -311,6 +324,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         const bool taped = tape && it < (uint32_t)kMaxTapeIters;
         float* lam = taped ? tape->lam[it] : s->lambda;
         float4* aux = taped ? tape->aux[it] : nullptr;
+        // a taped frame records the iteration's near lists into the tape (the delta pass reads them there)
+        const NbList L = (taped && use_lists) ? NbList{tape->near[it], tape->near_meta[it], N, kListMax} : Lf;
         if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
             PROF_BEGIN((use_full && it > 0) ? "lambda_list" : "lambda");
             const NbList Lr = (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS) ? L : L0;
@@ -565,6 +580,7 @@ int pbd_destroy(pbd_sim* s) {
     if (!s) return PBD_OK;
     cudaDeviceSynchronize();
     destroy_graphs(s);
+    for (auto& g : s->adj_graphs) cudaGraphExecDestroy(g.exec);
     if (s->adj_arena) cudaFree(s->adj_arena);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     cudaError_t e = cudaFree(s->arena);
@@ -577,6 +593,7 @@ int pbd_set_params(pbd_sim* s, const pbd_params* prm) {
     clear_error();
     if (int rc = check_sim(s, "pbd_set_params")) return rc;
     ++s->gen;
+    ++s->pgen;
     if (!prm) { set_error("pbd_set_params: null"); return PBD_ERR_INVALID_ARG; }
     if (int rc = pbd_validate_params(prm)) return rc;
     if (prm->collision_type != 0) { set_error("collisionType 1 (batched contact claims) is not implemented"); return PBD_ERR_UNSUPPORTED; }
@@ -607,6 +624,7 @@ int pbd_capacity(const pbd_sim* s, uint32_t* c) {
 static int add_common(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4,
                       const float* inv_mass, cudaMemcpyKind kind, cudaStream_t st, bool sync) {
     ++s->gen;
+    ++s->pgen;
     if (int rc = check_sim(s, "pbd_add_particles")) return rc;
     if (n == 0) return PBD_OK;
     if (!pos4 || !vel4) { set_error("pbd_add_particles: null position or velocity array"); return PBD_ERR_INVALID_ARG; }
@@ -659,6 +677,7 @@ int pbd_add_particle(pbd_sim* s, const float pos[3], const float dir[3]) {
     clear_error();
     if (int rc = check_sim(s, "pbd_add_particle")) return rc;
     ++s->gen;
+    ++s->pgen;
     if (s->batched) { set_error("a batch takes particles per scene: pbd_batch_add_particles"); return PBD_ERR_INVALID_ARG; }
     if (!pos || !dir) { set_error("pbd_add_particle: null"); return PBD_ERR_INVALID_ARG; }
     if ((uint64_t)s->N + 1 > s->cap) { set_error("pbd_add_particle: capacity reached"); return PBD_ERR_CAPACITY; }
@@ -674,6 +693,7 @@ int pbd_clear(pbd_sim* s) {
     clear_error();
     if (int rc = check_sim(s, "pbd_clear")) return rc;
     ++s->gen;
+    ++s->pgen;
     s->N = 0;   // Communication.h:657-660
     std::fill(s->scene_count.begin(), s->scene_count.end(), 0u);
     return PBD_OK;
@@ -894,6 +914,7 @@ int pbd_autotune(pbd_sim* s, const char* cache_path, void* stream, uint32_t* blo
     clear_error();
     if (int rc = check_sim(s, "pbd_autotune")) return rc;
     ++s->gen;
+    ++s->pgen;
     if (s->N == 0) { set_error("pbd_autotune: no particles"); return PBD_ERR_INVALID_ARG; }
     const std::string sig = tune_signature(s);
     int best = 0;
@@ -1054,17 +1075,7 @@ static int adjoint_supported(const pbd_sim* s) {
     return PBD_OK;
 }
 
-// Run `nf` frames with direct launches, keeping the tape of each (the cell tables must be
-// settled, as pbd_step leaves them).
-static int run_taped(pbd_sim* s, cudaStream_t st, int nf) {
-    for (int t = 0; t < nf; ++t) {
-        uint32_t nl = 0;
-        cudaError_t e = enqueue_frame(s, st, s->cur, false, nl, nullptr, &s->adj_tape[t]);
-        if (e != cudaSuccess) return cuda_fail("adjoint frame", e);
-        s->table_hint = s->N;
-    }
-    return PBD_OK;
-}
+static int adj_segment(pbd_sim* s, cudaStream_t st, int nf, int kind);
 
 int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     clear_error();
@@ -1079,9 +1090,9 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     const int nck = (nsteps + k - 1) / k;
     const uint32_t I = s->prm.solver_iterations;
     // workspace: checkpoints, the final state, k frames of tape, gradient buffers
-    const size_t per_tape = N * (16 + 16 + 4 + 4) + (size_t)I * N * (16 + 4 + 32);
+    const size_t per_tape = N * (16 + 16 + 4 + 4) + (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4);
     const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + 64 +
-                        (size_t)(16 + (4 + 3 * I) * k) * 256;
+                        (size_t)(16 + (4 + 5 * I) * k) * 256;
     if (need > s->adj_bytes) {
         if (s->adj_arena) CK(cudaStreamSynchronize(st));
         if (s->adj_arena) cudaFree(s->adj_arena);
@@ -1111,6 +1122,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
             T.p_it[it] = (float4*)take(N * 16);
             T.lam[it] = (float*)take(N * 4);
             T.aux[it] = (float4*)take(N * 32);
+            T.near[it] = (uint32_t*)take(N * 4 * kListMax);
+            T.near_meta[it] = (uint32_t*)take(N * 4);
         }
     }
     for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
@@ -1133,7 +1146,7 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
                 if (int rc = settle_tables(s, st)) return rc;
                 if (int rc = build_graphs(s)) return rc;
             }
-            if (int rc = run_taped(s, st, nf)) return rc;
+            if (int rc = adj_segment(s, st, nf, 0)) return rc;
         }
     }
     s->adj_last_taped = true;
@@ -1157,6 +1170,94 @@ static void retable(pbd_sim* s, cudaStream_t st, const uint32_t* held, const uin
     adj_set_cells_kernel<<<g, 256, 0, st>>>(keys, n, s->cell_start, s->cell_end, T);
 }
 
+// The reverse pass of one segment: recompute its frames from the checkpoint already in the
+// state buffers (unless the tape holds them), then walk its frames backwards, and leave the cell
+// tables holding the cells of keys[fin] again.  Only enqueues work (it is recorded as a graph).
+static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf, bool recompute) {
+    const uint32_t N = s->N, I = s->prm.solver_iterations;
+    const int fin = sort_passes(s) % 2;
+    const DevParams P = make_dev_params(s);
+    const bool lists = near_lists_on(s, P);
+    const bool collide = s->prm.collision_type == 0;
+    const uint32_t gn = div_up(N, 128), ge = div_up(N, 256);
+    float4 *gx_out = s->adj_g[0], *gv_out = s->adj_g[1], *gx = s->adj_g[2];
+    if (recompute) {
+        for (int t = 0; t < nf; ++t) {
+            uint32_t nl = 0;
+            cudaError_t e = enqueue_frame(s, st, cur, false, nl, nullptr, &s->adj_tape[t]);
+            if (e != cudaSuccess) return e;
+        }
+    }
+    const uint32_t* held = s->adj_tape[nf - 1].keys;   // same contents as keys[fin]
+    for (int t = nf - 1; t >= 0; --t) {
+        const Tape& T = s->adj_tape[t];
+        if (T.keys != held) { retable(s, st, held, T.keys, N); held = T.keys; }
+        // adj_update writes all of gp: each frame starts from the same pair of buffers
+        float4 *gp = s->adj_g[3], *gp2 = s->adj_g[4];
+        adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
+        for (int it = (int)I - 1; it >= 0; --it) {
+            const float4* p = T.p_it[it];
+            const float4* pa = T.p_it[0];
+            const NbList Lt = lists ? NbList{T.near[it], T.near_meta[it], N, kListMax} : NbList{nullptr, nullptr, 0u, 0u};
+            cudaError_t e = cudaMemcpyAsync(gp2, gp, (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
+            if (e == cudaSuccess) e = cudaMemsetAsync(s->adj_glam, 0, (size_t)N * 4, st);
+            if (e != cudaSuccess) return e;
+            adj_delta_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.lam[it], gp, gx, gp2, s->adj_glam, s->cell_start,
+                                                 s->cell_end, s->adj_acc, collide, Lt);
+            adj_lambda_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.aux[it], s->adj_glam, gp2, s->cell_start, s->cell_end,
+                                                  s->adj_acc, Lt);
+            std::swap(gp, gp2);
+        }
+        adj_predict_kernel<<<ge, 256, 0, st>>>(P, T.perm, T.x_in, T.v_in, s->fext, gp, gx, gx_out, gv_out);
+    }
+    // back to the tables the next recompute's predict expects: the cells of keys[fin]
+    retable(s, st, held, s->keys[fin], N);
+    return cudaGetLastError();
+}
+
+// Run one adjoint segment from the current buffer record as a recorded graph (recorded on first
+// use and kept while the parameters, N, the block size and the workspace stay the same):
+// kind 0: nf taped forward frames; 1: recompute nf taped frames, then their reverse pass;
+// 2: the reverse pass of nf frames whose tape is already there.
+static int adj_segment(pbd_sim* s, cudaStream_t st, int nf, int kind) {
+    if (s->adj_graphs_pgen != s->pgen || s->adj_graphs_arena != s->adj_arena || s->adj_graphs.size() >= 16) {
+        CK(cudaStreamSynchronize(st));
+        for (auto& g : s->adj_graphs) cudaGraphExecDestroy(g.exec);
+        s->adj_graphs.clear();
+        s->adj_graphs_pgen = s->pgen;
+        s->adj_graphs_arena = s->adj_arena;
+    }
+    pbd_sim::AdjGraph* g = nullptr;
+    for (auto& h : s->adj_graphs)
+        if (h.start == s->cur && h.nf == nf && h.kind == kind) { g = &h; break; }
+    if (!g) {
+        pbd_sim::AdjGraph h{s->cur, nf, kind, s->cur, nullptr};
+        CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        if (kind == 0) {
+            for (int t = 0; t < nf && e == cudaSuccess; ++t) {
+                uint32_t nl = 0;
+                e = enqueue_frame(s, s->cap_stream, h.end, false, nl, nullptr, &s->adj_tape[t]);
+            }
+        } else {
+            e = enqueue_segment(s, s->cap_stream, h.end, nf, kind == 1);
+        }
+        cudaGraph_t graph = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(s->cap_stream, &graph);
+        if (e != cudaSuccess) { if (graph) cudaGraphDestroy(graph); return cuda_fail("adjoint segment capture", e); }
+        if (e2 != cudaSuccess) return cuda_fail("cudaStreamEndCapture", e2);
+        e = cudaGraphInstantiate(&h.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return cuda_fail("cudaGraphInstantiate", e);
+        s->adj_graphs.push_back(h);
+        g = &s->adj_graphs.back();
+    }
+    CK(cudaGraphLaunch(g->exec, st));
+    s->cur = g->end;
+    s->table_hint = s->N;
+    return PBD_OK;
+}
+
 int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, float* dL_dx0, double* dL_drho0,
                          double* dL_deps, void* stream) {
     clear_error();
@@ -1167,49 +1268,21 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
     if (int rc = adjoint_supported(s)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
-    const uint32_t N = s->N, I = s->prm.solver_iterations;
+    const uint32_t N = s->N;
     const int fin = sort_passes(s) % 2;
-    float4 *gx_out = s->adj_g[0], *gv_out = s->adj_g[1], *gx = s->adj_g[2];
+    float4 *gx_out = s->adj_g[0], *gv_out = s->adj_g[1];
     CK(cudaMemcpyAsync(gx_out, dL_dx_final, (size_t)N * 16, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(gv_out, 0, (size_t)N * 16, st));
     CK(cudaMemsetAsync(s->adj_acc, 0, 64, st));
-    const bool collide = s->prm.collision_type == 0;
-    const uint32_t gn = div_up(N, 128), ge = div_up(N, 256);
-    const DevParams P = make_dev_params(s);
-    const uint32_t* held = s->keys[fin];       // the tables hold the cells of the last frame run
     for (int ck = s->adj_nck - 1; ck >= 0; --ck) {
         const int f0 = ck * s->adj_every;
         const int nf = std::min(s->adj_every, s->adj_steps - f0);
-        if (ck + 1 < s->adj_nck || !s->adj_last_taped) {
-            // recompute the segment from its checkpoint, keeping the tape
+        const bool recompute = ck + 1 < s->adj_nck || !s->adj_last_taped;
+        if (recompute) {   // the segment's checkpoint into the state buffers
             CK(cudaMemcpyAsync(s->x[s->cur.x], s->adj_ck_x + (size_t)ck * N, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
             CK(cudaMemcpyAsync(s->v[s->cur.v], s->adj_ck_v + (size_t)ck * N, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
-            if (int rc = run_taped(s, st, nf)) return rc;
         }
-        held = s->adj_tape[nf - 1].keys;       // same contents as keys[fin] now
-        for (int t = nf - 1; t >= 0; --t) {
-            const Tape& T = s->adj_tape[t];
-            if (T.keys != held) { retable(s, st, held, T.keys, N); held = T.keys; }
-            // adj_update writes all of gp: each frame starts from the same pair of buffers
-            float4 *gp = s->adj_g[3], *gp2 = s->adj_g[4];
-            adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
-            for (int it = (int)I - 1; it >= 0; --it) {
-                const float4* p = T.p_it[it];
-                const float4* pa = T.p_it[0];
-                CK(cudaMemcpyAsync(gp2, gp, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
-                CK(cudaMemsetAsync(s->adj_glam, 0, (size_t)N * 4, st));
-                adj_delta_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.lam[it], gp, gx, gp2, s->adj_glam, s->cell_start,
-                                                     s->cell_end, s->adj_acc, collide);
-                adj_lambda_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.aux[it], s->adj_glam, gp2, s->cell_start, s->cell_end,
-                                                      s->adj_acc);
-                std::swap(gp, gp2);
-            }
-            adj_predict_kernel<<<ge, 256, 0, st>>>(P, T.perm, T.x_in, T.v_in, s->fext, gp, gx, gx_out, gv_out);
-            CK(cudaGetLastError());
-        }
-        // back to the tables the next recompute's predict expects: the cells of keys[fin]
-        retable(s, st, held, s->keys[fin], N);
-        held = s->keys[fin];
+        if (int rc = adj_segment(s, st, nf, recompute ? 1 : 2)) return rc;
     }
     // restore the state after the forward: tables, sorted keys, x, v, p, colours and ids
     retable(s, st, s->keys[fin], s->adj_fin_keys, N);
