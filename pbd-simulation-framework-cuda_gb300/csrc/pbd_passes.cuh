@@ -379,7 +379,7 @@ lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __re
 // A particle without a stored list is handed to lambda_coop_kernel (the deferral list holds
 // every particle, so the hand-off cannot fail).  Kept apart from lambda_kernel so that its
 // register budget is the list walk's alone.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)
 lambda_list_kernel(DevParams P, const float4* __restrict__ p, float* __restrict__ lambda, DeferList D,
                    float4* __restrict__ aux, NbList L, NbList F) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -538,7 +538,7 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const f
 
 // delta pass 0 of an iteration over the near lists its lambda pass recorded; particles
 // without one go to delta_coop_kernel.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)
 delta_list_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, float4* __restrict__ pout,
                   float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
                   const float* __restrict__ w, float4* __restrict__ delta, DeferList D, NbList L) {
@@ -654,7 +654,7 @@ omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict
 
 // omega over the full list (recording the near list when L.list); particles without one go to
 // omega_coop_kernel.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)
 omega_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ v, float4* __restrict__ omega,
                   DeferList D, NbList L, NbList F) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -786,7 +786,7 @@ vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
 
 // vorticity + viscosity over a stored list (the full list with vorticity, else the omega pass's
 // near list); particles without one go to vort_visc_coop_kernel.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)
 vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ vin,
                       float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
                       int do_vort, int do_visc, const float* __restrict__ w, DeferList D, NbList Lv) {
