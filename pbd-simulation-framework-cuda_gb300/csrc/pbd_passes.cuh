@@ -538,7 +538,7 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const f
 
 // delta pass 0 of an iteration over the near lists its lambda pass recorded; particles
 // without one go to delta_coop_kernel.
-__global__ void __launch_bounds__(256, 5)
+__global__ void __launch_bounds__(256)
 delta_list_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, float4* __restrict__ pout,
                   float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
                   const float* __restrict__ w, float4* __restrict__ delta, DeferList D, NbList L) {

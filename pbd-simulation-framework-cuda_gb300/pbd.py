@@ -9,7 +9,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libpbd.so")
+# PBD_LIBRARY selects another build of the library (same ABI), e.g. for A/B measurements
+LIB_PATH = os.environ.get("PBD_LIBRARY") or os.path.join(HERE, "libpbd.so")
 
 # status codes (include/pbd.h)
 OK, ERR_INVALID_ARG, ERR_CAPACITY, ERR_CUDA, ERR_CONFIG, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_ALLOC, ERR_RANGE = range(9)
