@@ -414,6 +414,9 @@ def run_ours(args):
         t_rank = float(t.item())
     value = n * args.steps * world / t_rank
 
+    # ---- density constraint after the timed frames (mean / max |rho_i / rho0 - 1|)
+    _, derr_mean, derr_max = sim.density_error(stream=sh)
+
     # ---- per-kernel device time over the same number of frames (direct launches)
     prof = sim.profile(args.steps, stream=sh)
     stream.synchronize()
@@ -507,6 +510,7 @@ def run_ours(args):
                           "achieved_gbs": algorithmic_bytes_per_particle_step() * value / world / 1e9,
                           "frac": algorithmic_bytes_per_particle_step() * value / world / 1e9 / peak},
         "kernel_ms_per_frame": {k: v[1] / args.steps for k, v in prof.items()},
+        "density_error": {"mean": derr_mean, "max": derr_max, "after_frames": args.warmup + args.steps},
         "batched": batched,
         "solids": solids,
         "adjoint": adjoint,

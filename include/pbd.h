@@ -246,6 +246,14 @@ int pbd_batch_launches_per_step(pbd_batch* batch, uint32_t* n);
 int pbd_batch_profile_frames(pbd_batch* batch, int nsteps, void* stream, pbd_kernel_stat* stats,
                              uint32_t max_stats, uint32_t* n_stats);
 
+/* The density constraint after the last frame (no counterpart in the reference, whose density
+ * lives inside computeLambda, Density.h:48-93): C_i = rho_i / rest_density - 1, rho_i the poly6
+ * sum over particle i's list of the last frame (no self term) at the current positions.  `err`
+ * (host, N floats, nullable) receives C_i in the current particle order; mean_abs and max_abs
+ * the mean and maximum of |C_i| (nullable).  Needs a frame since the last add/clear
+ * (PBD_ERR_INVALID_ARG otherwise); synchronises. */
+int pbd_density_error(pbd_sim* sim, float* err, double* mean_abs, double* max_abs, void* stream);
+
 /* ---- adjoint ------------------------------------------------------------------------ */
 /* No counterpart in the reference.  Gradients of a loss on the final positions of a rollout
  * with respect to the initial velocities and positions, the rest density and the relaxation

@@ -818,6 +818,61 @@ vort_visc_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* _
 }
 
 // ======================================================================================
+// Density constraint after a frame: C_i = rho_i / rho0 - 1 with rho_i the poly6 sum over the
+// frame's list (no self term, Density.h:67-84) at the current positions.
+// ======================================================================================
+struct DensityVisit {
+    struct Contrib { float a; uint32_t near; };
+    const DevParams& P;
+    float4 pi;
+    float A = 0.f;
+    __device__ DensityVisit(const DevParams& P_, float4 pi_) : P(P_), pi(pi_) {}
+    __device__ static Contrib zero() { return Contrib{0.f, 0u}; }
+    __device__ static bool effective(const Contrib& c) { return c.near != 0u; }
+    __device__ static Contrib shfl(const Contrib& c, int k) { return Contrib{shfl_f(c.a, k), shfl_u(c.near, k)}; }
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, bool) const {
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = rx * rx + ry * ry + rz * rz;
+        if (r2 >= P.cut2) return zero();
+        return Contrib{poly6(P, sqrtf(r2)), 1u};
+    }
+    __device__ __forceinline__ void add(const Contrib& c, bool) { if (c.near) A += c.a; }
+};
+
+// err[i] = C_i; acc[0] += |C_i| (double), acc[1] = max |C_i| (double bits, non-negative)
+__global__ void __launch_bounds__(128)
+density_error_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
+                     const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float* __restrict__ err,
+                     double* acc) {
+    __shared__ double ssum[4], smax[4];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    double a = 0.0;
+    if (i < P.N) {
+        const SceneCtx S = scene_ctx(P, i);
+        DensityVisit vis(P, p[i]);
+        bool deferred = false;
+        walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
+        const float c = vis.A / S.rho0 - 1.0f;
+        err[i] = c;
+        a = fabs((double)c);
+    }
+    double sm = a, mx = a;
+    for (int o = 16; o > 0; o >>= 1) {
+        sm += __shfl_down_sync(0xffffffffu, sm, o);
+        mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31u) == 0u) { ssum[threadIdx.x >> 5] = sm; smax[threadIdx.x >> 5] = mx; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0, m = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t += ssum[w]; m = fmax(m, smax[w]); }
+        atomicAdd(acc, t);
+        atomicMax(reinterpret_cast<unsigned long long*>(acc + 1), (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+// ======================================================================================
 // Debug: materialise the neighbour list (findContacts + findNeighbours, Collision.h:11-160)
 // ======================================================================================
 struct ListVisit {

@@ -96,6 +96,8 @@ struct pbd_sim {
     bool adj_last_taped = false;   // the tape holds the forward's last segment
     uint64_t gen = 0, adj_gen = 0; // bumped by every call that changes the state or parameters
     uint64_t pgen = 0;             // bumped by every call that changes the parameters, N or the block size
+    int anchor = -1;               // p buffer holding the last frame's anchors (-1: none since the state changed)
+    double* stats = nullptr;       // device accumulators of pbd_density_error
     struct AdjGraph { Cur start; int nf; int kind; Cur end; cudaGraphExec_t exec; };   // kind: see adj_segment
     std::vector<AdjGraph> adj_graphs;   // recorded segments of the adjoint
     uint64_t adj_graphs_pgen = ~0ull;
@@ -534,7 +536,7 @@ int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<Scene
     parts.push_back({(void**)&s->hist, (size_t)kMaxPasses * kRadix * 4});
     parts.push_back({(void**)&s->status, (size_t)kMaxPasses * s->max_tiles * kRadix * 4});
     parts.push_back({(void**)&s->tile_counter, kMaxPasses * 4}); parts.push_back({(void**)&s->err, 4});
-    parts.push_back({(void**)&s->table_n, 4});
+    parts.push_back({(void**)&s->table_n, 4}); parts.push_back({(void**)&s->stats, 64});
     s->defer_cap = capacity;   // every particle can be handed to the cooperative kernels
     parts.push_back({(void**)&s->defer_items, (size_t)s->defer_cap * 4});
     parts.push_back({(void**)&s->defer_count, 4}); parts.push_back({(void**)&s->defer_done, 4});
@@ -624,6 +626,7 @@ int pbd_capacity(const pbd_sim* s, uint32_t* c) {
 static int add_common(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4,
                       const float* inv_mass, cudaMemcpyKind kind, cudaStream_t st, bool sync) {
     ++s->gen;
+    s->anchor = -1;
     ++s->pgen;
     if (int rc = check_sim(s, "pbd_add_particles")) return rc;
     if (n == 0) return PBD_OK;
@@ -677,6 +680,7 @@ int pbd_add_particle(pbd_sim* s, const float pos[3], const float dir[3]) {
     clear_error();
     if (int rc = check_sim(s, "pbd_add_particle")) return rc;
     ++s->gen;
+    s->anchor = -1;
     ++s->pgen;
     if (s->batched) { set_error("a batch takes particles per scene: pbd_batch_add_particles"); return PBD_ERR_INVALID_ARG; }
     if (!pos || !dir) { set_error("pbd_add_particle: null"); return PBD_ERR_INVALID_ARG; }
@@ -693,6 +697,7 @@ int pbd_clear(pbd_sim* s) {
     clear_error();
     if (int rc = check_sim(s, "pbd_clear")) return rc;
     ++s->gen;
+    s->anchor = -1;
     ++s->pgen;
     s->N = 0;   // Communication.h:657-660
     std::fill(s->scene_count.begin(), s->scene_count.end(), 0u);
@@ -719,6 +724,7 @@ int pbd_step(pbd_sim* s, int nsteps, void* stream) {
             if (int rc = build_graphs(s)) return rc;
             g = 0;
         }
+        s->anchor = (s->cur.p + 1) % 3;   // this frame's anchor buffer (see enqueue_frame)
         CK(cudaGraphLaunch(s->exec[g], st));
         s->cur = s->exec_end[g];
     }
@@ -818,6 +824,7 @@ int pbd_debug_front(pbd_sim* s, void* stream) {
     if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
     if (int rc = settle_tables(s, st)) return rc;
     uint32_t nl = 0;
+    s->anchor = (s->cur.p + 1) % 3;
     cudaError_t e = enqueue_frame(s, st, s->cur, true, nl);
     if (e != cudaSuccess) return cuda_fail("pbd_debug_front", e);
     CK(cudaStreamSynchronize(st));
@@ -841,6 +848,7 @@ int pbd_profile_frames(pbd_sim* s, int nsteps, void* stream, pbd_kernel_stat* st
     prof.st = st;
     for (int k = 0; k < nsteps; ++k) {
         uint32_t nl = 0;
+        s->anchor = (s->cur.p + 1) % 3;
         cudaError_t e = enqueue_frame(s, st, s->cur, false, nl, &prof);
         if (e != cudaSuccess) return cuda_fail("pbd_profile_frames", e);
         s->table_hint = s->N;
@@ -863,6 +871,33 @@ int pbd_profile_frames(pbd_sim* s, int nsteps, void* stream, pbd_kernel_stat* st
         stats[k].total_ms += ms;
     }
     *n_stats = n;
+    return PBD_OK;
+}
+
+int pbd_density_error(pbd_sim* s, float* err, double* mean_abs, double* max_abs, void* stream) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_density_error")) return rc;
+    if (s->N == 0) {
+        if (mean_abs) *mean_abs = 0.0;
+        if (max_abs) *max_abs = 0.0;
+        return PBD_OK;
+    }
+    if (s->anchor < 0) { set_error("pbd_density_error: run a frame (pbd_step) after the last change of the state"); return PBD_ERR_INVALID_ARG; }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
+    const DevParams P = make_dev_params(s);
+    const uint32_t N = s->N;
+    CK(cudaMemsetAsync(s->stats, 0, 16, st));
+    density_error_kernel<<<div_up(N, 128), 128, 0, st>>>(P, s->p[s->cur.p], s->p[s->anchor], s->cell_start, s->cell_end,
+                                                          s->lambda, s->stats);
+    CK(cudaGetLastError());
+    double acc[2] = {0.0, 0.0};
+    CK(cudaMemcpyAsync(acc, s->stats, 16, cudaMemcpyDeviceToHost, st));
+    if (err) CK(cudaMemcpyAsync(err, s->lambda, (size_t)N * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (mean_abs) *mean_abs = acc[0] / (double)N;
+    if (max_abs) *max_abs = acc[1];
+    s->last_stream = st;
     return PBD_OK;
 }
 
@@ -914,6 +949,7 @@ int pbd_autotune(pbd_sim* s, const char* cache_path, void* stream, uint32_t* blo
     clear_error();
     if (int rc = check_sim(s, "pbd_autotune")) return rc;
     ++s->gen;
+    s->anchor = -1;
     ++s->pgen;
     if (s->N == 0) { set_error("pbd_autotune: no particles"); return PBD_ERR_INVALID_ARG; }
     const std::string sig = tune_signature(s);
@@ -1150,6 +1186,7 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
         }
     }
     s->adj_last_taped = true;
+    s->anchor = -1;            // the taped segment does not record which buffer held the anchors
     s->adj_gen = s->gen;
     const int fin = sort_passes(s) % 2;
     CK(cudaMemcpyAsync(s->adj_fin_x, s->x[s->cur.x], N * 16, cudaMemcpyDeviceToDevice, st));
@@ -1293,6 +1330,7 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
     CK(cudaMemcpyAsync(s->col[s->cur.x], s->adj_fin_col, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->ids[s->cur.x], s->adj_fin_ids, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
     s->adj_last_taped = s->adj_nck == 1;       // else the tape now holds the first segment
+    s->anchor = -1;
     double acc[2] = {0.0, 0.0};
     CK(cudaMemcpyAsync(acc, s->adj_acc, 16, cudaMemcpyDeviceToHost, st));
     if (dL_dv0) CK(cudaMemcpyAsync(dL_dv0, gv_out, (size_t)N * 16, cudaMemcpyDeviceToHost, st));

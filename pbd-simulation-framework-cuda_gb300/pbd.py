@@ -32,6 +32,7 @@ EXPORTED = [
     "pbd_autotune", "pbd_batch_create", "pbd_batch_destroy", "pbd_batch_add_particles", "pbd_batch_step",
     "pbd_batch_sync", "pbd_batch_num_particles", "pbd_batch_get_state", "pbd_batch_autotune",
     "pbd_batch_launches_per_step", "pbd_batch_profile_frames", "pbd_adjoint_forward", "pbd_adjoint_backward",
+    "pbd_density_error",
 ]
 
 
@@ -114,6 +115,7 @@ def lib():
             "pbd_batch_launches_per_step": [vp, u32p],
             "pbd_batch_profile_frames": [vp, i32, vp, C.POINTER(KernelStat), u32, u32p],
             "pbd_adjoint_forward": [vp, i32, i32, vp],
+            "pbd_density_error": [vp, fp, C.POINTER(C.c_double), C.POINTER(C.c_double), vp],
             "pbd_adjoint_backward": [vp, fp, fp, fp, C.POINTER(C.c_double), C.POINTER(C.c_double), vp],
         }
         for name, args in sig.items():
@@ -267,6 +269,13 @@ class Sim:
         v = C.c_uint32()
         check(self.L.pbd_launches_per_step(self.h, C.byref(v)))
         return v.value
+
+    def density_error(self, stream=0):
+        """(C_i per particle in the current order, mean |C|, max |C|) after the last frame"""
+        err = np.zeros(self.n, np.float32)
+        mean, mx = C.c_double(), C.c_double()
+        check(self.L.pbd_density_error(self.h, _fp(err), C.byref(mean), C.byref(mx), C.c_void_p(stream)))
+        return err, mean.value, mx.value
 
     def adjoint_forward(self, nsteps, ckpt_every, stream=0):
         check(self.L.pbd_adjoint_forward(self.h, nsteps, ckpt_every, C.c_void_p(stream)))
