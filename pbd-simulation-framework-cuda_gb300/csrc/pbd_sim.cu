@@ -799,6 +799,7 @@ int pbd_debug_neighbours(pbd_sim* s, uint32_t max_entries, uint32_t* list, uint3
     CK(cudaMalloc(&dl, lb));
     CK(cudaMalloc(&dc, n * 4));
     CK(cudaMalloc(&dk, n * 4));
+    CK(cudaMemsetAsync(dl, 0, lb, s->last_stream));   // slots past each count read back as 0
     const DevParams P = make_dev_params(s);
     const bool cols = (s->prm.flags & PBD_FLAG_COLORS) && (s->prm.active & PBD_ACTIVE_FIND_NEIGHBOURS);
     const uint32_t threads = walker ? (uint32_t)n * 32u : (uint32_t)n;
