@@ -93,6 +93,8 @@ typedef struct orc_sim {
     uint32_t *keys_in, *keys_out, *vals_in, *vals_out, *tmpk, *tmpv;
     uint32_t *cell_start, *cell_end;
     uint32_t *nbr, *nbr_count, *contact_count;
+    uint8_t* csolved;           /* collisionType 1: constraint solved in this stabilization pass (N x M) */
+    uint64_t* cbest;            /* collisionType 1: each particle's chosen constraint (priority << 32 | c) */
     /* derived parameters (kernel/Initialize.h:42-69) */
     real diameter, h_spiky, h_poly, q_scorr;
 } orc_sim;
@@ -201,7 +203,8 @@ void orc_destroy(orc_sim* s) {
     if (!s) return;
     void* bufs[] = {s->x, s->p, s->v, s->col, s->fext, s->delta, s->omega, s->xc, s->pc, s->vc, s->colc,
                     s->lambda, s->w, s->wc, s->ids, s->idsc, s->keys_in, s->keys_out, s->vals_in, s->vals_out,
-                    s->tmpk, s->tmpv, s->cell_start, s->cell_end, s->nbr, s->nbr_count, s->contact_count};
+                    s->tmpk, s->tmpv, s->cell_start, s->cell_end, s->nbr, s->nbr_count, s->contact_count,
+                    s->csolved, s->cbest};
     for (size_t k = 0; k < sizeof(bufs) / sizeof(bufs[0]); ++k) free(bufs[k]);
     free(s);
 }
@@ -533,6 +536,93 @@ static void solve_collisions(orc_sim* s) {
     }
 }
 
+/* ------------------------------------- Collision.h:288-436 (collisionType 1), batched ---
+ * The reference claims contacts with a __syncthreads inside divergent code and lets blocks race
+ * on the claims (undefined across blocks).  Restated deterministically as locally dominant
+ * matching: the constraints are the frame's list entries c = i * M + k (partner list[k];
+ * Fluid.cu:37-47 fills the same array).  In each of maxCollisionBatches batches, a constraint
+ * not yet solved in this stabilization pass competes when its particles overlap at the batch's
+ * start (diameter - |p_j - p_i| > 0, |p_j - p_i| > 1e-5, a movable particle); its priority is
+ * lowbias32(c + 1) (C. Wellons' published 32-bit integer mix) above c itself; every particle takes
+ * its highest-priority competing constraint, and a constraint both of whose particles took it is
+ * solved -- a batch is a matching, so its projections are independent.  Solving follows
+ * setupCollisionConstraintBatchesCheck: d = p2 - p1 (w = 0), half = (diameter - |d|) / 2,
+ * p1 and x1 move by -n half (1 - stiffness), p2 and x2 by +n half (1 - stiffness), and both p*
+ * are written back with w = 0.  Unified solids split the overlap by inverse mass (w1 / (w1 + w2);
+ * 1/2 with unit masses, the same bits as half). */
+static inline uint32_t lowbias32(uint32_t x) {
+    x ^= x >> 16; x *= 0x7feb352dU; x ^= x >> 15; x *= 0x846ca68bU; x ^= x >> 16;
+    return x;
+}
+
+static int contact_geometry(const orc_sim* s, uint32_t i, uint32_t j, r4* n, real* h1, real* h2) {
+    r4 p1 = s->p[i], p2 = s->p[j];
+    p1.w = 0; p2.w = 0;
+    const r4 dir = sub4(p2, p1);
+    const real len = len3(dir);
+    real s1 = (real)0.5, s2 = (real)0.5;
+    if (s->mass_used) {
+        const real w1 = s->w[i], w2 = s->w[j];
+        if (!(w1 + w2 > 0)) return 0;
+        s1 = w1 / (w1 + w2);
+        s2 = w2 / (w1 + w2);
+    }
+    const real overlap = s->diameter - len;
+    if (!(overlap * (real)0.5 > 0) || len <= (real)0.00001f) return 0;
+    *n = mk4(dir.x / len, dir.y / len, dir.z / len, dir.w / len);
+    *h1 = overlap * s1;
+    *h2 = overlap * s2;
+    return 1;
+}
+
+static int solve_collisions_batched(orc_sim* s) {
+    const uint32_t N = s->N, M = s->M;
+    const real one_m = (real)1 - (real)s->prm.stiffness;
+    if (!s->csolved) {
+        s->csolved = (uint8_t*)zalloc((size_t)s->cap * M);
+        s->cbest = (uint64_t*)zalloc((size_t)s->cap * sizeof(uint64_t));
+        if (!s->csolved || !s->cbest) return PBD_ERR_ALLOC;
+    }
+    memset(s->csolved, 0, (size_t)N * M);
+    uint64_t* best = s->cbest;
+    for (uint32_t b = 0; b < s->prm.max_collision_batches; ++b) {
+        memset(best, 0, (size_t)N * sizeof(uint64_t));
+        for (uint32_t i = 0; i < N; ++i) {
+            const uint32_t* list = s->nbr + (size_t)i * M;
+            for (uint32_t k = 0; k < s->nbr_count[i]; ++k) {
+                const uint32_t c = i * M + k;
+                if (s->csolved[c]) continue;
+                r4 n; real h1, h2;
+                const uint32_t j = list[k];
+                if (!contact_geometry(s, i, j, &n, &h1, &h2)) continue;
+                const uint64_t key = ((uint64_t)lowbias32(c + 1u) << 32) | c;   /* never 0: lowbias32 fixes only 0 */
+                if (key > best[i]) best[i] = key;
+                if (key > best[j]) best[j] = key;
+            }
+        }
+        for (uint32_t i = 0; i < N; ++i) {
+            const uint64_t key = best[i];
+            if (!key) continue;
+            const uint32_t c = (uint32_t)key;
+            if (c / M != i) continue;
+            const uint32_t j = s->nbr[c];
+            if (best[j] != key) continue;
+            s->csolved[c] = 1;
+            r4 n; real h1, h2;
+            if (!contact_geometry(s, i, j, &n, &h1, &h2)) continue;
+            const r4 a1 = mk4(-n.x * h1 * one_m, -n.y * h1 * one_m, -n.z * h1 * one_m, -n.w * h1 * one_m);
+            const r4 a2 = mk4(n.x * h2 * one_m, n.y * h2 * one_m, n.z * h2 * one_m, n.w * h2 * one_m);
+            r4 p1 = s->p[i], p2 = s->p[j];
+            p1.w = 0; p2.w = 0;
+            s->p[i] = add4(p1, a1);
+            s->p[j] = add4(p2, a2);
+            s->x[i] = add4(s->x[i], a1);
+            s->x[j] = add4(s->x[j], a2);
+        }
+    }
+    return PBD_OK;
+}
+
 /* ---------------------------------------------------------------- Update.h:11-32 ---- */
 static void update_positions(orc_sim* s) {
     const int N = (int)s->N;
@@ -618,7 +708,7 @@ static void compute_viscosity(orc_sim* s) {
 int orc_step_phase(orc_sim* s, int phase) {
     const pbd_params* P = &s->prm;
     if (s->N == 0) return PBD_OK;                         /* Fluid.cu:19 */
-    if (P->collision_type != 0) return PBD_ERR_UNSUPPORTED;
+    if (P->collision_type > 1) return PBD_ERR_UNSUPPORTED;
     if (P->active & PBD_ACTIVE_APPLY_FORCES) apply_forces(s);
     initialize_cell_ids(s);
     sort_ids(s);
@@ -631,7 +721,14 @@ int orc_step_phase(orc_sim* s, int phase) {
     for (uint32_t it = 0; it < P->solver_iterations; ++it) {
         if (P->active & PBD_ACTIVE_COMPUTE_LAMBDA) compute_lambda(s);
         if (P->active & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS) compute_delta_positions(s);
-        for (uint32_t k = 0; k < P->stabilization_iterations; ++k) solve_collisions(s);
+        for (uint32_t k = 0; k < P->stabilization_iterations; ++k) {
+            if (P->collision_type == 0) {
+                solve_collisions(s);
+            } else {
+                const int rc = solve_collisions_batched(s);
+                if (rc) return rc;
+            }
+        }
         if (P->active & PBD_ACTIVE_APPLY_DELTA_POSITIONS) apply_delta_positions(s);
     }
     if (P->active & PBD_ACTIVE_UPDATE_POSITIONS) update_positions(s);
