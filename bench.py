@@ -348,6 +348,31 @@ def run_adjoint(torch, pbd, scenes, stream, sh, frames=60, every=10, fd_check=Tr
     return out
 
 
+def run_contacts(torch, pbd, scenes, stream, sh, frames):
+    """The large-fluid workload with collisionType 1 (contact constraints in batches of disjoint
+    pairs, maxCollisionBatches 16): particle-steps/s."""
+    params, pos, vel, _ = build_workload(pbd, scenes, "fluid_1m")
+    params.collision_type = 1
+    params.max_collision_batches = 16
+    with pbd.Sim(params, len(pos)) as sim:
+        sim.add_particles(pos, vel)
+        sim.step(3, stream=sh)
+        stream.synchronize()
+        e0, e1 = _events(torch)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        sim.step(frames, stream=sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sim.sync()
+        ms = e0.elapsed_time(e1) / frames
+        prof = sim.profile(3, stream=sh)
+        sim.sync()
+    return {"workload": "fluid_1m, collisionType 1", "particles": len(pos), "frames": frames,
+            "max_collision_batches": 16, "ms_per_frame": ms, "particle_steps_per_s": len(pos) * 1e3 / ms,
+            "kernel_ms_per_frame": {k: v[1] / 3 for k, v in prof.items()}}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -489,6 +514,7 @@ def run_ours(args):
     batched = leg(run_batched, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 60)))
     solids = leg(run_solids, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 100)))
     adjoint = leg(run_adjoint, torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check)
+    contacts = leg(run_contacts, torch, pbd, scenes, stream, sh, frames=20)
 
     working_set = n * (16 * 3 + 16 * 3 + 4 + 16 + 16 * 2) + 2 * params.max_grid * 4
     line = {
@@ -514,6 +540,7 @@ def run_ours(args):
         "batched": batched,
         "solids": solids,
         "adjoint": adjoint,
+        "contacts": contacts,
     }
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)

@@ -1,0 +1,162 @@
+// pbd_contacts.cuh -- collisionType 1: contact constraints solved in batches of disjoint pairs
+// (kernel/Collision.h:288-436, Fluid.cu:37-38,65-72).
+//
+// The reference claims contacts with a __syncthreads inside divergent code and lets blocks race
+// on the claims, so its batches are undefined across blocks.  Here the batches are defined as
+// locally dominant matching:
+//  - the constraints are the frame's list entries c = i * M + k (partner = entry k of particle
+//    i's list; the reference fills the same array, findContacts + findNeighbours);
+//  - in each batch, a constraint not yet solved in this stabilization pass competes when its
+//    particles overlap at the batch's start (diameter - |p_j - p_i| > 0, |p_j - p_i| > 1e-5, a
+//    movable particle); its key is lowbias32(c + 1) (C. Wellons' published 32-bit integer mix)
+//    above c; every particle takes its highest competing key (atomicMax over both ends) and a
+//    constraint both of whose particles took it is solved -- a batch is a matching, so its
+//    projections touch disjoint particles and run in parallel (Gauss-Seidel across batches);
+//  - solving follows setupCollisionConstraintBatchesCheck (Collision.h:389-436): d = p2 - p1
+//    (w = 0), half = (diameter - |d|) / 2, p1 and x1 move by -n half (1 - stiffness), p2 and x2 by
+//    +n half (1 - stiffness), and both p* are written back with w = 0.  With unified solids the
+//    overlap is split by inverse mass (1/2 each for unit masses, the same bits as half).
+// The oracle (solve_collisions_batched) restates the same definition.
+#pragma once
+#include "pbd_passes.cuh"
+
+namespace pbd {
+
+struct ContactStore {
+    uint32_t* list;      // M x stride partner indices, slot-major
+    uint32_t* count;     // entries per particle
+    uint32_t* solved;    // ceil(M / 32) x stride words: bit k of particle i = constraint (i, k) solved
+    unsigned long long* best;   // each particle's chosen constraint key (0: none)
+    uint32_t stride;
+    uint32_t M;
+};
+
+__device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// The contact between particles i and j at the current positions: false when it does not act
+// (no overlap, coincident particles, or two immovable particles).
+__device__ __forceinline__ bool contact_geometry(const DevParams& P, const float4* __restrict__ p,
+                                                 const float* __restrict__ w, uint32_t i, uint32_t j,
+                                                 float4& n, float& h1, float& h2) {
+    const float4 p1 = p[i], p2 = p[j];
+    const float dx = p2.x - p1.x, dy = p2.y - p1.y, dz = p2.z - p1.z;
+    const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+    float s1 = 0.5f, s2 = 0.5f;
+    if (w) {
+        const float w1 = w[i], w2 = w[j];
+        if (!(w1 + w2 > 0.f)) return false;
+        s1 = w1 / (w1 + w2);
+        s2 = w2 / (w1 + w2);
+    }
+    const float overlap = P.d - len;
+    if (!(overlap * 0.5f > 0.f) || len <= 0.00001f) return false;
+    n = make_float4(dx / len, dy / len, dz / len, 0.f);
+    h1 = overlap * s1;
+    h2 = overlap * s2;
+    return true;
+}
+
+// Every entry of particle i's list, in list order, up to the cap M.
+struct ContactListVisit {
+    struct Contrib { uint32_t j; };
+    uint32_t* list;
+    uint32_t stride, i, n = 0;
+    __device__ ContactListVisit(uint32_t* l, uint32_t s, uint32_t i_) : list(l), stride(s), i(i_) {}
+    __device__ static Contrib zero() { return Contrib{0u}; }
+    __device__ static bool effective(const Contrib&) { return true; }
+    __device__ static Contrib shfl(const Contrib& c, int k) { return Contrib{shfl_u(c.j, k)}; }
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4&, bool) const { return Contrib{j}; }
+    __device__ __forceinline__ void add(const Contrib& c, bool) { list[(size_t)n * stride + i] = c.j; ++n; }
+};
+
+// After the re-order: each particle's constraint list (the walk stops at the cap M itself).
+__global__ void __launch_bounds__(256)
+contact_list_kernel(DevParams P, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
+                    const uint32_t* __restrict__ ce, ContactStore C) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    ContactListVisit vis(C.list, C.stride, i);
+    bool deferred = false;
+    walk_seq(P, scene_ctx(P, i), i, pa[i], pa, cs, ce, vis, false, &deferred);
+    C.count[i] = vis.n;
+}
+
+__device__ __forceinline__ bool contact_solved(const ContactStore& C, uint32_t i, uint32_t k) {
+    return (C.solved[(size_t)(k >> 5) * C.stride + i] >> (k & 31u)) & 1u;
+}
+
+// Each pending overlapping constraint offers its key to both of its particles.  Entries go in
+// batches of 4 (index loads, then position loads, in flight together); a cheap squared-distance
+// test (a superset of the overlap test, |r| < diameter) skips most entries before the exact one.
+__global__ void __launch_bounds__(256)
+contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, const float* __restrict__ w) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const uint32_t n = C.count[i];
+    const float4 pi = p[i];
+    const float reach2 = P.d * P.d * 1.0001f;
+    const uint32_t* __restrict__ e = C.list + i;
+    uint32_t word = 0;
+#pragma unroll 1
+    for (uint32_t k0 = 0; k0 < n; k0 += 4) {
+        if ((k0 & 31u) == 0u) word = C.solved[(size_t)(k0 >> 5) * C.stride + i];
+        uint32_t j[4];
+        float4 pj[4];
+#pragma unroll
+        for (uint32_t b = 0; b < 4; ++b) j[b] = (k0 + b < n) ? __ldg(e + (size_t)(k0 + b) * C.stride) : i;
+#pragma unroll
+        for (uint32_t b = 0; b < 4; ++b) pj[b] = __ldg(p + j[b]);
+#pragma unroll
+        for (uint32_t b = 0; b < 4; ++b) {
+            const uint32_t k = k0 + b;
+            if (k >= n || ((word >> (k & 31u)) & 1u)) continue;
+            const float dx = pj[b].x - pi.x, dy = pj[b].y - pi.y, dz = pj[b].z - pi.z;
+            if (!(dx * dx + dy * dy + dz * dz < reach2)) continue;
+            float4 nn;
+            float h1, h2;
+            if (!contact_geometry(P, p, w, i, j[b], nn, h1, h2)) continue;
+            const uint32_t c = i * C.M + k;
+            const unsigned long long key = ((unsigned long long)lowbias32(c + 1u) << 32) | c;
+            if (key > *((volatile unsigned long long*)(C.best + i))) atomicMax(C.best + i, key);
+            if (key > *((volatile unsigned long long*)(C.best + j[b]))) atomicMax(C.best + j[b], key);
+        }
+    }
+}
+
+// The constraint particle i took, if it is i's own and its partner took it too: solve it.
+__global__ void __launch_bounds__(256)
+contact_solve_kernel(DevParams P, ContactStore C, float4* __restrict__ p, float4* __restrict__ x,
+                     const float* __restrict__ w) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const unsigned long long key = C.best[i];
+    if (key == 0ull) return;
+    const uint32_t c = (uint32_t)key;
+    if (c / C.M != i) return;
+    const uint32_t k = c - i * C.M;
+    const uint32_t j = C.list[(size_t)k * C.stride + i];
+    if (C.best[j] != key) return;
+    C.solved[(size_t)(k >> 5) * C.stride + i] |= 1u << (k & 31u);   // only this thread writes i's words
+    float4 n;
+    float h1, h2;
+    if (!contact_geometry(P, p, w, i, j, n, h1, h2)) return;
+    const float om = P.one_minus_stiffness;
+    const float4 a1 = make_float4(-n.x * h1 * om, -n.y * h1 * om, -n.z * h1 * om, -n.w * h1 * om);
+    const float4 a2 = make_float4(n.x * h2 * om, n.y * h2 * om, n.z * h2 * om, n.w * h2 * om);
+    const float4 p1 = p[i], p2 = p[j];
+    p[i] = make_float4(p1.x + a1.x, p1.y + a1.y, p1.z + a1.z, 0.f + a1.w);
+    p[j] = make_float4(p2.x + a2.x, p2.y + a2.y, p2.z + a2.z, 0.f + a2.w);
+    const float4 x1 = x[i], x2 = x[j];
+    x[i] = make_float4(x1.x + a1.x, x1.y + a1.y, x1.z + a1.z, x1.w + a1.w);
+    x[j] = make_float4(x2.x + a2.x, x2.y + a2.y, x2.z + a2.z, x2.w + a2.w);
+}
+
+}  // namespace pbd

@@ -320,10 +320,12 @@ struct LambdaVisit {
         aux[N + i] = make_float4(Cz, Cw, 0.f, 0.f);
     }
     __device__ __forceinline__ float finish(float rho0) const {
-        const float a = A / rho0 - 1.0f;
-        const float b = B / rho0;
-        const float c = (Cx * Cx + Cy * Cy + Cz * Cz + Cw * Cw) / rho0;
-        return -a / (b + c + P.lambda_eps);
+        // correctly rounded: every kernel that finishes a lambda gets the same bits
+        const float a = __fsub_rn(__fdiv_rn(A, rho0), 1.0f);
+        const float b = __fdiv_rn(B, rho0);
+        const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(Cx, Cx), __fmul_rn(Cy, Cy)), __fadd_rn(__fmul_rn(Cz, Cz), __fmul_rn(Cw, Cw)));
+        const float c = __fdiv_rn(s2, rho0);
+        return __fdiv_rn(-a, __fadd_rn(__fadd_rn(b, c), P.lambda_eps));
     }
 };
 
@@ -495,7 +497,8 @@ __device__ __forceinline__ void delta_finish(const DevParams& P, float rho0, uin
     // a solid (inverse mass 0) takes no density correction
     float4 pn = vis.pacc, xn = vis.xacc;
     float4 dp = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (mode & kDoDelta) dp = make_float4(vis.ax / rho0, vis.ay / rho0, vis.az / rho0, vis.aw / rho0);
+    if (mode & kDoDelta)   // correctly rounded: the list and the walking kernels store the same bits
+        dp = make_float4(__fdiv_rn(vis.ax, rho0), __fdiv_rn(vis.ay, rho0), __fdiv_rn(vis.az, rho0), __fdiv_rn(vis.aw, rho0));
     else if (mode & kLoadDelta) dp = delta[i];
     if (mode & kStoreDelta) delta[i] = dp;
     if (mode & kDoApply) {

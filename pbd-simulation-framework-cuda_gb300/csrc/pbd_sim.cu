@@ -22,6 +22,7 @@
 #include "pbd_internal.h"
 #include "pbd_kernels.cuh"
 #include "pbd_adjoint.cuh"
+#include "pbd_contacts.cuh"
 
 namespace pbd {
 thread_local std::string g_last_error;
@@ -97,6 +98,10 @@ struct pbd_sim {
     uint64_t gen = 0, adj_gen = 0; // bumped by every call that changes the state or parameters
     uint64_t pgen = 0;             // bumped by every call that changes the parameters, N or the block size
     int anchor = -1;               // p buffer holding the last frame's anchors (-1: none since the state changed)
+    // collisionType 1 workspace (allocated when the parameters select it, never inside a frame)
+    void* ct_arena = nullptr;
+    size_t ct_bytes = 0;
+    ContactStore ct{};
     double* stats = nullptr;       // device accumulators of pbd_density_error
     struct AdjGraph { Cur start; int nf; int kind; Cur end; cudaGraphExec_t exec; };   // kind: see adj_segment
     std::vector<AdjGraph> adj_graphs;   // recorded segments of the adjoint
@@ -318,6 +323,13 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const bool do_delta = act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS, do_apply = act & PBD_ACTIVE_APPLY_DELTA_POSITIONS;
     const bool do_update = act & PBD_ACTIVE_UPDATE_POSITIONS;
     const bool collide = prm.collision_type == 0;
+    const bool batched_contacts = prm.collision_type == 1;
+    if (batched_contacts) {   // every list entry of the frame is a constraint (Fluid.cu:37-47)
+        PROF_BEGIN("contact_list");
+        contact_list_kernel<<<div_up(N, kThreadsParticle), kThreadsParticle, 0, st>>>(P, pa, s->cell_start, s->cell_end, s->ct);
+        PROF_END();
+        ++nl;
+    }
     bool last_was_delta = false;
     for (uint32_t it = 0; it < I; ++it) {
         if (tape && it < (uint32_t)kMaxTapeIters)
@@ -340,6 +352,55 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             PROF_END();
             nl += 2;
             last_was_delta = false;
+        }
+        if (batched_contacts) {
+            // collisionType 1 (Fluid.cu:55-77): delta positions, then S passes of contact
+            // batches on p* and x in place, then applyDeltaPositions (+ updatePositions)
+            const bool recorded = (act & PBD_ACTIVE_COMPUTE_LAMBDA) && (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS);
+            if (do_delta) {
+                const uint32_t mode = kDoDelta | kStoreDelta;
+                const bool by_list = recorded && use_lists;
+                PROF_BEGIN(by_list ? "delta_list" : "delta");
+                const int pout = next_p(cur.p);
+                if (by_list)
+                    delta_list_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                                         s->delta, D, L);
+                else
+                    delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                                    s->delta, s->cell_start, s->cell_end, D);
+                delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
+                                                               s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
+                PROF_END();
+                nl += 2;
+                cur.p = pout;
+            }
+            const ContactStore& C = s->ct;
+            const size_t words = (C.M + 31) / 32;
+            for (uint32_t k = 0; k < Sx; ++k) {
+                PROF_BEGIN("contact_batches");
+                cudaMemsetAsync(C.solved, 0, words * C.stride * 4, st);
+                for (uint32_t b = 0; b < prm.max_collision_batches; ++b) {
+                    cudaMemsetAsync(C.best, 0, (size_t)N * 8, st);
+                    contact_claim_kernel<<<div_up(N, kThreadsParticle), kThreadsParticle, 0, st>>>(P, C, s->p[cur.p], wf);
+                    contact_solve_kernel<<<div_up(N, kThreadsParticle), kThreadsParticle, 0, st>>>(P, C, s->p[cur.p], s->x[cur.x], wf);
+                    nl += 2;
+                }
+                PROF_END();
+            }
+            uint32_t mode = 0;
+            if (do_apply) mode |= kLoadDelta | kDoApply;
+            if (it + 1 == I && do_update && mode) mode |= kDoUpdate;
+            if (mode) {
+                PROF_BEGIN("apply");
+                const int pout = next_p(cur.p);
+                delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                                s->delta, s->cell_start, s->cell_end, D);
+                PROF_END();
+                ++nl;
+                cur.p = pout;
+                last_was_delta = (mode & kDoUpdate) != 0;
+            }
+            continue;
         }
         // passes of this iteration: pass 0 carries computeDeltaPositions and the first
         // solveCollisions; pass k carries solveCollisions k; applyDeltaPositions rides on the
@@ -496,13 +557,44 @@ uint32_t pbd_abi_version(void) { return PBD_ABI_VERSION; }
 }  // extern "C"
 
 namespace {
+// collisionType 1 keeps every list entry of the frame (up to M per particle) as a constraint:
+// allocate that workspace when the parameters select it (at pbd_create / pbd_set_params).
+int ensure_contacts(pbd_sim* s) {
+    if (s->prm.collision_type != 1) return PBD_OK;
+    const size_t C = s->cap, M = std::max(1u, s->prm.max_neighbours_per_particle), W = (M + 31) / 32;
+    if (C * M >= (size_t(1) << 32)) {   // constraint indices are 32-bit
+        set_error("collisionType 1: capacity x maxNeighboursPerParticle must stay below 2^32");
+        return PBD_ERR_UNSUPPORTED;
+    }
+    const size_t need = ((C * M * 4 + 255) & ~size_t(255)) + ((C * 4 + 255) & ~size_t(255)) +
+                        ((C * W * 4 + 255) & ~size_t(255)) + C * 8 + 256;
+    if (s->ct_arena && s->ct_bytes >= need && s->ct.M == M) return PBD_OK;
+    if (s->ct_arena) {
+        cudaDeviceSynchronize();
+        cudaFree(s->ct_arena);
+        s->ct_arena = nullptr;
+        s->ct_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&s->ct_arena, need);
+    if (e != cudaSuccess) { set_error(std::string("collisionType 1 workspace: ") + cudaGetErrorString(e)); return PBD_ERR_ALLOC; }
+    s->ct_bytes = need;
+    char* c = static_cast<char*>(s->ct_arena);
+    auto take = [&](size_t b) { char* r = c; c += (b + 255) & ~size_t(255); return r; };
+    s->ct.list = (uint32_t*)take(C * M * 4);
+    s->ct.count = (uint32_t*)take(C * 4);
+    s->ct.solved = (uint32_t*)take(C * W * 4);
+    s->ct.best = (unsigned long long*)take(C * 8);
+    s->ct.stride = (uint32_t)C;
+    s->ct.M = (uint32_t)M;
+    return PBD_OK;
+}
+
 // Allocate a simulation: one arena for every buffer.  `scenes` is non-null for the batched form.
 int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<SceneParams>* scenes,
                const std::vector<uint32_t>* caps, pbd_sim** out) {
     *out = nullptr;
     int rc = pbd_validate_params(prm);
     if (rc) return rc;
-    if (prm->collision_type != 0) { set_error("collisionType 1 (batched contact claims) is not implemented"); return PBD_ERR_UNSUPPORTED; }
     if (capacity == 0 || capacity > (1u << 30) - 1u) { set_error("capacity must be in [1, 2^30)"); return PBD_ERR_INVALID_ARG; }
     pbd_sim* s = new (std::nothrow) pbd_sim();
     if (!s) { set_error("host allocation"); return PBD_ERR_ALLOC; }
@@ -564,6 +656,7 @@ int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<Scene
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) { cudaFree(s->arena); delete s; return cuda_fail("pbd_create init", e); }
+    if (int rc2 = ensure_contacts(s)) { cudaFree(s->arena); delete s; return rc2; }
     *out = s;
     return PBD_OK;
 }
@@ -584,6 +677,7 @@ int pbd_destroy(pbd_sim* s) {
     destroy_graphs(s);
     for (auto& g : s->adj_graphs) cudaGraphExecDestroy(g.exec);
     if (s->adj_arena) cudaFree(s->adj_arena);
+    if (s->ct_arena) cudaFree(s->ct_arena);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     cudaError_t e = cudaFree(s->arena);
     delete s;
@@ -598,9 +692,10 @@ int pbd_set_params(pbd_sim* s, const pbd_params* prm) {
     ++s->pgen;
     if (!prm) { set_error("pbd_set_params: null"); return PBD_ERR_INVALID_ARG; }
     if (int rc = pbd_validate_params(prm)) return rc;
-    if (prm->collision_type != 0) { set_error("collisionType 1 (batched contact claims) is not implemented"); return PBD_ERR_UNSUPPORTED; }
     if (prm->max_grid != s->prm.max_grid) { set_error("max_grid is fixed at pbd_create"); return PBD_ERR_UNSUPPORTED; }
+    const pbd_params old = s->prm;
     s->prm = *prm;
+    if (int rc = ensure_contacts(s)) { s->prm = old; return rc; }
     s->dirty = true;
     return PBD_OK;
 }
@@ -1109,6 +1204,7 @@ static int adjoint_supported(const pbd_sim* s) {
     if (p.stabilization_iterations != 1 || p.solver_iterations == 0 || p.solver_iterations > (uint32_t)kMaxTapeIters) { set_error("adjoint: stabilizationIterations must be 1 and solverIterations 1..16"); return PBD_ERR_UNSUPPORTED; }
     if (p.enclosure_position_damping != 0.0f) { set_error("adjoint: enclosurePositionDamping must be 0"); return PBD_ERR_UNSUPPORTED; }
     if (s->mass_used || s->batched) { set_error("adjoint: solids and batches have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
+    if (p.collision_type != 0) { set_error("adjoint: collisionType 1 has no reverse pass"); return PBD_ERR_UNSUPPORTED; }
     return PBD_OK;
 }
 

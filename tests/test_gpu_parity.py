@@ -212,11 +212,13 @@ def test_add_clear_and_capacity(need_gpu, pbd, scenes, oracle_mod):
     assert maxdiff(g["x"][:, :3], o["x"][:, :3]) < TOL_X1
 
 
-def test_collision_type_1_is_reported(need_gpu, pbd, scenes):
+def test_collision_type_1_rejects_oversized_constraint_indices(need_gpu, pbd, scenes):
+    """collisionType 1 numbers its constraints i * M + k in 32 bits"""
     params, pos, vel = workload(pbd, scenes)
     params.collision_type = 1
+    params.max_neighbours_per_particle = 512
     with pytest.raises(pbd.PBDError) as e:
-        pbd.Sim(params, 16)
+        pbd.Sim(params, (1 << 23) + 1)
     assert e.value.code == pbd.ERR_UNSUPPORTED
 
 
