@@ -373,6 +373,28 @@ def run_contacts(torch, pbd, scenes, stream, sh, frames):
             "kernel_ms_per_frame": {k: v[1] / 3 for k, v in prof.items()}}
 
 
+def run_render(torch, pbd, sim, stream, sh, reps=10):
+    """Headless sprites of the simulation's current state at 1920 x 1080 (device time per image,
+    no copies to the host; plus one call that also copies RGBA and depth back)."""
+    cam = pbd.camera(eye=(230.0, 150.0, 250.0), center=(64.0, 30.0, 64.0), width=1920, height=1080)
+    L = pbd.lib()
+    sim.render(cam, stream=sh)                     # workspace + warm-up
+    e0, e1 = _events(torch)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        pbd.check(L.pbd_render_sprites(sim.h, pbd.C.byref(cam), None, None, pbd.C.c_void_p(sh)))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    t0 = time.perf_counter()
+    rgba, depth = sim.render(cam, stream=sh)
+    ms_host = (time.perf_counter() - t0) * 1e3
+    return {"width": 1920, "height": 1080, "particles": sim.n, "ms_per_image": ms,
+            "sprites_per_s": sim.n * 1e3 / ms, "ms_with_host_copies": ms_host,
+            "covered_pixel_fraction": float((depth < 1.0).mean())}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -441,6 +463,12 @@ def run_ours(args):
 
     # ---- density constraint after the timed frames (mean / max |rho_i / rho0 - 1|)
     _, derr_mean, derr_max = sim.density_error(stream=sh)
+
+    # ---- headless sprites of this state
+    try:
+        render = run_render(torch, pbd, sim, stream, sh)
+    except Exception as e:  # noqa: BLE001
+        render = {"error": f"{type(e).__name__}: {e}"}
 
     # ---- per-kernel device time over the same number of frames (direct launches)
     prof = sim.profile(args.steps, stream=sh)
@@ -541,6 +569,7 @@ def run_ours(args):
         "solids": solids,
         "adjoint": adjoint,
         "contacts": contacts,
+        "render": render,
     }
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)

@@ -254,6 +254,35 @@ int pbd_batch_profile_frames(pbd_batch* batch, int nsteps, void* stream, pbd_ker
  * (PBD_ERR_INVALID_ARG otherwise); synchronises. */
 int pbd_density_error(pbd_sim* sim, float* err, double* mean_abs, double* max_abs, void* stream);
 
+/* ---- headless particle sprites -------------------------------------------------------- */
+/* The reference draws each particle as a shaded sphere sprite through OpenGL
+ * (src/app/rendering/shader/particles/particleSpriteGeom.{vert,geom,frag}, Particles.cc:234-284).
+ * This renders the same sprites without a graphics API, into an image:
+ *  - colour per particle: mix((0.95, 0.97, 0.97), (0, 0, 1), colour.x^(1/6)) (.vert);
+ *  - a quad of half-size sphere_radius around view * position, facing the camera (.geom);
+ *  - per pixel inside the unit disc of the quad: normal (u, v, sqrt(1 - u^2 - v^2)) rotated back
+ *    by the inverse of the view's rotation, Phong shading 0.3 ambient + 0.7 diffuse + 0.2 specular
+ *    (exponent 10) with L = normalize(light_position - position), V = normalize(-view_direction),
+ *    and the depth of the sphere surface 0.5 (z / w) + 0.5 (.frag); nearest fragment wins.
+ * A pixel is covered when its centre lies in the quad's window rectangle [x0, x1) x [y0, y1);
+ * colours are rounded to 8 bits.  Rows are returned top-down (row 0 = the window's top).
+ * The matrices are column-major as glm and glUniformMatrix4fv(..., GL_FALSE, ...) use them; the
+ * view's upper 3x3 must be a rotation (glm::lookAt).  The particle colours are the simulation's
+ * colour array (PBD_FLAG_COLORS: neighbour count / maxNeighboursPerParticle). */
+typedef struct pbd_camera {
+    float view[16];            /* glm::lookAt (GLFW_Controls.cc:244) */
+    float projection[16];      /* glm::perspective (GLFW_Controls.cc:69) */
+    float view_direction[3];   /* world space (GL_Renderable.cc:34) */
+    float light_position[3];   /* (0, 0, 10) in particleSpriteGeom.geom */
+    float sphere_radius;       /* 0.5 in particleSpriteGeom.geom/.frag */
+    uint32_t width, height;    /* pixels */
+    float clear_rgba[4];       /* (0, 0, 0, 1) in GLFW_Window.cc:96 */
+} pbd_camera;
+/* rgba: width*height*4 bytes, depth: width*height floats (1 where no sprite); host pointers,
+ * either may be NULL.  Allocates its image workspace on first use or when the size grows;
+ * synchronises. */
+int pbd_render_sprites(pbd_sim* sim, const pbd_camera* camera, uint8_t* rgba, float* depth, void* stream);
+
 /* ---- adjoint ------------------------------------------------------------------------ */
 /* No counterpart in the reference.  Gradients of a loss on the final positions of a rollout
  * with respect to the initial velocities and positions, the rest density and the relaxation

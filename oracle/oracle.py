@@ -44,6 +44,7 @@ def _lib(precision):
         lib.orc_set_threads.argtypes = [i32]
         lib.orc_max_threads.restype = i32
         lib.orc_real_size.restype = i32
+        lib.orc_render_sprites.argtypes = [f32p, f32p, u32, vp, C.POINTER(C.c_uint8), f32p]
         _LIBS[precision] = lib
     return _LIBS[precision]
 
@@ -156,6 +157,17 @@ def expand_bits(v):
 
 def morton(x, y, z):
     return _lib("f32").orc_morton_f32(x, y, z)
+
+
+def render_sprites(pos4, col4, cam):
+    """The sprite renderer's CPU restatement: (rgba (H, W, 4) uint8 rows top-down, depth (H, W))."""
+    pos4 = np.ascontiguousarray(pos4, dtype=np.float32)
+    col4 = None if col4 is None else np.ascontiguousarray(col4, dtype=np.float32)
+    rgba = np.zeros((cam.height, cam.width, 4), np.uint8)
+    depth = np.zeros((cam.height, cam.width), np.float32)
+    _lib("f32").orc_render_sprites(_ptr(pos4, C.c_float), _ptr(col4, C.c_float), len(pos4), C.byref(cam),
+                                   rgba.ctypes.data_as(C.POINTER(C.c_uint8)), _ptr(depth, C.c_float))
+    return rgba, depth
 
 
 def set_threads(n, precision="f32"):

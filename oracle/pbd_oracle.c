@@ -801,3 +801,122 @@ void orc_density_error(orc_sim* s, double* out) {
 }
 
 int orc_real_size(void) { return (int)sizeof(real); }
+
+/* ---------------------------------- particle sprites (particleSpriteGeom.vert/.geom/.frag) ---
+ * Float arithmetic with every operation correctly rounded and in a fixed order (this file is
+ * built with -ffp-contract=off), so the CUDA renderer, written with the same operations in the
+ * same order, gives the same bits.  pow(x, 1/6) is a 32-step bisection on [0, 1] and pow(s, 10)
+ * repeated squaring -- the renderer's own definitions, not GLSL's pow. */
+static float spr_root6(float x) {
+    if (!(x > 0.0f)) return 0.0f;
+    if (x >= 1.0f) return 1.0f;
+    float lo = 0.0f, hi = 1.0f;
+    for (int k = 0; k < 32; ++k) {
+        const float m = (lo + hi) * 0.5f;
+        const float m2 = m * m;
+        const float m6 = (m2 * m2) * m2;
+        if (m6 < x) lo = m; else hi = m;
+    }
+    return lo;
+}
+
+/* column-major 4x4 times (x, y, z, w): ((m0 x + m4 y) + m8 z) + m12 w per row */
+static void spr_mat4(const float* m, float x, float y, float z, float w, float* o) {
+    for (int r = 0; r < 4; ++r) o[r] = ((m[r] * x + m[4 + r] * y) + m[8 + r] * z) + m[12 + r] * w;
+}
+
+static void spr_normalize3(float* v) {
+    const float l = sqrtf((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+    v[0] = v[0] / l; v[1] = v[1] / l; v[2] = v[2] / l;
+}
+
+static uint32_t spr_unorm8(float c) {
+    c = c < 0.0f ? 0.0f : (c > 1.0f ? 1.0f : c);
+    return (uint32_t)floorf(c * 255.0f + 0.5f);
+}
+
+void orc_render_sprites(const float* pos4, const float* col4, uint32_t n, const pbd_camera* cam, uint8_t* rgba,
+                        float* depth) {
+    const uint32_t W = cam->width, H = cam->height;
+    uint64_t* key = (uint64_t*)malloc((size_t)W * H * sizeof(uint64_t));
+    if (!key) return;
+    uint32_t clear = spr_unorm8(cam->clear_rgba[0]) | (spr_unorm8(cam->clear_rgba[1]) << 8) |
+                     (spr_unorm8(cam->clear_rgba[2]) << 16) | (spr_unorm8(cam->clear_rgba[3]) << 24);
+    float one = 1.0f;
+    uint32_t one_bits;
+    memcpy(&one_bits, &one, 4);
+    for (size_t q = 0; q < (size_t)W * H; ++q) key[q] = ((uint64_t)one_bits << 32) | clear;
+    const float* V = cam->view;
+    const float r = cam->sphere_radius;
+    float vd[3] = {-cam->view_direction[0], -cam->view_direction[1], -cam->view_direction[2]};
+    spr_normalize3(vd);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float px = pos4[4 * i], py = pos4[4 * i + 1], pz = pos4[4 * i + 2];
+        const float t = spr_root6(col4 ? col4[4 * i] : 0.0f);
+        const float c[3] = {0.95f * (1.0f - t) + 0.0f * t, 0.97f * (1.0f - t) + 0.0f * t, 0.97f * (1.0f - t) + 1.0f * t};
+        float L[3] = {cam->light_position[0] - px, cam->light_position[1] - py, cam->light_position[2] - pz};
+        spr_normalize3(L);
+        float vp[4];
+        spr_mat4(V, px, py, pz, 1.0f, vp);
+        float lo[4], hi[4];
+        spr_mat4(cam->projection, vp[0] - r, vp[1] - r, vp[2], vp[3], lo);
+        spr_mat4(cam->projection, vp[0] + r, vp[1] + r, vp[2], vp[3], hi);
+        if (!(lo[3] > 0.0f)) continue;                              /* behind the eye */
+        const float zn = lo[2] / lo[3];
+        if (zn < -1.0f || zn > 1.0f) continue;                     /* outside the near / far planes */
+        const float x0 = (lo[0] / lo[3] * 0.5f + 0.5f) * (float)W, y0 = (lo[1] / lo[3] * 0.5f + 0.5f) * (float)H;
+        const float x1 = (hi[0] / hi[3] * 0.5f + 0.5f) * (float)W, y1 = (hi[1] / hi[3] * 0.5f + 0.5f) * (float)H;
+        if (!(x1 > x0) || !(y1 > y0)) continue;
+        long ix0 = (long)ceilf(x0 - 0.5f), ix1 = (long)ceilf(x1 - 0.5f);
+        long iy0 = (long)ceilf(y0 - 0.5f), iy1 = (long)ceilf(y1 - 0.5f);
+        if (ix0 < 0) ix0 = 0;
+        if (iy0 < 0) iy0 = 0;
+        if (ix1 > (long)W) ix1 = (long)W;
+        if (iy1 > (long)H) iy1 = (long)H;
+        const float sx = 2.0f / (x1 - x0), sy = 2.0f / (y1 - y0);
+        for (long iy = iy0; iy < iy1; ++iy) {
+            const float v = ((float)iy + 0.5f - y0) * sy - 1.0f;
+            for (long ix = ix0; ix < ix1; ++ix) {
+                const float u = ((float)ix + 0.5f - x0) * sx - 1.0f;
+                const float mag = u * u + v * v;
+                if (mag > 1.0f) continue;
+                const float nz = sqrtf(1.0f - mag);
+                /* inverse of the view rotation = its transpose: N_world[k] = sum_r V[4k + r] N[r] */
+                float N[3];
+                for (int k = 0; k < 3; ++k) N[k] = (V[4 * k] * u + V[4 * k + 1] * v) + V[4 * k + 2] * nz;
+                spr_normalize3(N);
+                const float ln = (L[0] * N[0] + L[1] * N[1]) + L[2] * N[2];
+                float R[3];
+                for (int k = 0; k < 3; ++k) R[k] = -L[k] + (2.0f * ln) * N[k];
+                float rv = (R[0] * vd[0] + R[1] * vd[1]) + R[2] * vd[2];
+                rv = rv < 0.0f ? 0.0f : (rv > 1.0f ? 1.0f : rv);
+                const float s2 = rv * rv, s4 = s2 * s2, s8 = s4 * s4, s10 = s8 * s2;
+                const float diff = ln > 0.0f ? ln : 0.0f;
+                uint32_t col = 0;
+                for (int k = 0; k < 3; ++k) {
+                    const float f = (0.3f * c[k] + (0.7f * diff) * c[k]) + (0.2f * s10) * 1.0f;
+                    col |= spr_unorm8(f) << (8 * k);
+                }
+                col |= 255u << 24;
+                float dp[4];
+                spr_mat4(cam->projection, vp[0], vp[1], vp[2] + r * nz, vp[3], dp);
+                float dz = 0.5f * (dp[2] / dp[3]) + 0.5f;
+                if (dz < 0.0f) dz = 0.0f;
+                if (!(dz < 1.0f)) continue;                        /* GL_LESS against the cleared 1 */
+                uint32_t db;
+                memcpy(&db, &dz, 4);
+                const uint64_t k64 = ((uint64_t)db << 32) | col;
+                const size_t q = (size_t)iy * W + (size_t)ix;
+                if (k64 < key[q]) key[q] = k64;
+            }
+        }
+    }
+    for (uint32_t y = 0; y < H; ++y)
+        for (uint32_t x = 0; x < W; ++x) {
+            const uint64_t k64 = key[(size_t)y * W + x];
+            const size_t o = (size_t)(H - 1 - y) * W + x;             /* rows top-down */
+            if (rgba) { const uint32_t c = (uint32_t)k64; memcpy(rgba + 4 * o, &c, 4); }
+            if (depth) { const uint32_t db = (uint32_t)(k64 >> 32); memcpy(depth + o, &db, 4); }
+        }
+    free(key);
+}

@@ -23,6 +23,7 @@
 #include "pbd_kernels.cuh"
 #include "pbd_adjoint.cuh"
 #include "pbd_contacts.cuh"
+#include "pbd_sprites.cuh"
 
 namespace pbd {
 thread_local std::string g_last_error;
@@ -102,6 +103,9 @@ struct pbd_sim {
     void* ct_arena = nullptr;
     size_t ct_bytes = 0;
     ContactStore ct{};
+    // sprite image workspace (allocated by pbd_render_sprites on first use or growth)
+    void* img_arena = nullptr;
+    size_t img_bytes = 0;
     double* stats = nullptr;       // device accumulators of pbd_density_error
     struct AdjGraph { Cur start; int nf; int kind; Cur end; cudaGraphExec_t exec; };   // kind: see adj_segment
     std::vector<AdjGraph> adj_graphs;   // recorded segments of the adjoint
@@ -678,6 +682,7 @@ int pbd_destroy(pbd_sim* s) {
     for (auto& g : s->adj_graphs) cudaGraphExecDestroy(g.exec);
     if (s->adj_arena) cudaFree(s->adj_arena);
     if (s->ct_arena) cudaFree(s->ct_arena);
+    if (s->img_arena) cudaFree(s->img_arena);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     cudaError_t e = cudaFree(s->arena);
     delete s;
@@ -993,6 +998,48 @@ int pbd_density_error(pbd_sim* s, float* err, double* mean_abs, double* max_abs,
     CK(cudaStreamSynchronize(st));
     if (mean_abs) *mean_abs = acc[0] / (double)N;
     if (max_abs) *max_abs = acc[1];
+    s->last_stream = st;
+    return PBD_OK;
+}
+
+int pbd_render_sprites(pbd_sim* s, const pbd_camera* cam, uint8_t* rgba, float* depth, void* stream) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_render_sprites")) return rc;
+    if (!cam || cam->width == 0 || cam->height == 0 || (size_t)cam->width * cam->height > (size_t(1) << 28)) {
+        set_error("pbd_render_sprites: camera size must be in [1, 2^28] pixels");
+        return PBD_ERR_INVALID_ARG;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
+    const size_t npx = (size_t)cam->width * cam->height;
+    const size_t need = npx * 8 + ((npx * 4 + 255) & ~size_t(255)) * 2 + 256;
+    if (need > s->img_bytes) {
+        CK(cudaStreamSynchronize(st));
+        if (s->img_arena) cudaFree(s->img_arena);
+        s->img_arena = nullptr;
+        cudaError_t e = cudaMalloc(&s->img_arena, need);
+        if (e != cudaSuccess) { s->img_bytes = 0; set_error(std::string("sprite image: ") + cudaGetErrorString(e)); return PBD_ERR_ALLOC; }
+        s->img_bytes = need;
+    }
+    unsigned long long* key = static_cast<unsigned long long*>(s->img_arena);
+    uint32_t* d_rgba = reinterpret_cast<uint32_t*>(static_cast<char*>(s->img_arena) + npx * 8);
+    float* d_depth = reinterpret_cast<float*>(reinterpret_cast<char*>(d_rgba) + ((npx * 4 + 255) & ~size_t(255)));
+    SpriteCam c{};
+    std::memcpy(c.V, cam->view, sizeof(c.V));
+    std::memcpy(c.Pm, cam->projection, sizeof(c.Pm));
+    for (int k = 0; k < 3; ++k) { c.vd[k] = -cam->view_direction[k]; c.light[k] = cam->light_position[k]; }
+    c.r = cam->sphere_radius;
+    c.W = cam->width;
+    c.H = cam->height;
+    const uint32_t gs = std::max(1u, std::min((uint32_t)div_up(npx, 256), (uint32_t)s->num_sms * 16u));
+    sprite_clear_kernel<<<gs, 256, 0, st>>>(key, npx, make_float4(cam->clear_rgba[0], cam->clear_rgba[1],
+                                                                    cam->clear_rgba[2], cam->clear_rgba[3]));
+    if (s->N) sprite_splat_kernel<<<div_up(s->N, 256), 256, 0, st>>>(c, s->x[s->cur.x], s->col[s->cur.x], s->N, key);
+    sprite_resolve_kernel<<<(uint32_t)div_up(npx, 256), 256, 0, st>>>(key, cam->width, cam->height, d_rgba, d_depth);
+    CK(cudaGetLastError());
+    if (rgba) CK(cudaMemcpyAsync(rgba, d_rgba, npx * 4, cudaMemcpyDeviceToHost, st));
+    if (depth) CK(cudaMemcpyAsync(depth, d_depth, npx * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     s->last_stream = st;
     return PBD_OK;
 }

@@ -31,7 +31,7 @@ EXPORTED = [
     "pbd_launches_per_step", "pbd_profile_frames", "pbd_sort_keys_noalloc", "pbd_last_error", "pbd_abi_version",
     "pbd_autotune", "pbd_batch_create", "pbd_batch_destroy", "pbd_batch_add_particles", "pbd_batch_step",
     "pbd_batch_sync", "pbd_batch_num_particles", "pbd_batch_get_state", "pbd_batch_autotune",
-    "pbd_batch_launches_per_step", "pbd_batch_profile_frames", "pbd_adjoint_forward", "pbd_adjoint_backward",
+    "pbd_batch_launches_per_step", "pbd_batch_profile_frames", "pbd_adjoint_forward", "pbd_adjoint_backward", "pbd_render_sprites",
     "pbd_density_error",
 ]
 
@@ -72,6 +72,54 @@ class SceneDesc(C.Structure):
 
 class KernelStat(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint32), ("total_ms", C.c_float)]
+
+
+class Camera(C.Structure):
+    """pbd_camera (include/pbd.h): column-major view and projection as glm builds them."""
+    _fields_ = [("view", C.c_float * 16), ("projection", C.c_float * 16), ("view_direction", C.c_float * 3),
+                ("light_position", C.c_float * 3), ("sphere_radius", C.c_float), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("clear_rgba", C.c_float * 4)]
+
+
+def look_at(eye, center, up):
+    """glm::lookAt (right-handed): column-major 4x4 as a (16,) float32 array, and the view direction"""
+    eye, center, up = (np.asarray(a, np.float64) for a in (eye, center, up))
+    f = center - eye
+    f /= np.linalg.norm(f)
+    s_ = np.cross(f, up)
+    s_ /= np.linalg.norm(s_)
+    u = np.cross(s_, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = s_, u, -f          # rows of the rotation
+    m[0, 3], m[1, 3], m[2, 3] = -s_ @ eye, -u @ eye, f @ eye
+    return m.T.astype(np.float32).ravel(), f.astype(np.float32)
+
+
+def perspective(fovy, aspect, near, far):
+    """glm::perspective (radians, right-handed, depth -1..1): column-major (16,) float32"""
+    t = np.tan(fovy / 2.0)
+    m = np.zeros((4, 4))
+    m[0, 0] = 1.0 / (aspect * t)
+    m[1, 1] = 1.0 / t
+    m[2, 2] = -(far + near) / (far - near)
+    m[3, 2] = -1.0
+    m[2, 3] = -(2.0 * far * near) / (far - near)
+    return m.T.astype(np.float32).ravel()
+
+
+def camera(eye, center, width, height, fovy=np.pi / 4, near=0.1, far=1000.0, up=(0.0, 1.0, 0.0),
+           light=(0.0, 0.0, 10.0), radius=0.5, clear=(0.0, 0.0, 0.0, 1.0)):
+    """A pbd_camera looking from `eye` at `center` (the reference's defaults for the rest)."""
+    c = Camera()
+    v, f = look_at(eye, center, up)
+    c.view[:] = v.tolist()
+    c.projection[:] = perspective(fovy, width / height, near, far).tolist()
+    c.view_direction[:] = f.tolist()
+    c.light_position[:] = list(light)
+    c.sphere_radius = radius
+    c.width, c.height = width, height
+    c.clear_rgba[:] = list(clear)
+    return c
 
 
 class PBDError(RuntimeError):
@@ -115,6 +163,7 @@ def lib():
             "pbd_batch_launches_per_step": [vp, u32p],
             "pbd_batch_profile_frames": [vp, i32, vp, C.POINTER(KernelStat), u32, u32p],
             "pbd_adjoint_forward": [vp, i32, i32, vp],
+            "pbd_render_sprites": [vp, C.POINTER(Camera), C.POINTER(C.c_uint8), fp, vp],
             "pbd_density_error": [vp, fp, C.POINTER(C.c_double), C.POINTER(C.c_double), vp],
             "pbd_adjoint_backward": [vp, fp, fp, fp, C.POINTER(C.c_double), C.POINTER(C.c_double), vp],
         }
@@ -269,6 +318,14 @@ class Sim:
         v = C.c_uint32()
         check(self.L.pbd_launches_per_step(self.h, C.byref(v)))
         return v.value
+
+    def render(self, cam, stream=0):
+        """(rgba (H, W, 4) uint8 rows top-down, depth (H, W) float32) of the particle sprites"""
+        rgba = np.zeros((cam.height, cam.width, 4), np.uint8)
+        depth = np.zeros((cam.height, cam.width), np.float32)
+        check(self.L.pbd_render_sprites(self.h, C.byref(cam), rgba.ctypes.data_as(C.POINTER(C.c_uint8)), _fp(depth),
+                                        C.c_void_p(stream)))
+        return rgba, depth
 
     def density_error(self, stream=0):
         """(C_i per particle in the current order, mean |C|, max |C|) after the last frame"""
