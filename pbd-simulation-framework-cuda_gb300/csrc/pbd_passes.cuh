@@ -186,17 +186,26 @@ __device__ __forceinline__ uint32_t walk_coop(const DevParams& P, const SceneCtx
 // end_contacts, then the rest.  Entries go in batches of kListBatch: the batch's index loads,
 // then its position loads, are all in flight before the first contribution, instead of one
 // dependent pair per entry.
+// Every visitor adds its contributions with __fadd_rn: an explicitly rounded add is never
+// fused with the product that made the contribution, so the sums get the same bits whichever
+// walker (cells, stored list, cooperative warp) and whichever loop shape the compiler sees.
+//
+// kOwn: the list was written by this thread in this kernel, so it is read with ordinary
+// (coherent) loads rather than through the read-only path.
 constexpr uint32_t kListBatch = 4;
-template <class V>
+template <bool kOwn = false, class V>
 __device__ __forceinline__ void walk_list_part(const NbList& L, uint32_t i, uint32_t k0, uint32_t k1, bool contact,
                                                const float4* __restrict__ p, V& vis) {
-    const uint32_t* __restrict__ e = L.list + i;
+    const uint32_t* e = L.list + i;
 #pragma unroll 1
     for (uint32_t kb = k0; kb < k1; kb += kListBatch) {
         uint32_t j[kListBatch];
         float4 pj[kListBatch];
 #pragma unroll
-        for (uint32_t b = 0; b < kListBatch; ++b) j[b] = (kb + b < k1) ? __ldg(e + (size_t)(kb + b) * L.stride) : i;
+        for (uint32_t b = 0; b < kListBatch; ++b) {
+            const uint32_t* a = e + (size_t)(kb + b) * L.stride;
+            j[b] = (kb + b < k1) ? (kOwn ? *a : __ldg(a)) : i;
+        }
 #pragma unroll
         for (uint32_t b = 0; b < kListBatch; ++b) pj[b] = __ldg(p + j[b]);
 #pragma unroll
@@ -204,12 +213,46 @@ __device__ __forceinline__ void walk_list_part(const NbList& L, uint32_t i, uint
             if (kb + b < k1) vis.add(vis.contrib(j[b], pj[b], contact), contact);
     }
 }
-template <class V>
+template <bool kOwn = false, class V>
 __device__ __forceinline__ void walk_list(const NbList& L, uint32_t i, uint32_t meta, const float4* __restrict__ p, V& vis) {
     const uint32_t n = meta & 0xFFu, nc = (meta >> 8) & 0xFFu;
-    walk_list_part(L, i, 0u, nc, true, p, vis);
+    walk_list_part<kOwn>(L, i, 0u, nc, true, p, vis);
     vis.end_contacts(nc);
-    walk_list_part(L, i, nc, n, false, p, vis);
+    walk_list_part<kOwn>(L, i, nc, n, false, p, vis);
+}
+
+// Particle i's near list from its full list (meta fm): the entries with r^2 < cut2 at p, in
+// list order, the boundary of the contact entries kept.  No sums: a pass then walks the near
+// list alone (every entry left out adds an exact zero to every sum of a lambda, omega or delta
+// pass), so the warp runs the kernel arithmetic for ~6 entries per particle instead of ~32.
+// Returns the near list's meta (kListOff when it does not fit).
+__device__ __forceinline__ uint32_t filter_list(const NbList& F, uint32_t fm, const NbList& L, uint32_t i,
+                                                const float4& pi, float cut2, const float4* __restrict__ p) {
+    const uint32_t n = fm & 0xFFu, nc = (fm >> 8) & 0xFFu;
+    const uint32_t* __restrict__ e = F.list + i;
+    uint32_t m = 0, mc = 0;
+#pragma unroll 1
+    for (uint32_t kb = 0; kb < n; kb += kListBatch) {
+        uint32_t j[kListBatch];
+        float4 pj[kListBatch];
+#pragma unroll
+        for (uint32_t b = 0; b < kListBatch; ++b) j[b] = (kb + b < n) ? __ldg(e + (size_t)(kb + b) * F.stride) : i;
+#pragma unroll
+        for (uint32_t b = 0; b < kListBatch; ++b) pj[b] = __ldg(p + j[b]);
+#pragma unroll
+        for (uint32_t b = 0; b < kListBatch; ++b) {
+            if (kb + b == nc) mc = m;
+            if (kb + b < n) {
+                const float rx = pi.x - pj[b].x, ry = pi.y - pj[b].y, rz = pi.z - pj[b].z;
+                if (rx * rx + ry * ry + rz * rz < cut2) {
+                    if (m < L.kmax) L.list[(size_t)m * L.stride + i] = j[b];
+                    ++m;
+                }
+            }
+        }
+    }
+    if (nc >= n) mc = m;
+    return m > L.kmax ? kListOff : (m | (mc << 8));
 }
 
 // Wraps the visitor of a walking pass and keeps particle i's near list (when `list` is set)
@@ -253,6 +296,17 @@ struct Recorder {
         const uint32_t c = fnc == 0xFFFFFFFFu ? fn : fnc;
         return fn > fkmax ? kListOff : (fn | (c << 8));
     }
+};
+
+// A visitor that sums nothing: a walk with Recorder<NullVisit> only stores the lists.
+struct NullVisit {
+    struct Contrib {};
+    __device__ static Contrib zero() { return Contrib{}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ __forceinline__ Contrib contrib(uint32_t, const float4&, bool) const { return Contrib{}; }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
 };
 
 __device__ __forceinline__ float shfl_f(float v, int k) { return __shfl_sync(kFullMask, v, k); }
@@ -311,8 +365,8 @@ struct LambdaVisit {
     }
     __device__ __forceinline__ void add(const Contrib& c, bool) {
         if (!c.near) return;
-        A += c.a; B += c.b;
-        Cx += c.gx; Cy += c.gy; Cz += c.gz; Cw += c.gw;
+        A = __fadd_rn(A, c.a); B = __fadd_rn(B, c.b);
+        Cx = __fadd_rn(Cx, c.gx); Cy = __fadd_rn(Cy, c.gy); Cz = __fadd_rn(Cz, c.gz); Cw = __fadd_rn(Cw, c.gw);
     }
     // the sums the reverse pass needs: aux[i] = (rho, B, S.x, S.y), aux[N + i] = (S.z, S.w, 0, 0)
     __device__ __forceinline__ void store_aux(float4* __restrict__ aux, uint32_t N, uint32_t i) const {
@@ -342,13 +396,19 @@ lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restric
     LambdaVisit vis(P, pi);
     bool deferred = false;
     if (L.list || F.list) {
-        Recorder<LambdaVisit> rec(vis, L, F, F.list != nullptr, i, pi, P.cut2);
+        // the walk stores the lists; the sums then run over the shortest list that fits
+        Recorder<NullVisit> rec(NullVisit{}, L, F, F.list != nullptr, i, pi, P.cut2);
         walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
-        if (L.list) L.meta[i] = deferred ? kListOff : rec.meta();
-        if (F.list) F.meta[i] = deferred ? kListOff : rec.fmeta();
+        const uint32_t lm = (L.list && !deferred) ? rec.meta() : kListOff;
+        const uint32_t fm = (F.list && !deferred) ? rec.fmeta() : kListOff;
+        if (L.list) L.meta[i] = lm;
+        if (F.list) F.meta[i] = fm;
         if (!deferred) {
-            lambda[i] = rec.inner.finish(S.rho0);
-            if (aux) rec.inner.store_aux(aux, P.N, i);
+            if (lm != kListOff) walk_list<true>(L, i, lm, p, vis);
+            else if (fm != kListOff) walk_list<true>(F, i, fm, p, vis);
+            else walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
+            lambda[i] = vis.finish(S.rho0);
+            if (aux) vis.store_aux(aux, P.N, i);
             return;
         }
     } else {
@@ -394,18 +454,13 @@ lambda_list_kernel(DevParams P, const float4* __restrict__ p, float* __restrict_
     }
     const SceneCtx S = scene_ctx(P, i);
     const float4 pi = p[i];
-    if (L.list) {
-        Recorder<LambdaVisit> rec(LambdaVisit(P, pi), L, F, false, i, pi, P.cut2);
-        walk_list(F, i, fm, p, rec);
-        L.meta[i] = rec.meta();
-        lambda[i] = rec.inner.finish(S.rho0);
-        if (aux) rec.inner.store_aux(aux, P.N, i);
-    } else {
-        LambdaVisit vis(P, pi);
-        walk_list(F, i, fm, p, vis);
-        lambda[i] = vis.finish(S.rho0);
-        if (aux) vis.store_aux(aux, P.N, i);
-    }
+    LambdaVisit vis(P, pi);
+    const uint32_t lm = L.list ? filter_list(F, fm, L, i, pi, P.cut2, p) : kListOff;
+    if (L.list) L.meta[i] = lm;
+    if (lm != kListOff) walk_list<true>(L, i, lm, p, vis);
+    else walk_list(F, i, fm, p, vis);
+    lambda[i] = vis.finish(S.rho0);
+    if (aux) vis.store_aux(aux, P.N, i);
 }
 
 // ======================================================================================
@@ -482,11 +537,11 @@ struct DeltaVisit {
         return c;
     }
     __device__ __forceinline__ void add(const Contrib& c, bool) {
-        if (c.flags & 1u) { ax += c.ax; ay += c.ay; az += c.az; aw += c.aw; }
+        if (c.flags & 1u) { ax = __fadd_rn(ax, c.ax); ay = __fadd_rn(ay, c.ay); az = __fadd_rn(az, c.az); aw = __fadd_rn(aw, c.aw); }
         if (c.flags & 2u) {
-            pacc.x += c.cx; xacc.x += c.cx;
-            pacc.y += c.cy; xacc.y += c.cy;
-            pacc.z += c.cz; xacc.z += c.cz;
+            pacc.x = __fadd_rn(pacc.x, c.cx); xacc.x = __fadd_rn(xacc.x, c.cx);
+            pacc.y = __fadd_rn(pacc.y, c.cy); xacc.y = __fadd_rn(xacc.y, c.cy);
+            pacc.z = __fadd_rn(pacc.z, c.cz); xacc.z = __fadd_rn(xacc.z, c.cz);
         }
     }
 };
@@ -621,7 +676,7 @@ struct OmegaVisit {
     }
     __device__ __forceinline__ void add(const Contrib& c, bool) {
         if (!c.near) return;
-        ox += c.ox; oy += c.oy; oz += c.oz;
+        ox = __fadd_rn(ox, c.ox); oy = __fadd_rn(oy, c.oy); oz = __fadd_rn(oz, c.oz);
     }
 };
 
@@ -669,16 +724,12 @@ omega_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __res
         return;
     }
     const float4 pi = p[i];
-    if (L.list) {
-        Recorder<OmegaVisit> rec(OmegaVisit(P, v, pi, v[i]), L, F, false, i, pi, P.cut2);
-        walk_list(F, i, fm, p, rec);
-        L.meta[i] = rec.meta();
-        omega[i] = make_float4(rec.inner.ox, rec.inner.oy, rec.inner.oz, 0.f);
-    } else {
-        OmegaVisit vis(P, v, pi, v[i]);
-        walk_list(F, i, fm, p, vis);
-        omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
-    }
+    OmegaVisit vis(P, v, pi, v[i]);
+    const uint32_t lm = L.list ? filter_list(F, fm, L, i, pi, P.cut2, p) : kListOff;
+    if (L.list) L.meta[i] = lm;
+    if (lm != kListOff) walk_list<true>(L, i, lm, p, vis);
+    else walk_list(F, i, fm, p, vis);
+    omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
 }
 
 __global__ void __launch_bounds__(128)
@@ -743,8 +794,8 @@ struct VortViscVisit {
         return c;
     }
     __device__ __forceinline__ void add(const Contrib& c, bool) {
-        if (c.flags & 1u) { gx += c.gx; gy += c.gy; gz += c.gz; }
-        if (c.flags & 2u) { sx += c.sx; sy += c.sy; sz += c.sz; sw += c.sw; }
+        if (c.flags & 1u) { gx = __fadd_rn(gx, c.gx); gy = __fadd_rn(gy, c.gy); gz = __fadd_rn(gz, c.gz); }
+        if (c.flags & 2u) { sx = __fadd_rn(sx, c.sx); sy = __fadd_rn(sy, c.sy); sz = __fadd_rn(sz, c.sz); sw = __fadd_rn(sw, c.sw); }
     }
 };
 
@@ -788,11 +839,13 @@ vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
 }
 
 // vorticity + viscosity over a stored list (the full list with vorticity, else the omega pass's
-// near list); particles without one go to vort_visc_coop_kernel.
+// near list); particles without one go to vort_visc_coop_kernel.  With both terms and the omega
+// pass's near list Ln at hand, vorticity runs over the full list and viscosity over the near list
+// (its entries beyond the cut add exact zeros): the two sums keep their own order.
 __global__ void __launch_bounds__(256, 5)
 vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ vin,
                       float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
-                      int do_vort, int do_visc, const float* __restrict__ w, DeferList D, NbList Lv) {
+                      int do_vort, int do_visc, const float* __restrict__ w, DeferList D, NbList Lv, NbList Ln) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const uint32_t meta = Lv.meta[i];
@@ -801,6 +854,17 @@ vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* _
         return;
     }
     const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const uint32_t nm = (do_vort && do_visc && Ln.list) ? Ln.meta[i] : kListOff;
+    if (nm != kListOff) {
+        VortViscVisit vo(P, vin, omega, p[i], vin[i], oi, true, false);
+        walk_list(Lv, i, meta, p, vo);
+        VortViscVisit vs(P, vin, omega, p[i], vin[i], oi, false, true);
+        walk_list(Ln, i, nm, p, vs);
+        vo.sx = vs.sx; vo.sy = vs.sy; vo.sz = vs.sz; vo.sw = vs.sw;
+        vo.visc = true;
+        vort_visc_finish(P, i, vo, vout, fext, w);
+        return;
+    }
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
     walk_list(Lv, i, meta, p, vis);
     vort_visc_finish(P, i, vis, vout, fext, w);
@@ -840,7 +904,7 @@ struct DensityVisit {
         if (r2 >= P.cut2) return zero();
         return Contrib{poly6(P, sqrtf(r2)), 1u};
     }
-    __device__ __forceinline__ void add(const Contrib& c, bool) { if (c.near) A += c.a; }
+    __device__ __forceinline__ void add(const Contrib& c, bool) { if (c.near) A = __fadd_rn(A, c.a); }
 };
 
 // err[i] = C_i; acc[0] += |C_i| (double), acc[1] = max |C_i| (double bits, non-negative)

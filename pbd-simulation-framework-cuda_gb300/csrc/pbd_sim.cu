@@ -451,7 +451,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     }
     if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
         PROF_BEGIN(use_full ? "omega_list" : "omega");
-        const NbList Lo = (act & PBD_ACTIVE_COMPUTE_VORTICITY) ? L0 : L;   // near lists for viscosity alone
+        // near lists for viscosity (over the full list, omega filters them out before its sums)
+        const NbList Lo = (use_full || !(act & PBD_ACTIVE_COMPUTE_VORTICITY)) ? L : L0;
         if (use_full)
             omega_list_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->omega, D, Lo, F);
         else
@@ -464,10 +465,11 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     if (vort || visc) {
         // vorticity sums every list entry: the full list; viscosity alone: the omega pass's near list
         const NbList Lv = vort ? F : ((act & PBD_ACTIVE_COMPUTE_OMEGAS) ? L : L0);
+        const NbList Ln = (vort && use_full && (act & PBD_ACTIVE_COMPUTE_OMEGAS)) ? L : L0;
         PROF_BEGIN(Lv.list ? "vort_visc_list" : "vort_visc");
         if (Lv.list)
             vort_visc_list_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->v[cur.v ^ 1], s->omega, s->fext,
-                                                     vort, visc, wf, D, Lv);
+                                                     vort, visc, wf, D, Lv, Ln);
         else
             vort_visc_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega, s->fext,
                                                 s->cell_start, s->cell_end, vort, visc, wf, D);
