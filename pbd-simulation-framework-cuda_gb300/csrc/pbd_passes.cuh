@@ -1,24 +1,49 @@
-// pbd_passes.cuh -- the neighbour passes of a frame (no stored neighbour list).
+// pbd_passes.cuh -- the neighbour passes of a frame.
 //
 // The reference builds an explicit N x M list once per frame (findContacts +
 // findNeighbours, kernel/Collision.h:11-160) and every density/vorticity/viscosity kernel
-// loops over it (kernel/Density.h).  Here every pass re-walks the cells in exactly the order
-// the list would hold them (27 cells with the x offset outer and z inner, then the shells of
-// findNeighbours), skipping self and stopping at the cap M, so sums run in the list's order.
+// loops over it (kernel/Density.h).  Here the frame's first lambda pass walks the cells in
+// exactly the order the list would hold them (27 cells with the x offset outer and z inner,
+// then the shells of findNeighbours), skipping self and stopping at the cap M, and stores the
+// result (the full list); later passes read the stored lists, so sums run in the list's order.
 //
 // Each pass is split into a per-candidate contribution (`contrib`) and an in-order
-// accumulation (`add`).  Two walkers drive them:
-//  - walk_seq: one thread per particle (the common case);
+// accumulation (`add`); a visitor may also name per-neighbour data (`Extra`, loaded by
+// `fetch(j)`) that the walkers load together with the neighbour's position.  Three walkers
+// drive them:
+//  - walk_seq: one thread per particle over the cells;
 //  - walk_coop: one warp per particle.  Lanes evaluate 32 candidates at once and the
 //    contributions are added in list order through shuffles, so the result is bit-identical
 //    to walk_seq.  It takes the particles whose walk meets a cell range longer than
 //    kLongRange -- in practice the range that SortReorder.h:183-184 extends to N (up to M
-//    entries) -- which would otherwise serialise a whole warp behind one thread.
+//    entries) -- which would otherwise serialise a whole warp behind one thread;
+//  - walk_list: one thread per particle over a stored list.
 #pragma once
+#include <type_traits>
 #include "pbd_device.cuh"
 #include "../../include/pbd.h"
 
 namespace pbd {
+
+// Per-neighbour data a visitor loads with the neighbour's position: V::Extra and V::fetch(j)
+// when the visitor declares them, nothing otherwise.
+struct NoExtra {};
+template <class V, class = void> struct ExtraOf { using type = NoExtra; static constexpr bool has = false; };
+template <class V> struct ExtraOf<V, std::void_t<typename V::Extra>> {
+    using type = typename V::Extra;
+    static constexpr bool has = true;
+};
+template <class V>
+__device__ __forceinline__ typename ExtraOf<V>::type fetch_extra(const V& vis, uint32_t j) {
+    if constexpr (ExtraOf<V>::has) return vis.fetch(j);
+    else return NoExtra{};
+}
+template <class V>
+__device__ __forceinline__ typename V::Contrib contrib_of(V& vis, uint32_t j, const float4& pj,
+                                                          const typename ExtraOf<V>::type& ex, bool contact) {
+    if constexpr (ExtraOf<V>::has) return vis.contrib(j, pj, ex, contact);
+    else return vis.contrib(j, pj, contact);
+}
 
 constexpr uint32_t kLongRange = 32;
 constexpr uint32_t kFullMask = 0xffffffffu;
@@ -137,7 +162,7 @@ __device__ __forceinline__ uint32_t walk_seq(const DevParams& P, const SceneCtx&
         if (defer && e - s > kLongRange) { *deferred = true; return true; }
         for (uint32_t j = s; j < e; ++j) {
             if (j == i) continue;
-            vis.add(vis.contrib(j, __ldg(p + j), contact), contact);
+            vis.add(contrib_of(vis, j, __ldg(p + j), fetch_extra(vis, j), contact), contact);
             if (++cnt == M) return true;
         }
         return false;
@@ -162,7 +187,7 @@ __device__ __forceinline__ uint32_t walk_coop(const DevParams& P, const SceneCtx
             bool valid = j < e && j != i;
             const uint32_t b = __ballot_sync(kFullMask, valid);
             valid = valid && __popc(b & lt) < M - cnt;
-            typename V::Contrib c = valid ? vis.contrib(j, __ldg(p + j), contact) : V::zero();
+            typename V::Contrib c = valid ? contrib_of(vis, j, __ldg(p + j), fetch_extra(vis, j), contact) : V::zero();
             const uint32_t n = __popc(__ballot_sync(kFullMask, valid));
             // only entries whose contribution changes a sum are added (in order); the others
             // are exact no-ops of add() and still count toward the cap
@@ -192,33 +217,53 @@ __device__ __forceinline__ uint32_t walk_coop(const DevParams& P, const SceneCtx
 //
 // kOwn: the list was written by this thread in this kernel, so it is read with ordinary
 // (coherent) loads rather than through the read-only path.
-constexpr uint32_t kListBatch = 4;
-template <bool kOwn = false, class V>
+// Batch sizes measured on fluid_1m (1M particles, GB300): full lists 4 (2, 3, 6 and 8 were
+// slower), near lists 1 (2, 3 and 8 slower; a deeper software pipeline too).
+constexpr uint32_t kListBatch = 4;   // full lists (~32 entries)
+constexpr uint32_t kNearBatch = 1;   // near lists (~6 entries)
+template <bool kOwn = false, uint32_t B = kListBatch, class V>
 __device__ __forceinline__ void walk_list_part(const NbList& L, uint32_t i, uint32_t k0, uint32_t k1, bool contact,
                                                const float4* __restrict__ p, V& vis) {
     const uint32_t* e = L.list + i;
-#pragma unroll 1
-    for (uint32_t kb = k0; kb < k1; kb += kListBatch) {
-        uint32_t j[kListBatch];
-        float4 pj[kListBatch];
+    uint32_t jn[B];
 #pragma unroll
-        for (uint32_t b = 0; b < kListBatch; ++b) {
-            const uint32_t* a = e + (size_t)(kb + b) * L.stride;
-            j[b] = (kb + b < k1) ? (kOwn ? *a : __ldg(a)) : i;
+    for (uint32_t b = 0; b < B; ++b) {
+        const uint32_t* a = e + (size_t)(k0 + b) * L.stride;
+        jn[b] = (k0 + b < k1) ? (kOwn ? *a : __ldg(a)) : i;
+    }
+#pragma unroll 1
+    for (uint32_t kb = k0; kb < k1; kb += B) {
+        uint32_t j[B];
+        float4 pj[B];
+        typename ExtraOf<V>::type ex[B];
+#pragma unroll
+        for (uint32_t b = 0; b < B; ++b) j[b] = jn[b];
+#pragma unroll
+        for (uint32_t b = 0; b < B; ++b) {
+            pj[b] = __ldg(p + j[b]);
+            ex[b] = fetch_extra(vis, j[b]);
         }
 #pragma unroll
-        for (uint32_t b = 0; b < kListBatch; ++b) pj[b] = __ldg(p + j[b]);
+        for (uint32_t b = 0; b < B; ++b) {
+            const uint32_t* a = e + (size_t)(kb + B + b) * L.stride;
+            jn[b] = (kb + B + b < k1) ? (kOwn ? *a : __ldg(a)) : i;
+        }
 #pragma unroll
-        for (uint32_t b = 0; b < kListBatch; ++b)
-            if (kb + b < k1) vis.add(vis.contrib(j[b], pj[b], contact), contact);
+        for (uint32_t b = 0; b < B; ++b)
+            if (kb + b < k1) vis.add(contrib_of(vis, j[b], pj[b], ex[b], contact), contact);
     }
 }
-template <bool kOwn = false, class V>
+template <bool kOwn = false, uint32_t B = kListBatch, class V>
 __device__ __forceinline__ void walk_list(const NbList& L, uint32_t i, uint32_t meta, const float4* __restrict__ p, V& vis) {
     const uint32_t n = meta & 0xFFu, nc = (meta >> 8) & 0xFFu;
-    walk_list_part<kOwn>(L, i, 0u, nc, true, p, vis);
+    walk_list_part<kOwn, B>(L, i, 0u, nc, true, p, vis);
     vis.end_contacts(nc);
-    walk_list_part<kOwn>(L, i, nc, n, false, p, vis);
+    walk_list_part<kOwn, B>(L, i, nc, n, false, p, vis);
+}
+// A near list (~6 entries): one entry at a time, the next entry's index in flight.
+template <bool kOwn = false, class V>
+__device__ __forceinline__ void walk_near(const NbList& L, uint32_t i, uint32_t meta, const float4* __restrict__ p, V& vis) {
+    walk_list<kOwn, kNearBatch>(L, i, meta, p, vis);
 }
 
 // Particle i's near list from its full list (meta fm): the entries with r^2 < cut2 at p, in
@@ -226,19 +271,31 @@ __device__ __forceinline__ void walk_list(const NbList& L, uint32_t i, uint32_t 
 // list alone (every entry left out adds an exact zero to every sum of a lambda, omega or delta
 // pass), so the warp runs the kernel arithmetic for ~6 entries per particle instead of ~32.
 // Returns the near list's meta (kListOff when it does not fit).
+template <bool kOwn = false>
 __device__ __forceinline__ uint32_t filter_list(const NbList& F, uint32_t fm, const NbList& L, uint32_t i,
                                                 const float4& pi, float cut2, const float4* __restrict__ p) {
     const uint32_t n = fm & 0xFFu, nc = (fm >> 8) & 0xFFu;
-    const uint32_t* __restrict__ e = F.list + i;
+    const uint32_t* e = F.list + i;
     uint32_t m = 0, mc = 0;
+    uint32_t jn[kListBatch];
+#pragma unroll
+    for (uint32_t b = 0; b < kListBatch; ++b) {
+        const uint32_t* a = e + (size_t)b * F.stride;
+        jn[b] = (b < n) ? (kOwn ? *a : __ldg(a)) : i;
+    }
 #pragma unroll 1
     for (uint32_t kb = 0; kb < n; kb += kListBatch) {
         uint32_t j[kListBatch];
         float4 pj[kListBatch];
 #pragma unroll
-        for (uint32_t b = 0; b < kListBatch; ++b) j[b] = (kb + b < n) ? __ldg(e + (size_t)(kb + b) * F.stride) : i;
+        for (uint32_t b = 0; b < kListBatch; ++b) j[b] = jn[b];
 #pragma unroll
         for (uint32_t b = 0; b < kListBatch; ++b) pj[b] = __ldg(p + j[b]);
+#pragma unroll
+        for (uint32_t b = 0; b < kListBatch; ++b) {
+            const uint32_t* a = e + (size_t)(kb + kListBatch + b) * F.stride;
+            jn[b] = (kb + kListBatch + b < n) ? (kOwn ? *a : __ldg(a)) : i;
+        }
 #pragma unroll
         for (uint32_t b = 0; b < kListBatch; ++b) {
             if (kb + b == nc) mc = m;
@@ -261,6 +318,7 @@ __device__ __forceinline__ uint32_t filter_list(const NbList& F, uint32_t fm, co
 template <class V>
 struct Recorder {
     using Contrib = typename V::Contrib;
+    using Extra = typename ExtraOf<V>::type;
     V inner;
     uint32_t* list;
     uint32_t* flist;
@@ -273,7 +331,8 @@ struct Recorder {
           fkmax(F.kmax), i(i_), pi(p_i), cut2(c2) {}
     __device__ static Contrib zero() { return V::zero(); }
     __device__ __forceinline__ void end_contacts(uint32_t c) { nc = n; fnc = fn; inner.end_contacts(c); }
-    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool contact) {
+    __device__ __forceinline__ Extra fetch(uint32_t j) const { return fetch_extra(inner, j); }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, const Extra& ex, bool contact) {
         if (flist) {
             if (fn < fkmax) flist[(size_t)fn * fstride + i] = j;
             ++fn;
@@ -285,7 +344,7 @@ struct Recorder {
                 ++n;
             }
         }
-        return inner.contrib(j, pj, contact);
+        return contrib_of(inner, j, pj, ex, contact);
     }
     __device__ __forceinline__ void add(const Contrib& c, bool contact) { inner.add(c, contact); }
     __device__ __forceinline__ uint32_t meta() const {
@@ -295,6 +354,30 @@ struct Recorder {
     __device__ __forceinline__ uint32_t fmeta() const {
         const uint32_t c = fnc == 0xFFFFFFFFu ? fn : fnc;
         return fn > fkmax ? kListOff : (fn | (c << 8));
+    }
+};
+
+// A walk that only stores particle i's full list: indices, no positions (the walk's position
+// loads are dead and vanish), the boundary of the contact entries kept.
+struct ListRecorder {
+    struct Contrib {};
+    uint32_t* list;
+    uint32_t stride, kmax, i;
+    uint32_t n = 0, nc = 0xFFFFFFFFu;
+    __device__ ListRecorder(const NbList& F, uint32_t i_) : list(F.list), stride(F.stride), kmax(F.kmax), i(i_) {}
+    __device__ static Contrib zero() { return Contrib{}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ void end_contacts(uint32_t) { nc = n; }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4&, bool) {
+        if (n < kmax) list[(size_t)n * stride + i] = j;
+        ++n;
+        return Contrib{};
+    }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
+    __device__ __forceinline__ uint32_t meta() const {
+        const uint32_t c = nc == 0xFFFFFFFFu ? n : nc;
+        return n > kmax ? kListOff : (n | (c << 8));
     }
 };
 
@@ -395,17 +478,31 @@ lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restric
     const float4 pi = p[i];
     LambdaVisit vis(P, pi);
     bool deferred = false;
-    if (L.list || F.list) {
-        // the walk stores the lists; the sums then run over the shortest list that fits
-        Recorder<NullVisit> rec(NullVisit{}, L, F, F.list != nullptr, i, pi, P.cut2);
+    if (F.list) {
+        // the walk stores the full list (indices only), the filter the near list; the sums then
+        // run over the shortest list that fits
+        ListRecorder rec(F, i);
         walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
-        const uint32_t lm = (L.list && !deferred) ? rec.meta() : kListOff;
-        const uint32_t fm = (F.list && !deferred) ? rec.fmeta() : kListOff;
+        const uint32_t fm = deferred ? kListOff : rec.meta();
+        F.meta[i] = fm;
+        const uint32_t lm = (L.list && fm != kListOff) ? filter_list<true>(F, fm, L, i, pi, P.cut2, p) : kListOff;
         if (L.list) L.meta[i] = lm;
-        if (F.list) F.meta[i] = fm;
         if (!deferred) {
-            if (lm != kListOff) walk_list<true>(L, i, lm, p, vis);
+            if (lm != kListOff) walk_near<true>(L, i, lm, p, vis);
             else if (fm != kListOff) walk_list<true>(F, i, fm, p, vis);
+            else walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
+            lambda[i] = vis.finish(S.rho0);
+            if (aux) vis.store_aux(aux, P.N, i);
+            return;
+        }
+    } else if (L.list) {
+        // the walk stores the near list; the sums then run over it when it fits
+        Recorder<NullVisit> rec(NullVisit{}, L, F, false, i, pi, P.cut2);
+        walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
+        const uint32_t lm = deferred ? kListOff : rec.meta();
+        L.meta[i] = lm;
+        if (!deferred) {
+            if (lm != kListOff) walk_near<true>(L, i, lm, p, vis);
             else walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
             lambda[i] = vis.finish(S.rho0);
             if (aux) vis.store_aux(aux, P.N, i);
@@ -457,7 +554,7 @@ lambda_list_kernel(DevParams P, const float4* __restrict__ p, float* __restrict_
     LambdaVisit vis(P, pi);
     const uint32_t lm = L.list ? filter_list(F, fm, L, i, pi, P.cut2, p) : kListOff;
     if (L.list) L.meta[i] = lm;
-    if (lm != kListOff) walk_list<true>(L, i, lm, p, vis);
+    if (lm != kListOff) walk_near<true>(L, i, lm, p, vis);
     else walk_list(F, i, fm, p, vis);
     lambda[i] = vis.finish(S.rho0);
     if (aux) vis.store_aux(aux, P.N, i);
@@ -500,7 +597,9 @@ struct DeltaVisit {
                        shfl_f(c.cy, k), shfl_f(c.cz, k), shfl_u(c.flags, k)};
     }
     __device__ __forceinline__ void end_contacts(uint32_t) {}
-    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool contact) const {
+    using Extra = float;   // lambda_j
+    __device__ __forceinline__ float fetch(uint32_t j) const { return do_delta ? __ldg(lambda + j) : 0.f; }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, float lj, bool contact) const {
         Contrib c = zero();
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z, rw = pi.w - pj.w;
         const float r2 = rx * rx + ry * ry + rz * rz;
@@ -511,7 +610,7 @@ struct DeltaVisit {
             if (s != 0.0f || all_pairs) {
                 const float W = poly6(P, dist);
                 const float sc = -P.k_scorr * powi(W * P.inv_wq, P.n_scorr);
-                const float coef = (li + __ldg(lambda + j) + sc) * s;
+                const float coef = (li + lj + sc) * s;
                 c.ax = coef * rx; c.ay = coef * ry; c.az = coef * rz; c.aw = coef * rw;
                 c.flags |= 1u;
             }
@@ -595,11 +694,14 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const f
 }
 
 // delta pass 0 of an iteration over the near lists its lambda pass recorded; particles
-// without one go to delta_coop_kernel.
+// without one go to delta_coop_kernel.  kMode != 0: the pass mode fixed at compile time (the
+// two passes of a fluid frame), kMode = 0: `mode` at run time.
+template <uint32_t kMode>
 __global__ void __launch_bounds__(256)
-delta_list_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, float4* __restrict__ pout,
+delta_list_kernel(DevParams P, uint32_t mode_rt, const float4* __restrict__ pin, float4* __restrict__ pout,
                   float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
                   const float* __restrict__ w, float4* __restrict__ delta, DeferList D, NbList L) {
+    const uint32_t mode = kMode ? kMode : mode_rt;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const uint32_t meta = L.meta[i];
@@ -613,7 +715,7 @@ delta_list_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, fl
     const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
     const SceneCtx S = scene_ctx(P, i);
     DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
-    walk_list(L, i, meta, pin, vis);
+    walk_near(L, i, meta, pin, vis);
     delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
 }
 
@@ -662,14 +764,15 @@ struct OmegaVisit {
         return Contrib{shfl_f(c.ox, k), shfl_f(c.oy, k), shfl_f(c.oz, k), shfl_u(c.near, k)};
     }
     __device__ __forceinline__ void end_contacts(uint32_t) {}
-    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool) const {
+    using Extra = float4;   // v_j
+    __device__ __forceinline__ float4 fetch(uint32_t j) const { return __ldg(v + j); }
+    __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, const float4& vj, bool) const {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z, rw = pi.w - pj.w;
         const float r2 = rx * rx + ry * ry + rz * rz;
         if (r2 >= P.cut2) return zero();
         const float dist = sqrtf(r2);
         const float s = spiky_scale(P, dist, r2 + rw * rw);
         if (s == 0.0f) return zero();
-        const float4 vj = __ldg(v + j);
         const float wx = vj.x - vi.x, wy = vj.y - vi.y, wz = vj.z - vi.z;
         const float gx = s * rx, gy = s * ry, gz = s * rz;
         return Contrib{wy * gz - wz * gy, wz * gx - wx * gz, wx * gy - wy * gx, 1u};
@@ -727,8 +830,8 @@ omega_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __res
     OmegaVisit vis(P, v, pi, v[i]);
     const uint32_t lm = L.list ? filter_list(F, fm, L, i, pi, P.cut2, p) : kListOff;
     if (L.list) L.meta[i] = lm;
-    if (lm != kListOff) walk_list<true>(L, i, lm, p, vis);
-    else walk_list(F, i, fm, p, vis);
+    if (lm != kListOff) walk_near<true>(L, i, lm, p, vis);
+    else walk_list<false, 2>(F, i, fm, p, vis);
     omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
 }
 
@@ -749,7 +852,13 @@ omega_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __res
 // Vorticity sums |omega_j - omega_i| / (p_j - p_i + 1e-8) componentwise over EVERY list
 // entry (no kernel weight), so with vorticity on no pair may be skipped.
 // ======================================================================================
-struct VortViscVisit {
+// kTerms: the terms this visitor may run (1 vorticity, 2 viscosity, 3 either, as the run-time
+// flags say); a visitor for one term loads one neighbour vector per entry.
+template <uint32_t T> struct VortViscExtra { float4 oj, vj; };
+template <> struct VortViscExtra<1u> { float4 oj; };
+template <> struct VortViscExtra<2u> { float4 vj; };
+template <uint32_t kTerms = 3u>
+struct VortViscVisitT {
     struct Contrib { float gx, gy, gz, sx, sy, sz, sw; uint32_t flags; };   // 1 vorticity, 2 viscosity
     const DevParams& P;
     const float4* __restrict__ v;
@@ -758,9 +867,9 @@ struct VortViscVisit {
     bool vort, visc;
     float gx = 0.f, gy = 0.f, gz = 0.f;
     float sx = 0.f, sy = 0.f, sz = 0.f, sw = 0.f;
-    __device__ VortViscVisit(const DevParams& P_, const float4* v_, const float4* om, float4 pi_, float4 vi_, float4 oi_,
-                             bool vo, bool vs)
-        : P(P_), v(v_), omega(om), pi(pi_), vi(vi_), oi(oi_), vort(vo), visc(vs) {}
+    __device__ VortViscVisitT(const DevParams& P_, const float4* v_, const float4* om, float4 pi_, float4 vi_, float4 oi_,
+                              bool vo, bool vs)
+        : P(P_), v(v_), omega(om), pi(pi_), vi(vi_), oi(oi_), vort(vo && (kTerms & 1u)), visc(vs && (kTerms & 2u)) {}
     __device__ void reset() { gx = gy = gz = sx = sy = sz = sw = 0.f; }
     __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u}; }
     __device__ static bool effective(const Contrib& c) { return c.flags != 0u; }
@@ -769,10 +878,17 @@ struct VortViscVisit {
                        shfl_f(c.sy, k), shfl_f(c.sz, k), shfl_f(c.sw, k), shfl_u(c.flags, k)};
     }
     __device__ __forceinline__ void end_contacts(uint32_t) {}
-    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool) const {
+    using Extra = VortViscExtra<kTerms>;
+    __device__ __forceinline__ Extra fetch(uint32_t j) const {
+        Extra e;
+        if constexpr ((kTerms & 1u) != 0u) e.oj = vort ? __ldg(omega + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if constexpr ((kTerms & 2u) != 0u) e.vj = visc ? __ldg(v + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+        return e;
+    }
+    __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, const Extra& ex, bool) const {
         Contrib c = zero();
-        if (vort) {
-            const float4 oj = __ldg(omega + j);
+        if constexpr ((kTerms & 1u) != 0u) if (vort) {
+            const float4 oj = ex.oj;
             const float dx = oj.x - oi.x, dy = oj.y - oi.y, dz = oj.z - oi.z;
             const float ol = sqrtf(dx * dx + dy * dy + dz * dz);
             c.gx = ol / ((pj.x - pi.x) + 0.00000001f);
@@ -780,13 +896,13 @@ struct VortViscVisit {
             c.gz = ol / ((pj.z - pi.z) + 0.00000001f);
             c.flags |= 1u;
         }
-        if (visc) {
+        if constexpr ((kTerms & 2u) != 0u) if (visc) {
             const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
             const float r2 = rx * rx + ry * ry + rz * rz;
             if (r2 >= P.hp2) return c;
             const float W = poly6(P, sqrtf(r2));
             if (W == 0.0f) return c;
-            const float4 vj = __ldg(v + j);
+            const float4 vj = ex.vj;
             c.sx = (vj.x - vi.x) * W; c.sy = (vj.y - vi.y) * W;
             c.sz = (vj.z - vi.z) * W; c.sw = (vj.w - vi.w) * W;
             c.flags |= 2u;
@@ -799,7 +915,10 @@ struct VortViscVisit {
     }
 };
 
-__device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i, const VortViscVisit& vis,
+using VortViscVisit = VortViscVisitT<3u>;
+
+template <class VV>
+__device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i, const VV& vis,
                                                  float4* __restrict__ vout, float4* __restrict__ fext,
                                                  const float* __restrict__ w) {
     if (vis.vort) {
@@ -856,17 +975,17 @@ vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* _
     const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const uint32_t nm = (do_vort && do_visc && Ln.list) ? Ln.meta[i] : kListOff;
     if (nm != kListOff) {
-        VortViscVisit vo(P, vin, omega, p[i], vin[i], oi, true, false);
-        walk_list(Lv, i, meta, p, vo);
-        VortViscVisit vs(P, vin, omega, p[i], vin[i], oi, false, true);
-        walk_list(Ln, i, nm, p, vs);
+        VortViscVisitT<1u> vo(P, vin, omega, p[i], vin[i], oi, true, false);
+        walk_list<false, 2>(Lv, i, meta, p, vo);   // position + omega per entry: batches of 2 fit the registers
+        VortViscVisitT<2u> vs(P, vin, omega, p[i], vin[i], oi, false, true);
+        walk_near(Ln, i, nm, p, vs);
         vo.sx = vs.sx; vo.sy = vs.sy; vo.sz = vs.sz; vo.sw = vs.sw;
         vo.visc = true;
         vort_visc_finish(P, i, vo, vout, fext, w);
         return;
     }
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
-    walk_list(Lv, i, meta, p, vis);
+    walk_list<false, 2>(Lv, i, meta, p, vis);
     vort_visc_finish(P, i, vis, vout, fext, w);
 }
 

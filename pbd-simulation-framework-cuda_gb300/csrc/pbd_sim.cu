@@ -250,6 +250,19 @@ static bool near_lists_on(const pbd_sim* s, const DevParams& P) {
     return !(s->prm.flags & PBD_FLAG_FULL_WALK) && P.far_pairs_zero != 0u;
 }
 
+// delta_list_kernel for `mode`: the fluid frame's two pass modes run specialised code.
+static void launch_delta_list(uint32_t gn, int tn, cudaStream_t st, const DevParams& P, uint32_t mode,
+                              const float4* pin, float4* pout, float4* x, float4* v, const float* lam,
+                              const float* w, float4* delta, const DeferList& D, const NbList& L) {
+    constexpr uint32_t kFluid = kDoDelta | kDoCollide | kDoApply;
+    if (mode == kFluid)
+        delta_list_kernel<kFluid><<<gn, tn, 0, st>>>(P, mode, pin, pout, x, v, lam, w, delta, D, L);
+    else if (mode == (kFluid | kDoUpdate))
+        delta_list_kernel<kFluid | kDoUpdate><<<gn, tn, 0, st>>>(P, mode, pin, pout, x, v, lam, w, delta, D, L);
+    else
+        delta_list_kernel<0><<<gn, tn, 0, st>>>(P, mode, pin, pout, x, v, lam, w, delta, D, L);
+}
+
 // Record (or run) one frame of Fluid::compute (Fluid.cu:14-97) on `st`.
 cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only, uint32_t& nl,
                           Profiler* prof = nullptr, const Tape* tape = nullptr) {
@@ -367,8 +380,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
                 PROF_BEGIN(by_list ? "delta_list" : "delta");
                 const int pout = next_p(cur.p);
                 if (by_list)
-                    delta_list_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
-                                                         s->delta, D, L);
+                    launch_delta_list(gn, tn, st, P, mode, s->p[cur.p], s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                      s->delta, D, L);
                 else
                     delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
                                                     s->delta, s->cell_start, s->cell_end, D);
@@ -430,8 +443,8 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             const int pout = next_p(cur.p);
             // the near lists hold this iteration's lambda walk (same positions) on pass 0 only
             if (by_list)
-                delta_list_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
-                                                     s->delta, D, L);
+                launch_delta_list(gn, tn, st, P, mode, s->p[cur.p], s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                  s->delta, D, L);
             else
                 delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
                                                 s->delta, s->cell_start, s->cell_end, D);

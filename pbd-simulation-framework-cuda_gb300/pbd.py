@@ -302,6 +302,14 @@ class Sim:
     def front(self, stream=0):
         check(self.L.pbd_debug_front(self.h, C.c_void_p(stream)))
 
+    def autotune(self, cache_path=None, stream=0):
+        """Threads per block of the neighbour passes (64, 128 or 256), timed on this simulation
+        (which advances frames) unless `cache_path` already holds this workload."""
+        b = C.c_uint32()
+        check(self.L.pbd_autotune(self.h, None if cache_path is None else os.fsencode(cache_path),
+                                  C.c_void_p(stream), C.byref(b)))
+        return b.value
+
     def profile(self, nsteps, stream=0):
         """{kernel name: (launches, total device ms)} over `nsteps` directly launched frames."""
         stats = (KernelStat * 32)()
