@@ -114,8 +114,18 @@ __device__ __forceinline__ float spiky_scale(const DevParams& P, float dist, flo
     return 0.0f;
 }
 
-// Integer power by repeated multiplication (the reference's pow(float, int)).
+// Integer power by repeated multiplication (the reference's pow(float, int)): r = 1, then
+// r *= x |n| times.  The usual exponents are spelled out with the same products in the same
+// order (1 * x = x exactly), without the loop.
 __device__ __forceinline__ float powi(float x, int n) {
+    switch (n) {
+        case 0: return 1.0f;
+        case 1: return x;
+        case 2: return x * x;
+        case 3: return (x * x) * x;
+        case 4: return ((x * x) * x) * x;
+        default: break;
+    }
     int m = n < 0 ? -n : n;
     float r = 1.0f;
     for (int k = 0; k < m; ++k) r *= x;

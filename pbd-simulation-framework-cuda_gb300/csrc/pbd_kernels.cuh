@@ -32,7 +32,7 @@ __global__ void __launch_bounds__(256)
 predict_key_kernel(DevParams P, float4* __restrict__ x, float4* __restrict__ v, float4* __restrict__ p,
                    const float4* __restrict__ fext, const float* __restrict__ w, uint32_t* keys, const uint32_t* old_keys,
                    const uint32_t* __restrict__ table_n, uint32_t* __restrict__ cell_start,
-                   uint32_t* __restrict__ hist, int npasses, uint32_t* __restrict__ err) {
+                   uint32_t* __restrict__ hist, int npasses, uint32_t* __restrict__ err, uint32_t* __restrict__ clear_word) {
     __shared__ uint32_t sh[kMaxPasses * kRadix];
     for (int b = threadIdx.x; b < kMaxPasses * kRadix; b += blockDim.x) sh[b] = 0u;
     __syncthreads();
@@ -40,6 +40,7 @@ predict_key_kernel(DevParams P, float4* __restrict__ x, float4* __restrict__ v, 
     const uint32_t old_n = *table_n;            // sorted keys whose cells the tables still hold
     const uint32_t total = N > old_n ? N : old_n;
     const bool forces = (P.active & PBD_ACTIVE_APPLY_FORCES) != 0;
+    if (clear_word && blockIdx.x == 0 && threadIdx.x == 0) *clear_word = 0u;   // a set the frame refills
     if (P.batched && blockIdx.x == 0)           // scene ranges are rebuilt by the re-order
         for (uint32_t k = threadIdx.x; k < 2 * P.nscenes; k += blockDim.x) P.scene_range[k] = 0u;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {

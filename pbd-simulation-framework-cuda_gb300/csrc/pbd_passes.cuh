@@ -420,6 +420,42 @@ __device__ __forceinline__ void for_each_deferred(const DeferList& D, F&& f) {
     }
 }
 
+// The leading `blocks` blocks of a list kernel walk a set of particles over the cells (one warp
+// per particle, walk_coop) while the other blocks walk the stored lists.  The particles without
+// a list are known before such a kernel starts (the frame's first lambda pass, or the pass
+// that recorded the near lists), so their long walks run beside the list walks instead of in a
+// kernel after them.  With `reset`, the last of these blocks empties the set for its producer.
+struct CoopSet {
+    const uint32_t* items;
+    uint32_t* count;
+    uint32_t* done;
+    uint32_t cap;
+    uint32_t blocks;
+    uint32_t reset;
+};
+template <class F>
+__device__ __forceinline__ void run_coop_set(const CoopSet& C, F&& f) {
+    const uint32_t n = min(*((volatile uint32_t*)C.count), C.cap);
+    const uint32_t wpb = blockDim.x >> 5;
+    const uint32_t warps = C.blocks * wpb;
+    for (uint32_t w = blockIdx.x * wpb + (threadIdx.x >> 5); w < n; w += warps) f(C.items[w]);
+    if (C.reset) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(C.done, 1u) == C.blocks - 1) {
+                *C.count = 0u;
+                *C.done = 0u;
+                __threadfence();
+            }
+        }
+    }
+}
+// Append i to a set when the set is given (items non-null).
+__device__ __forceinline__ void note_particle(const DeferList& D, uint32_t i) {
+    if (D.items) defer_particle(D, i);
+}
+
 // ======================================================================================
 // computeLambda (Density.h:48-93)
 // ======================================================================================
@@ -469,9 +505,10 @@ struct LambdaVisit {
 __global__ void __launch_bounds__(256)
 lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
               const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D, float4* __restrict__ aux,
-              NbList L, NbList F) {
-    // walks the cells; L.list: record the near lists for the delta pass that follows;
-    // F.list: store the full lists (the frame's first lambda pass)
+              NbList L, NbList F, DeferList DF, DeferList DN) {
+    // walks the cells; L.list: record the near lists for the delta pass that follows (the
+    // particles left without one noted in DN); F.list: store the full lists (the frame's first
+    // lambda pass; the particles left without one noted in DF)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
@@ -485,8 +522,12 @@ lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restric
         walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
         const uint32_t fm = deferred ? kListOff : rec.meta();
         F.meta[i] = fm;
+        if (fm == kListOff) note_particle(DF, i);
         const uint32_t lm = (L.list && fm != kListOff) ? filter_list<true>(F, fm, L, i, pi, P.cut2, p) : kListOff;
-        if (L.list) L.meta[i] = lm;
+        if (L.list) {
+            L.meta[i] = lm;
+            if (lm == kListOff) note_particle(DN, i);
+        }
         if (!deferred) {
             if (lm != kListOff) walk_near<true>(L, i, lm, p, vis);
             else if (fm != kListOff) walk_list<true>(F, i, fm, p, vis);
@@ -501,6 +542,7 @@ lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restric
         walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
         const uint32_t lm = deferred ? kListOff : rec.meta();
         L.meta[i] = lm;
+        if (lm == kListOff) note_particle(DN, i);
         if (!deferred) {
             if (lm != kListOff) walk_near<true>(L, i, lm, p, vis);
             else walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
@@ -520,40 +562,55 @@ lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restric
     if (aux) vis.store_aux(aux, P.N, i);
 }
 
+// One warp computes lambda_i over the cells.
+__device__ __noinline__ void coop_lambda(const DevParams& P, const float4* __restrict__ p, const float4* __restrict__ pa,
+                                            const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                                            float* __restrict__ lambda, float4* __restrict__ aux, uint32_t i) {
+    const SceneCtx S = scene_ctx(P, i);
+    LambdaVisit vis(P, p[i]);
+    walk_coop(P, S, i, pa[i], p, cs, ce, vis);
+    if (lane_id() == 0) {
+        lambda[i] = vis.finish(S.rho0);
+        if (aux) vis.store_aux(aux, P.N, i);
+    }
+}
+
 __global__ void __launch_bounds__(128)
 lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
                    const uint32_t* __restrict__ ce, float* __restrict__ lambda, DeferList D, float4* __restrict__ aux) {
-    for_each_deferred(D, [&](uint32_t i) {
-        const SceneCtx S = scene_ctx(P, i);
-        LambdaVisit vis(P, p[i]);
-        walk_coop(P, S, i, pa[i], p, cs, ce, vis);
-        if (lane_id() == 0) {
-            lambda[i] = vis.finish(S.rho0);
-            if (aux) vis.store_aux(aux, P.N, i);
-        }
-    });
+    for_each_deferred(D, [&](uint32_t i) { coop_lambda(P, p, pa, cs, ce, lambda, aux, i); });
 }
 
 // The frame's later lambda passes: read the full list (no cell tables), record the near list.
-// A particle without a stored list is handed to lambda_coop_kernel (the deferral list holds
-// every particle, so the hand-off cannot fail).  Kept apart from lambda_kernel so that its
-// register budget is the list walk's alone.
+// The particles without a full list (the set C) are walked by the leading blocks; the ones left
+// without a near list are noted in DN for the delta pass.  Kept apart from lambda_kernel so that
+// its register budget is the list walk's alone.
 __global__ void __launch_bounds__(256, 5)
-lambda_list_kernel(DevParams P, const float4* __restrict__ p, float* __restrict__ lambda, DeferList D,
-                   float4* __restrict__ aux, NbList L, NbList F) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+lambda_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
+                   const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float* __restrict__ lambda,
+                   CoopSet C, DeferList DN, float4* __restrict__ aux, NbList L, NbList F) {
+    if (blockIdx.x < C.blocks) {
+        run_coop_set(C, [&](uint32_t i) { coop_lambda(P, p, pa, cs, ce, lambda, aux, i); });
+        return;
+    }
+    const uint32_t i = (blockIdx.x - C.blocks) * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const uint32_t fm = F.meta[i];
     if (fm == kListOff) {
-        if (L.list) L.meta[i] = kListOff;
-        defer_particle(D, i);
+        if (L.list) {
+            L.meta[i] = kListOff;
+            note_particle(DN, i);
+        }
         return;
     }
     const SceneCtx S = scene_ctx(P, i);
     const float4 pi = p[i];
     LambdaVisit vis(P, pi);
     const uint32_t lm = L.list ? filter_list(F, fm, L, i, pi, P.cut2, p) : kListOff;
-    if (L.list) L.meta[i] = lm;
+    if (L.list) {
+        L.meta[i] = lm;
+        if (lm == kListOff) note_particle(DN, i);
+    }
     if (lm != kListOff) walk_near<true>(L, i, lm, p, vis);
     else walk_list(F, i, fm, p, vis);
     lambda[i] = vis.finish(S.rho0);
@@ -693,22 +750,40 @@ delta_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, const f
     delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
 }
 
-// delta pass 0 of an iteration over the near lists its lambda pass recorded; particles
-// without one go to delta_coop_kernel.  kMode != 0: the pass mode fixed at compile time (the
-// two passes of a fluid frame), kMode = 0: `mode` at run time.
+// One warp runs the delta pass for particle i over the cells.
+__device__ __noinline__ void coop_delta(const DevParams& P, uint32_t mode, const float4* __restrict__ pin,
+                                           const float4* __restrict__ pa, float4* __restrict__ pout, float4* __restrict__ x,
+                                           float4* __restrict__ v, const float* __restrict__ lambda, const float* __restrict__ w,
+                                           float4* __restrict__ delta, const uint32_t* __restrict__ cs,
+                                           const uint32_t* __restrict__ ce, uint32_t i) {
+    const float4 pi = pin[i];
+    const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
+    const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
+    const SceneCtx S = scene_ctx(P, i);
+    DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
+    walk_coop(P, S, i, pa[i], pin, cs, ce, vis);
+    if (lane_id() == 0) delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
+}
+
+// delta pass 0 of an iteration over the near lists its lambda pass recorded; the particles
+// without one (the set C, which the leading blocks empty) walk the cells.  kMode != 0: the pass
+// mode fixed at compile time (the two passes of a fluid frame), kMode = 0: `mode` at run time.
 template <uint32_t kMode>
-__global__ void __launch_bounds__(256)
-delta_list_kernel(DevParams P, uint32_t mode_rt, const float4* __restrict__ pin, float4* __restrict__ pout,
-                  float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda,
-                  const float* __restrict__ w, float4* __restrict__ delta, DeferList D, NbList L) {
+__global__ void __launch_bounds__(256, 5)
+delta_list_kernel(DevParams P, uint32_t mode_rt, const float4* __restrict__ pin, const float4* __restrict__ pa,
+                  float4* __restrict__ pout, float4* __restrict__ x, float4* __restrict__ v,
+                  const float* __restrict__ lambda, const float* __restrict__ w, float4* __restrict__ delta,
+                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, CoopSet C, NbList L) {
     const uint32_t mode = kMode ? kMode : mode_rt;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.N) return;
-    const uint32_t meta = L.meta[i];
-    if (meta == kListOff) {
-        defer_particle(D, i);
+    if (blockIdx.x < C.blocks) {
+        run_coop_set(C, [&](uint32_t i) { coop_delta(P, mode, pin, pa, pout, x, v, lambda, w, delta, cs, ce, i); });
         return;
     }
+    const uint32_t i = (blockIdx.x - C.blocks) * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const uint32_t meta = L.meta[i];
+    if (meta == kListOff) return;
     const float4 pi = pin[i];
     const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
     const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -724,16 +799,7 @@ delta_coop_kernel(DevParams P, uint32_t mode, const float4* __restrict__ pin, co
                   float4* __restrict__ x, float4* __restrict__ v, const float* __restrict__ lambda, const float* __restrict__ w,
                   float4* __restrict__ delta, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
                   DeferList D) {
-    for_each_deferred(D, [&](uint32_t i) {
-        const float4 pi = pin[i];
-        const bool need_x = (mode & (kDoCollide | kDoUpdate)) != 0;
-        const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
-        const SceneCtx S = scene_ctx(P, i);
-        DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
-        walk_coop(P, S, i, pa[i], pin, cs, ce, vis);
-        if (lane_id() == 0) delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
-    });
+    for_each_deferred(D, [&](uint32_t i) { coop_delta(P, mode, pin, pa, pout, x, v, lambda, w, delta, cs, ce, i); });
 }
 
 // updatePositions on its own (Update.h:11-32), when no delta pass can carry it.
@@ -786,11 +852,12 @@ struct OmegaVisit {
 __global__ void __launch_bounds__(256)
 omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ v,
              const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega, DeferList D,
-             NbList L) {
+             NbList L, DeferList DN) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
-    // walks the cells; L.list: record the near lists for a viscosity pass without vorticity
+    // walks the cells; L.list: record the near lists for a viscosity pass without vorticity (the
+    // particles left without one noted in DN when DN is given)
     const float4 pi = p[i];
     OmegaVisit vis(P, v, pi, v[i]);
     bool deferred = false;
@@ -798,6 +865,7 @@ omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict
         Recorder<OmegaVisit> rec(vis, L, L, false, i, pi, P.cut2);
         walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
         L.meta[i] = deferred ? kListOff : rec.meta();
+        if (L.meta[i] == kListOff) note_particle(DN, i);
         if (!deferred) {
             omega[i] = make_float4(rec.inner.ox, rec.inner.oy, rec.inner.oz, 0.f);
             return;
@@ -813,23 +881,44 @@ omega_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict
     omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
 }
 
-// omega over the full list (recording the near list when L.list); particles without one go to
-// omega_coop_kernel.
+// One warp computes omega_i over the cells.
+__device__ __noinline__ void coop_omega(const DevParams& P, const float4* __restrict__ p, const float4* __restrict__ pa,
+                                           const float4* __restrict__ v, const uint32_t* __restrict__ cs,
+                                           const uint32_t* __restrict__ ce, float4* __restrict__ omega, uint32_t i) {
+    const SceneCtx S = scene_ctx(P, i);
+    OmegaVisit vis(P, v, p[i], v[i]);
+    walk_coop(P, S, i, pa[i], p, cs, ce, vis);
+    if (lane_id() == 0) omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
+}
+
+// omega over the full list (recording the near list when L.list, and noting the particles left
+// without one in DN when DN is given); the particles without a full list (the set C) are walked
+// by the leading blocks.
 __global__ void __launch_bounds__(256, 5)
-omega_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ v, float4* __restrict__ omega,
-                  DeferList D, NbList L, NbList F) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+omega_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ v,
+                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega,
+                  CoopSet C, DeferList DN, NbList L, NbList F) {
+    if (blockIdx.x < C.blocks) {
+        run_coop_set(C, [&](uint32_t i) { coop_omega(P, p, pa, v, cs, ce, omega, i); });
+        return;
+    }
+    const uint32_t i = (blockIdx.x - C.blocks) * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const uint32_t fm = F.meta[i];
     if (fm == kListOff) {
-        if (L.list) L.meta[i] = kListOff;
-        defer_particle(D, i);
+        if (L.list) {
+            L.meta[i] = kListOff;
+            note_particle(DN, i);
+        }
         return;
     }
     const float4 pi = p[i];
     OmegaVisit vis(P, v, pi, v[i]);
     const uint32_t lm = L.list ? filter_list(F, fm, L, i, pi, P.cut2, p) : kListOff;
-    if (L.list) L.meta[i] = lm;
+    if (L.list) {
+        L.meta[i] = lm;
+        if (lm == kListOff) note_particle(DN, i);
+    }
     if (lm != kListOff) walk_near<true>(L, i, lm, p, vis);
     else walk_list<false, 2>(F, i, fm, p, vis);
     omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
@@ -839,12 +928,7 @@ __global__ void __launch_bounds__(128)
 omega_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ v,
                   const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega,
                   DeferList D) {
-    for_each_deferred(D, [&](uint32_t i) {
-        const SceneCtx S = scene_ctx(P, i);
-        OmegaVisit vis(P, v, p[i], v[i]);
-        walk_coop(P, S, i, pa[i], p, cs, ce, vis);
-        if (lane_id() == 0) omega[i] = make_float4(vis.ox, vis.oy, vis.oz, 0.f);
-    });
+    for_each_deferred(D, [&](uint32_t i) { coop_omega(P, p, pa, v, cs, ce, omega, i); });
 }
 
 // ======================================================================================
@@ -957,21 +1041,37 @@ vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
     vort_visc_finish(P, i, vis, vout, fext, w);
 }
 
+// One warp runs vorticity + viscosity for particle i over the cells.
+__device__ __noinline__ void coop_vort_visc(const DevParams& P, const float4* __restrict__ p, const float4* __restrict__ pa,
+                                               const float4* __restrict__ vin, float4* __restrict__ vout,
+                                               const float4* __restrict__ omega, float4* __restrict__ fext,
+                                               const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                                               int do_vort, int do_visc, const float* __restrict__ w, uint32_t i) {
+    const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const SceneCtx S = scene_ctx(P, i);
+    VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
+    walk_coop(P, S, i, pa[i], p, cs, ce, vis);
+    if (lane_id() == 0) vort_visc_finish(P, i, vis, vout, fext, w);
+}
+
 // vorticity + viscosity over a stored list (the full list with vorticity, else the omega pass's
-// near list); particles without one go to vort_visc_coop_kernel.  With both terms and the omega
-// pass's near list Ln at hand, vorticity runs over the full list and viscosity over the near list
-// (its entries beyond the cut add exact zeros): the two sums keep their own order.
+// near list); the particles without one (the set C) are walked by the leading blocks.  With both
+// terms and the omega pass's near list Ln at hand, vorticity runs over the full list and
+// viscosity over the near list (its entries beyond the cut add exact zeros): the two sums keep
+// their own order.
 __global__ void __launch_bounds__(256, 5)
-vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ vin,
-                      float4* __restrict__ vout, const float4* __restrict__ omega, float4* __restrict__ fext,
-                      int do_vort, int do_visc, const float* __restrict__ w, DeferList D, NbList Lv, NbList Ln) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.N) return;
-    const uint32_t meta = Lv.meta[i];
-    if (meta == kListOff) {
-        defer_particle(D, i);
+vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
+                      const float4* __restrict__ vin, float4* __restrict__ vout, const float4* __restrict__ omega,
+                      float4* __restrict__ fext, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                      int do_vort, int do_visc, const float* __restrict__ w, CoopSet C, NbList Lv, NbList Ln) {
+    if (blockIdx.x < C.blocks) {
+        run_coop_set(C, [&](uint32_t i) { coop_vort_visc(P, p, pa, vin, vout, omega, fext, cs, ce, do_vort, do_visc, w, i); });
         return;
     }
+    const uint32_t i = (blockIdx.x - C.blocks) * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const uint32_t meta = Lv.meta[i];
+    if (meta == kListOff) return;
     const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const uint32_t nm = (do_vort && do_visc && Ln.list) ? Ln.meta[i] : kListOff;
     if (nm != kListOff) {
@@ -995,11 +1095,7 @@ vort_visc_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* _
                       const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
                       const float* __restrict__ w, DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
-        const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const SceneCtx S = scene_ctx(P, i);
-        VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
-        walk_coop(P, S, i, pa[i], p, cs, ce, vis);
-        if (lane_id() == 0) vort_visc_finish(P, i, vis, vout, fext, w);
+        coop_vort_visc(P, p, pa, vin, vout, omega, fext, cs, ce, do_vort, do_visc, w, i);
     });
 }
 

@@ -48,6 +48,7 @@ constexpr uint32_t kFullMax = 128;   // full list: every entry of the frame's li
 constexpr int kThreadsParticle = 256;
 constexpr int kThreadsNeighbourDefault = 128;
 constexpr int kThreadsCoop = 128;         // 4 warps, one deferred particle per warp
+constexpr uint32_t kCoopBlocks = 16;      // leading blocks of a list pass that walk its particles without a list
 
 inline uint32_t div_up(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
 
@@ -124,6 +125,10 @@ struct pbd_sim {
     uint32_t *fl_list = nullptr, *fl_meta = nullptr;   // full lists (recorded by the frame's first lambda)
     uint32_t *defer_items = nullptr, *defer_count = nullptr, *defer_done = nullptr;
     uint32_t defer_cap = 0;
+    // particles without a stored list, walked by the leading blocks of the list passes:
+    // DF = no full list (noted by the frame's first lambda pass), DN = no near list (noted by
+    // the pass that records the near lists, emptied by the pass that reads them)
+    uint32_t *dfr_items = nullptr, *dfr_count = nullptr, *dnr_items = nullptr, *dnr_count = nullptr;
     Cur cur;
     int table_passes = -1;        // passes of the sort whose keys the cell tables hold (-1: none)
     uint32_t table_hint = 0;      // host upper bound of the device word table_n
@@ -252,15 +257,17 @@ static bool near_lists_on(const pbd_sim* s, const DevParams& P) {
 
 // delta_list_kernel for `mode`: the fluid frame's two pass modes run specialised code.
 static void launch_delta_list(uint32_t gn, int tn, cudaStream_t st, const DevParams& P, uint32_t mode,
-                              const float4* pin, float4* pout, float4* x, float4* v, const float* lam,
-                              const float* w, float4* delta, const DeferList& D, const NbList& L) {
+                              const float4* pin, const float4* pa, float4* pout, float4* x, float4* v, const float* lam,
+                              const float* w, float4* delta, const uint32_t* cs, const uint32_t* ce, const CoopSet& C,
+                              const NbList& L) {
     constexpr uint32_t kFluid = kDoDelta | kDoCollide | kDoApply;
+    const uint32_t g = gn + C.blocks;
     if (mode == kFluid)
-        delta_list_kernel<kFluid><<<gn, tn, 0, st>>>(P, mode, pin, pout, x, v, lam, w, delta, D, L);
+        delta_list_kernel<kFluid><<<g, tn, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, L);
     else if (mode == (kFluid | kDoUpdate))
-        delta_list_kernel<kFluid | kDoUpdate><<<gn, tn, 0, st>>>(P, mode, pin, pout, x, v, lam, w, delta, D, L);
+        delta_list_kernel<kFluid | kDoUpdate><<<g, tn, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, L);
     else
-        delta_list_kernel<0><<<gn, tn, 0, st>>>(P, mode, pin, pout, x, v, lam, w, delta, D, L);
+        delta_list_kernel<0><<<g, tn, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, L);
 }
 
 // Record (or run) one frame of Fluid::compute (Fluid.cu:14-97) on `st`.
@@ -285,7 +292,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const float* wcur = s->mass_used ? s->w[cur.x] : nullptr;
     predict_key_kernel<<<gpred, kThreadsParticle, 0, st>>>(P, s->x[cur.x], s->v[cur.v], s->p[cur.p], s->fext, wcur,
                                                            s->keys[0], s->keys[np % 2], s->table_n, s->cell_start,
-                                                           s->hist, np, s->err);
+                                                           s->hist, np, s->err, s->dfr_count);
     PROF_END();
     ++nl;
     // sortIds
@@ -326,6 +333,13 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const uint32_t gn = div_up(N, tn);
     const DeferList D{s->defer_items, s->defer_count, s->defer_done, s->defer_cap};
     const uint32_t gc = (uint32_t)s->num_sms * 2u;   // cooperative kernels: grid-stride over the deferred
+    // the list passes' own cooperative blocks: DF is read by every full-list pass of the frame,
+    // DN emptied by the pass that reads it
+    const DeferList DF{s->dfr_items, s->dfr_count, s->dfr_count + 1, s->defer_cap};
+    const DeferList DN{s->dnr_items, s->dnr_count, s->dnr_count + 1, s->defer_cap};
+    const DeferList DX{nullptr, nullptr, nullptr, 0u};
+    const CoopSet CF{s->dfr_items, s->dfr_count, s->dfr_count + 1, s->defer_cap, kCoopBlocks, 0u};
+    const CoopSet CN{s->dnr_items, s->dnr_count, s->dnr_count + 1, s->defer_cap, kCoopBlocks, 1u};
     const uint32_t act = prm.active;
     const uint32_t I = prm.solver_iterations, Sx = prm.stabilization_iterations;
     // near lists: recorded by a walking pass for the pass after it at the same positions; they
@@ -360,14 +374,17 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
             PROF_BEGIN((use_full && it > 0) ? "lambda_list" : "lambda");
             const NbList Lr = (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS) ? L : L0;
-            if (use_full && it > 0)
-                lambda_list_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], lam, D, aux, Lr, F);
-            else
+            if (use_full && it > 0) {
+                lambda_list_kernel<<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam,
+                                                                    CF, Lr.list ? DN : DX, aux, Lr, F);
+                nl += 1;
+            } else {
                 lambda_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux, Lr,
-                                                 use_full ? F : L0);
-            lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux);
+                                                 use_full ? F : L0, use_full ? DF : DX, Lr.list ? DN : DX);
+                lambda_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, D, aux);
+                nl += 2;
+            }
             PROF_END();
-            nl += 2;
             last_was_delta = false;
         }
         if (batched_contacts) {
@@ -379,16 +396,18 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
                 const bool by_list = recorded && use_lists;
                 PROF_BEGIN(by_list ? "delta_list" : "delta");
                 const int pout = next_p(cur.p);
-                if (by_list)
-                    launch_delta_list(gn, tn, st, P, mode, s->p[cur.p], s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
-                                      s->delta, D, L);
-                else
+                if (by_list) {
+                    launch_delta_list(gn, tn, st, P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                      s->delta, s->cell_start, s->cell_end, CN, L);
+                    nl += 1;
+                } else {
                     delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
                                                     s->delta, s->cell_start, s->cell_end, D);
-                delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
-                                                               s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
+                    delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
+                                                                   s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
+                    nl += 2;
+                }
                 PROF_END();
-                nl += 2;
                 cur.p = pout;
             }
             const ContactStore& C = s->ct;
@@ -442,16 +461,18 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             PROF_BEGIN(by_list ? "delta_list" : "delta");
             const int pout = next_p(cur.p);
             // the near lists hold this iteration's lambda walk (same positions) on pass 0 only
-            if (by_list)
-                launch_delta_list(gn, tn, st, P, mode, s->p[cur.p], s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
-                                  s->delta, D, L);
-            else
+            if (by_list) {
+                launch_delta_list(gn, tn, st, P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                  s->delta, s->cell_start, s->cell_end, CN, L);
+                nl += 1;
+            } else {
                 delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
                                                 s->delta, s->cell_start, s->cell_end, D);
-            delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
-                                                           s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
+                delta_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x],
+                                                               s->v[cur.v], lam, wf, s->delta, s->cell_start, s->cell_end, D);
+                nl += 2;
+            }
             PROF_END();
-            nl += 2;
             cur.p = pout;
             last_was_delta = (mode & kDoUpdate) != 0;
         }
@@ -462,34 +483,43 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         PROF_END();
         ++nl;
     }
+    const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
         PROF_BEGIN(use_full ? "omega_list" : "omega");
-        // near lists for viscosity (over the full list, omega filters them out before its sums)
-        const NbList Lo = (use_full || !(act & PBD_ACTIVE_COMPUTE_VORTICITY)) ? L : L0;
-        if (use_full)
-            omega_list_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->omega, D, Lo, F);
-        else
-            omega_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D, Lo);
-        omega_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
+        // near lists for viscosity: read by viscosity alone, or beside the full list for vorticity
+        // (omega filters them out of the full list before its sums)
+        const NbList Lo = ((vort || visc) && (use_full || !vort)) ? L : L0;
+        // viscosity alone walks them: the particles left without one go to its cooperative blocks
+        const DeferList DNo = (Lo.list && !vort) ? DN : DX;
+        if (use_full) {
+            omega_list_kernel<<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end,
+                                                               s->omega, CF, DNo, Lo, F);
+            nl += 1;
+        } else {
+            omega_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D, Lo, DNo);
+            omega_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end, s->omega, D);
+            nl += 2;
+        }
         PROF_END();
-        nl += 2;
     }
-    const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     if (vort || visc) {
         // vorticity sums every list entry: the full list; viscosity alone: the omega pass's near list
         const NbList Lv = vort ? F : ((act & PBD_ACTIVE_COMPUTE_OMEGAS) ? L : L0);
         const NbList Ln = (vort && use_full && (act & PBD_ACTIVE_COMPUTE_OMEGAS)) ? L : L0;
         PROF_BEGIN(Lv.list ? "vort_visc_list" : "vort_visc");
-        if (Lv.list)
-            vort_visc_list_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], s->v[cur.v], s->v[cur.v ^ 1], s->omega, s->fext,
-                                                     vort, visc, wf, D, Lv, Ln);
-        else
+        if (Lv.list) {
+            vort_visc_list_kernel<<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
+                                                                   s->fext, s->cell_start, s->cell_end, vort, visc, wf,
+                                                                   vort ? CF : CN, Lv, Ln);
+            nl += 1;
+        } else {
             vort_visc_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega, s->fext,
                                                 s->cell_start, s->cell_end, vort, visc, wf, D);
-        vort_visc_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
-                                                           s->fext, s->cell_start, s->cell_end, vort, visc, wf, D);
+            vort_visc_coop_kernel<<<gc, kThreadsCoop, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
+                                                               s->fext, s->cell_start, s->cell_end, vort, visc, wf, D);
+            nl += 2;
+        }
         PROF_END();
-        nl += 2;
         if (visc) cur.v ^= 1;
     }
     return cudaGetLastError();
@@ -651,6 +681,8 @@ int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<Scene
     s->defer_cap = capacity;   // every particle can be handed to the cooperative kernels
     parts.push_back({(void**)&s->defer_items, (size_t)s->defer_cap * 4});
     parts.push_back({(void**)&s->defer_count, 4}); parts.push_back({(void**)&s->defer_done, 4});
+    parts.push_back({(void**)&s->dfr_items, (size_t)s->defer_cap * 4}); parts.push_back({(void**)&s->dfr_count, 8});
+    parts.push_back({(void**)&s->dnr_items, (size_t)s->defer_cap * 4}); parts.push_back({(void**)&s->dnr_count, 8});
     parts.push_back({(void**)&s->nb_list, (size_t)kListMax * C * 4}); parts.push_back({(void**)&s->nb_meta, C * 4});
     parts.push_back({(void**)&s->fl_list, (size_t)kFullMax * C * 4}); parts.push_back({(void**)&s->fl_meta, C * 4});
     if (s->batched) {
