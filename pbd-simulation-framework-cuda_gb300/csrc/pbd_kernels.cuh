@@ -5,8 +5,9 @@
 //                                                  -> predict_key_kernel
 //   sortIds (CUB SortPairs)                        -> onesweep_pass x P   (pbd_sort.cuh)
 //   copy + reorder + resetCellInfo + computeCellInfo -> reorder_cells_kernel
-//   findContacts / findNeighbours                  -> no stored list: every neighbour pass
-//                                                     re-walks the cells in the list's order
+//   findContacts / findNeighbours                  -> the frame's first lambda pass walks the
+//                                                     cells in the list's order and stores the
+//                                                     full list; later passes read it
 //   computeLambda, computeDeltaPositions + solveCollisions + applyDeltaPositions
 //   (+ updatePositions), computeOmega, computeVorticity + computeViscosity
 //                                                  -> pbd_passes.cuh
