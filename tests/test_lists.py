@@ -97,3 +97,22 @@ def test_lists_in_batches(need_gpu, pbd, scenes):
         b.close()
     for s1, s2 in zip(*out):
         assert np.array_equal(s1["x"], s2["x"]) and np.array_equal(s1["v"], s2["v"])
+
+
+@pytest.mark.parametrize("vort,visc", [(0.0, 0.0), (0.0005, 0.01), (0.0, 0.01)])
+def test_lists_dense_blob_without_lists(need_gpu, pbd, scenes, vort, visc):
+    """a blob at spacing 0.35 inside a lattice at spacing 1: the blob's particles have more than
+    128 entries (no full list) and up to ~100 within the cut (no near list), so every pass hands
+    them to its cooperative blocks through the noted sets; the rest walk stored lists"""
+    params = scenes.workload_params(pbd, 32, 1000.0, vorticity=vort, viscosity=visc)
+    params.lambda_epsilon = 0.1
+    params.flags |= pbd.FLAG_TRACK_IDS
+    params.flags &= ~pbd.FLAG_CELL_END_QUIRK
+    pos, vel = scenes.lattice(16, 12, 16, spacing=1.0, seed=6)
+    lo, sp = np.array([8.0, 6.0, 8.0]), 0.35
+    blob, bv = scenes.lattice(9, 9, 9, origin=tuple(lo), spacing=sp, jitter=0.02, seed=7)
+    inside = np.all((pos[:, :3] > lo - 0.5) & (pos[:, :3] < lo + 8 * sp + 0.5), axis=1)
+    pos = np.concatenate([pos[~inside], blob]); vel = np.concatenate([vel[~inside], bv])
+    a = _run(pbd, params, pos, vel, 8)
+    b = _run(pbd, params, pos, vel, 8, full_walk=True)
+    _same(a, b)
