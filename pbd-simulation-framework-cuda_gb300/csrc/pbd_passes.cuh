@@ -381,6 +381,61 @@ struct ListRecorder {
     }
 };
 
+
+// The frame's full list of particle i for a 27-cell neighbourhood (kernelWidthNeighbours 1,
+// findContacts on), indices only: the entries, order, cap M, self-skip and long-range hand-over
+// of walk_seq over for_each_range, with the three cells of a column stored by one loop.
+// Returns the list's meta (kListOff when it does not fit or the particle is handed over; then
+// *deferred tells which).
+__device__ __forceinline__ uint32_t store_full_list(const DevParams& P, const SceneCtx& S, uint32_t i, float4 pa,
+                                                    const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                                                    const NbList& F, bool* deferred) {
+    const uint32_t N = P.N, M = P.M;
+    if (M == 0) return 0u;
+    const bool quirk = (P.flags & PBD_FLAG_CELL_END_QUIRK) && S.n >= 2;
+    uint32_t mx[3], my[3], mz[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        mx[c] = morton_axis(__fmaf_rn((float)(c - 1), P.d, pa.x)) << 2;
+        my[c] = morton_axis(__fmaf_rn((float)(c - 1), P.d, pa.y)) << 1;
+        mz[c] = morton_axis(__fmaf_rn((float)(c - 1), P.d, pa.z));
+    }
+    uint32_t* out = F.list + i;
+    uint32_t n = 0;
+#pragma unroll 1
+    for (int col = 0; col < 9; ++col) {
+        const int a = col / 3, b = col - 3 * (col / 3);
+        const uint32_t hxy = (a == 0 ? mx[0] : (a == 1 ? mx[1] : mx[2])) + (b == 0 ? my[0] : (b == 1 ? my[1] : my[2]));
+        uint32_t h[3], s3[3], e3[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            h[c] = hxy + mz[c];
+            s3[c] = h[c] < P.G ? __ldg(cs + S.base + h[c]) : kEmptyCell;
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) e3[c] = h[c] < P.G ? __ldg(ce + S.base + h[c]) : 0u;
+        uint32_t len[3];
+        uint32_t reach = n;   // entries stored before the cell: the walk reaches it while below the cap
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const bool valid = s3[c] < N;
+            const uint32_t e = ((quirk && h[c] == S.n - 1) || e3[c] > S.end) ? S.end : e3[c];
+            len[c] = valid ? e - s3[c] : 0u;
+            if (valid && reach < M && len[c] > kLongRange) { *deferred = true; return kListOff; }
+            reach += len[c] - ((valid && s3[c] <= i && i < e) ? 1u : 0u);
+        }
+        const uint32_t l01 = len[0] + len[1], T = l01 + len[2];
+#pragma unroll 1
+        for (uint32_t t = 0; t < T; ++t) {
+            const uint32_t j = t < len[0] ? s3[0] + t : (t < l01 ? s3[1] + (t - len[0]) : s3[2] + (t - l01));
+            if (j == i) continue;
+            if (n < F.kmax) out[(size_t)n * F.stride] = j;
+            if (++n == M) return n > F.kmax ? kListOff : (n | (n << 8));
+        }
+    }
+    return n > F.kmax ? kListOff : (n | (n << 8));
+}
+
 // A visitor that sums nothing: a walk with Recorder<NullVisit> only stores the lists.
 struct NullVisit {
     struct Contrib {};
@@ -518,9 +573,14 @@ lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restric
     if (F.list) {
         // the walk stores the full list (indices only), the filter the near list; the sums then
         // run over the shortest list that fits
-        ListRecorder rec(F, i);
-        walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
-        const uint32_t fm = deferred ? kListOff : rec.meta();
+        uint32_t fm;
+        if (P.K <= 1 && (P.active & PBD_ACTIVE_FIND_CONTACTS)) {
+            fm = store_full_list(P, S, i, pa[i], cs, ce, F, &deferred);
+        } else {
+            ListRecorder rec(F, i);
+            walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
+            fm = deferred ? kListOff : rec.meta();
+        }
         F.meta[i] = fm;
         if (fm == kListOff) note_particle(DF, i);
         const uint32_t lm = (L.list && fm != kListOff) ? filter_list<true>(F, fm, L, i, pi, P.cut2, p) : kListOff;

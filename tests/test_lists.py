@@ -116,3 +116,16 @@ def test_lists_dense_blob_without_lists(need_gpu, pbd, scenes, vort, visc):
     a = _run(pbd, params, pos, vel, 8)
     b = _run(pbd, params, pos, vel, 8, full_walk=True)
     _same(a, b)
+
+
+@pytest.mark.parametrize("cap", [20, 40])
+def test_lists_with_a_small_cap(need_gpu, pbd, scenes, cap):
+    """maxNeighboursPerParticle below the ~32 candidates of the 27 cells: every stored list is
+    cut at the cap in the cells' order, as the walk cuts it"""
+    params = scenes.workload_params(pbd, 32, 1000.0, vorticity=0.0005, viscosity=0.01, max_neighbours=cap)
+    params.lambda_epsilon = 0.1
+    params.flags |= pbd.FLAG_TRACK_IDS
+    pos, vel = scenes.lattice(20, 16, 20, spacing=0.9, seed=8)
+    a = _run(pbd, params, pos, vel, 12)
+    b = _run(pbd, params, pos, vel, 12, full_walk=True)
+    _same(a, b)
