@@ -645,7 +645,7 @@ lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __re
 // The particles without a full list (the set C) are walked by the leading blocks; the ones left
 // without a near list are noted in DN for the delta pass.  Kept apart from lambda_kernel so that
 // its register budget is the list walk's alone.
-__global__ void __launch_bounds__(256, 5)
+__global__ void __launch_bounds__(256, 6)
 lambda_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
                    const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float* __restrict__ lambda,
                    CoopSet C, DeferList DN, float4* __restrict__ aux, NbList L, NbList F) {
@@ -954,7 +954,7 @@ __device__ __noinline__ void coop_omega(const DevParams& P, const float4* __rest
 // omega over the full list (recording the near list when L.list, and noting the particles left
 // without one in DN when DN is given); the particles without a full list (the set C) are walked
 // by the leading blocks.
-__global__ void __launch_bounds__(256, 5)
+__global__ void __launch_bounds__(256, 6)
 omega_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ v,
                   const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega,
                   CoopSet C, DeferList DN, NbList L, NbList F) {
