@@ -310,7 +310,7 @@ int pbd_adjoint_backward(pbd_sim* sim, const float* dL_dx_final, float* dL_dv0, 
  * buffers: d_keys_out receives the keys in ascending order and d_perm_out the input index of
  * each output key (a stable sort, so equal keys keep their input order).  Only the low
  * `key_bits` bits (1..32) are sorted.  d_keys_out and d_perm_out must not overlap d_keys_in.
- * Limit: n <= 1,048,576 keys (the fixed array is about 10 MiB and stays on every GPU that loads
+ * Limit: n <= 1,048,576 keys (the fixed array is about 9 MiB and stays on every GPU that loads
  * the library until the process exits); larger n returns PBD_ERR_CAPACITY.  The first call on
  * each device looks up the array's device address (make it before any stream capture).  All
  * calls share the array: calls whose GPU work overlaps race and must be serialised by the
