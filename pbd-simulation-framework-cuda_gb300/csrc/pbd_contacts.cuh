@@ -111,7 +111,7 @@ contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, 
         uint32_t j[4];
         float4 pj[4];
 #pragma unroll
-        for (uint32_t b = 0; b < 4; ++b) j[b] = (k0 + b < n) ? __ldg(e + (size_t)(k0 + b) * C.stride) : i;
+        for (uint32_t b = 0; b < 4; ++b) j[b] = (k0 + b < n) ? __ldcs(e + (size_t)(k0 + b) * C.stride) : i;
 #pragma unroll
         for (uint32_t b = 0; b < 4; ++b) pj[b] = __ldg(p + j[b]);
 #pragma unroll
