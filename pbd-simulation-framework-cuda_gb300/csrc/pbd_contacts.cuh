@@ -105,15 +105,20 @@ contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, 
     const float reach2 = P.d * P.d * 1.0001f;
     const uint32_t* __restrict__ e = C.list + i;
     uint32_t word = 0;
+    uint32_t jn[4];   // the next batch's entries, loaded while this batch is tested
+#pragma unroll
+    for (uint32_t b = 0; b < 4; ++b) jn[b] = (b < n) ? __ldcs(e + (size_t)b * C.stride) : i;
 #pragma unroll 1
     for (uint32_t k0 = 0; k0 < n; k0 += 4) {
         if ((k0 & 31u) == 0u) word = C.solved[(size_t)(k0 >> 5) * C.stride + i];
         uint32_t j[4];
         float4 pj[4];
 #pragma unroll
-        for (uint32_t b = 0; b < 4; ++b) j[b] = (k0 + b < n) ? __ldcs(e + (size_t)(k0 + b) * C.stride) : i;
+        for (uint32_t b = 0; b < 4; ++b) j[b] = jn[b];
 #pragma unroll
         for (uint32_t b = 0; b < 4; ++b) pj[b] = __ldg(p + j[b]);
+#pragma unroll
+        for (uint32_t b = 0; b < 4; ++b) jn[b] = (k0 + 4 + b < n) ? __ldcs(e + (size_t)(k0 + 4 + b) * C.stride) : i;
 #pragma unroll
         for (uint32_t b = 0; b < 4; ++b) {
             const uint32_t k = k0 + b;
