@@ -695,7 +695,9 @@ enum DeltaMode : uint32_t {
 };
 
 struct DeltaVisit {
-    struct Contrib { float ax, ay, az, aw, cx, cy, cz; uint32_t flags; };   // flags: 1 delta part, 2 contact part
+    // coef * r is the density part, t * (-r) the contact part; add() applies both with explicit
+    // FMAs, so every walker (cells, lists, cooperative warp) rounds them the same way
+    struct Contrib { float coef, rx, ry, rz, rw, t; uint32_t flags; };   // flags: 1 delta part, 2 contact part
     const DevParams& P;
     const float* __restrict__ lambda;
     const float* __restrict__ w;       // inverse masses, or null (all 1, the reference)
@@ -710,11 +712,11 @@ struct DeltaVisit {
         : P(P_), lambda(lam), w(w_), pi(pi_), li(li_), wi(wi_), do_delta(dd), do_collide(dc),
           all_pairs(P_.far_pairs_zero == 0u), pacc(pi_), xacc(xi_), xi(xi_) {}
     __device__ void reset() { ax = ay = az = aw = 0.f; pacc = pi; xacc = xi; }
-    __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u}; }
+    __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u}; }
     __device__ static bool effective(const Contrib& c) { return c.flags != 0u; }
     __device__ static Contrib shfl(const Contrib& c, int k) {
-        return Contrib{shfl_f(c.ax, k), shfl_f(c.ay, k), shfl_f(c.az, k), shfl_f(c.aw, k), shfl_f(c.cx, k),
-                       shfl_f(c.cy, k), shfl_f(c.cz, k), shfl_u(c.flags, k)};
+        return Contrib{shfl_f(c.coef, k), shfl_f(c.rx, k), shfl_f(c.ry, k), shfl_f(c.rz, k), shfl_f(c.rw, k),
+                       shfl_f(c.t, k), shfl_u(c.flags, k)};
     }
     __device__ __forceinline__ void end_contacts(uint32_t) {}
     using Extra = float;   // lambda_j
@@ -722,6 +724,7 @@ struct DeltaVisit {
     __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, float lj, bool contact) const {
         Contrib c = zero();
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z, rw = pi.w - pj.w;
+        c.rx = rx; c.ry = ry; c.rz = rz; c.rw = rw;
         const float r2 = rx * rx + ry * ry + rz * rz;
         if (!all_pairs && r2 >= P.cut2) return c;
         const float dist = sqrtf(r2);
@@ -730,8 +733,7 @@ struct DeltaVisit {
             if (s != 0.0f || all_pairs) {
                 const float W = poly6(P, dist);
                 const float sc = -P.k_scorr * powi(W * P.inv_wq, P.n_scorr);
-                const float coef = (li + lj + sc) * s;
-                c.ax = coef * rx; c.ay = coef * ry; c.az = coef * rz; c.aw = coef * rw;
+                c.coef = (li + lj + sc) * s;
                 c.flags |= 1u;
             }
         }
@@ -745,22 +747,22 @@ struct DeltaVisit {
                 share = (wi + wj) > 0.0f ? wi / (wi + wj) : 0.0f;
             }
             if (overlap > 0.0f && dist > 0.00001f && share != 0.0f) {
-                const float sc = -share * overlap;
-                const float inv = 1.0f / dist;      // dir / len with one reciprocal
-                c.cx = (sc * (-rx * inv)) * P.one_minus_stiffness;
-                c.cy = (sc * (-ry * inv)) * P.one_minus_stiffness;
-                c.cz = (sc * (-rz * inv)) * P.one_minus_stiffness;
+                // -share * overlap * (1 - stiffness) along -r / |r|
+                c.t = __fmul_rn(__fmul_rn(-share * overlap, 1.0f / dist), P.one_minus_stiffness);
                 c.flags |= 2u;
             }
         }
         return c;
     }
     __device__ __forceinline__ void add(const Contrib& c, bool) {
-        if (c.flags & 1u) { ax = __fadd_rn(ax, c.ax); ay = __fadd_rn(ay, c.ay); az = __fadd_rn(az, c.az); aw = __fadd_rn(aw, c.aw); }
+        if (c.flags & 1u) {
+            ax = __fmaf_rn(c.coef, c.rx, ax); ay = __fmaf_rn(c.coef, c.ry, ay);
+            az = __fmaf_rn(c.coef, c.rz, az); aw = __fmaf_rn(c.coef, c.rw, aw);
+        }
         if (c.flags & 2u) {
-            pacc.x = __fadd_rn(pacc.x, c.cx); xacc.x = __fadd_rn(xacc.x, c.cx);
-            pacc.y = __fadd_rn(pacc.y, c.cy); xacc.y = __fadd_rn(xacc.y, c.cy);
-            pacc.z = __fadd_rn(pacc.z, c.cz); xacc.z = __fadd_rn(xacc.z, c.cz);
+            pacc.x = __fmaf_rn(-c.rx, c.t, pacc.x); xacc.x = __fmaf_rn(-c.rx, c.t, xacc.x);
+            pacc.y = __fmaf_rn(-c.ry, c.t, pacc.y); xacc.y = __fmaf_rn(-c.ry, c.t, xacc.y);
+            pacc.z = __fmaf_rn(-c.rz, c.t, pacc.z); xacc.z = __fmaf_rn(-c.rz, c.t, xacc.z);
         }
     }
 };
