@@ -518,17 +518,19 @@ __device__ __forceinline__ void note_particle(const DeferList& D, uint32_t i) {
 // computeLambda (Density.h:48-93)
 // ======================================================================================
 struct LambdaVisit {
-    struct Contrib { float a, b, gx, gy, gz, gw; uint32_t near; };
+    // a = W, b = |grad|^2 = s^2 |r|^2; the gradient sum takes s * r by explicit FMAs, so every
+    // walker rounds it the same way
+    struct Contrib { float a, b, s, rx, ry, rz, rw; uint32_t near; };
     const DevParams& P;
     float4 pi;
     float A = 0.f, B = 0.f, Cx = 0.f, Cy = 0.f, Cz = 0.f, Cw = 0.f;
     __device__ LambdaVisit(const DevParams& P_, float4 pi_) : P(P_), pi(pi_) {}
     __device__ void reset() { A = B = Cx = Cy = Cz = Cw = 0.f; }
-    __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u}; }
+    __device__ static Contrib zero() { return Contrib{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0u}; }
     __device__ static bool effective(const Contrib& c) { return c.near != 0u; }
     __device__ static Contrib shfl(const Contrib& c, int k) {
-        return Contrib{shfl_f(c.a, k), shfl_f(c.b, k), shfl_f(c.gx, k), shfl_f(c.gy, k), shfl_f(c.gz, k),
-                       shfl_f(c.gw, k), shfl_u(c.near, k)};
+        return Contrib{shfl_f(c.a, k), shfl_f(c.b, k), shfl_f(c.s, k), shfl_f(c.rx, k), shfl_f(c.ry, k),
+                       shfl_f(c.rz, k), shfl_f(c.rw, k), shfl_u(c.near, k)};
     }
     __device__ __forceinline__ void end_contacts(uint32_t) {}
     __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, bool) const {
@@ -536,14 +538,15 @@ struct LambdaVisit {
         const float r2 = rx * rx + ry * ry + rz * rz;
         if (r2 >= P.cut2) return zero();      // every kernel is exactly 0 there
         const float dist = sqrtf(r2);
-        const float s = spiky_scale(P, dist, r2 + rw * rw);
-        const float gx = s * rx, gy = s * ry, gz = s * rz, gw = s * rw;
-        return Contrib{poly6(P, dist), gx * gx + gy * gy + gz * gz + gw * gw, gx, gy, gz, gw, 1u};
+        const float r2w = r2 + rw * rw;
+        const float s = spiky_scale(P, dist, r2w);
+        return Contrib{poly6(P, dist), __fmul_rn(__fmul_rn(s, s), r2w), s, rx, ry, rz, rw, 1u};
     }
     __device__ __forceinline__ void add(const Contrib& c, bool) {
         if (!c.near) return;
         A = __fadd_rn(A, c.a); B = __fadd_rn(B, c.b);
-        Cx = __fadd_rn(Cx, c.gx); Cy = __fadd_rn(Cy, c.gy); Cz = __fadd_rn(Cz, c.gz); Cw = __fadd_rn(Cw, c.gw);
+        Cx = __fmaf_rn(c.s, c.rx, Cx); Cy = __fmaf_rn(c.s, c.ry, Cy);
+        Cz = __fmaf_rn(c.s, c.rz, Cz); Cw = __fmaf_rn(c.s, c.rw, Cw);
     }
     // the sums the reverse pass needs: aux[i] = (rho, B, S.x, S.y), aux[N + i] = (S.z, S.w, 0, 0)
     __device__ __forceinline__ void store_aux(float4* __restrict__ aux, uint32_t N, uint32_t i) const {
