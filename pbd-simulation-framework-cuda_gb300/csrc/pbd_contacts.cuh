@@ -105,6 +105,7 @@ contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, 
     const float reach2 = P.d * P.d * 1.0001f;
     const uint32_t* __restrict__ e = C.list + i;
     uint32_t word = 0;
+    unsigned long long own = 0ull;
     uint32_t jn[4];   // the next batch's entries, loaded while this batch is tested
 #pragma unroll
     for (uint32_t b = 0; b < 4; ++b) jn[b] = (b < n) ? __ldcs(e + (size_t)b * C.stride) : i;
@@ -130,10 +131,11 @@ contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, 
             if (!contact_geometry(P, p, w, i, j[b], nn, h1, h2)) continue;
             const uint32_t c = i * C.M + k;
             const unsigned long long key = ((unsigned long long)lowbias32(c + 1u) << 32) | c;
-            if (key > *((volatile unsigned long long*)(C.best + i))) atomicMax(C.best + i, key);
-            if (key > *((volatile unsigned long long*)(C.best + j[b]))) atomicMax(C.best + j[b], key);
+            own = key > own ? key : own;          // i's own offers: one atomic at the end
+            atomicMax(C.best + j[b], key);        // the partner's (no read first: fire and forget)
         }
     }
+    if (own) atomicMax(C.best + i, own);
 }
 
 // The constraint particle i took, if it is i's own and its partner took it too: solve it.
