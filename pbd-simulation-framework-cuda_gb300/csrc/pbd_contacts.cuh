@@ -40,23 +40,35 @@ __device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
     return x;
 }
 
-// The contact between particles i and j at the current positions: false when it does not act
-// (no overlap, coincident particles, or two immovable particles).
+// |p_j - p_i| of a contact pair, with explicit FMAs: the claim and the solve pass round it the
+// same way, so they agree on which contacts act.
+__device__ __forceinline__ float contact_len(float dx, float dy, float dz) {
+    return sqrtf(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))));
+}
+// Whether the contact of i and j at distance len acts: an overlap, not coincident, and not two
+// immovable particles.
+__device__ __forceinline__ bool contact_acts(const DevParams& P, const float* __restrict__ w, uint32_t i, uint32_t j,
+                                             float len) {
+    if (w && !(w[i] + w[j] > 0.f)) return false;
+    const float overlap = P.d - len;
+    return (overlap * 0.5f > 0.f) && len > 0.00001f;
+}
+
+// The contact between particles i and j at the current positions: false when it does not act.
 __device__ __forceinline__ bool contact_geometry(const DevParams& P, const float4* __restrict__ p,
                                                  const float* __restrict__ w, uint32_t i, uint32_t j,
                                                  float4& n, float& h1, float& h2) {
     const float4 p1 = p[i], p2 = p[j];
     const float dx = p2.x - p1.x, dy = p2.y - p1.y, dz = p2.z - p1.z;
-    const float len = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float len = contact_len(dx, dy, dz);
+    if (!contact_acts(P, w, i, j, len)) return false;
     float s1 = 0.5f, s2 = 0.5f;
     if (w) {
         const float w1 = w[i], w2 = w[j];
-        if (!(w1 + w2 > 0.f)) return false;
         s1 = w1 / (w1 + w2);
         s2 = w2 / (w1 + w2);
     }
     const float overlap = P.d - len;
-    if (!(overlap * 0.5f > 0.f) || len <= 0.00001f) return false;
     n = make_float4(dx / len, dy / len, dz / len, 0.f);
     h1 = overlap * s1;
     h2 = overlap * s2;
@@ -126,9 +138,7 @@ contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, 
             if (k >= n || ((word >> (k & 31u)) & 1u)) continue;
             const float dx = pj[b].x - pi.x, dy = pj[b].y - pi.y, dz = pj[b].z - pi.z;
             if (!(dx * dx + dy * dy + dz * dz < reach2)) continue;
-            float4 nn;
-            float h1, h2;
-            if (!contact_geometry(P, p, w, i, j[b], nn, h1, h2)) continue;
+            if (!contact_acts(P, w, i, j[b], contact_len(dx, dy, dz))) continue;
             const uint32_t c = i * C.M + k;
             const unsigned long long key = ((unsigned long long)lowbias32(c + 1u) << 32) | c;
             own = key > own ? key : own;          // i's own offers: one atomic at the end
