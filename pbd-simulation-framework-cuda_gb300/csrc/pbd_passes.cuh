@@ -1069,23 +1069,30 @@ struct VortViscVisitT {
 
 using VortViscVisit = VortViscVisitT<3u>;
 
-template <class VV>
-__device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i, const VV& vis,
+// The vorticity force from the vorticity sums of `vo` and the viscosity update from the sums of
+// `vs` (the same visitor when one walk summed both terms).  Explicitly rounded, so every kernel
+// that finishes a particle stores the same bits.
+template <class VO, class VS>
+__device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i, const VO& vo, const VS& vs,
                                                  float4* __restrict__ vout, float4* __restrict__ fext,
                                                  const float* __restrict__ w) {
-    if (vis.vort) {
+    if (vo.vort) {
         const float EPS = 0.00000001f;
-        const float gl = sqrtf(vis.gx * vis.gx + vis.gy * vis.gy + vis.gz * vis.gz);
-        const float inv = 1.0f / (gl + EPS);
-        const float nx = inv * (vis.gx + EPS), ny = inv * (vis.gy + EPS), nz = inv * (vis.gz + EPS);
+        const float gl = sqrtf(__fmaf_rn(vo.gz, vo.gz, __fmaf_rn(vo.gy, vo.gy, __fmul_rn(vo.gx, vo.gx))));
+        const float inv = 1.0f / __fadd_rn(gl, EPS);
+        const float nx = __fmul_rn(inv, __fadd_rn(vo.gx, EPS)), ny = __fmul_rn(inv, __fadd_rn(vo.gy, EPS)),
+                    nz = __fmul_rn(inv, __fadd_rn(vo.gz, EPS));
         const float e = P.e_vort;
-        const float4 oi = vis.oi;
-        fext[i] = make_float4(e * (ny * oi.z - nz * oi.y), e * (nz * oi.x - nx * oi.z), e * (nx * oi.y - ny * oi.x), 0.f);
+        const float4 oi = vo.oi;
+        fext[i] = make_float4(__fmul_rn(e, __fmaf_rn(ny, oi.z, -__fmul_rn(nz, oi.y))),
+                              __fmul_rn(e, __fmaf_rn(nz, oi.x, -__fmul_rn(nx, oi.z))),
+                              __fmul_rn(e, __fmaf_rn(nx, oi.y, -__fmul_rn(ny, oi.x))), 0.f);
     }
-    if (vis.visc) {
-        const float c = w ? w[i] * P.c_visc : P.c_visc;   // a solid keeps its velocity
-        const float4 vi = vis.vi;
-        vout[i] = make_float4(vi.x + c * vis.sx, vi.y + c * vis.sy, vi.z + c * vis.sz, vi.w + c * vis.sw);
+    if (vs.visc) {
+        const float c = w ? __fmul_rn(w[i], P.c_visc) : P.c_visc;   // a solid keeps its velocity
+        const float4 vi = vs.vi;
+        vout[i] = make_float4(__fmaf_rn(c, vs.sx, vi.x), __fmaf_rn(c, vs.sy, vi.y), __fmaf_rn(c, vs.sz, vi.z),
+                              __fmaf_rn(c, vs.sw, vi.w));
     }
 }
 
@@ -1106,7 +1113,7 @@ vort_visc_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
         vis.reset();
         walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
     }
-    vort_visc_finish(P, i, vis, vout, fext, w);
+    vort_visc_finish(P, i, vis, vis, vout, fext, w);
 }
 
 // One warp runs vorticity + viscosity for particle i over the cells.
@@ -1119,7 +1126,7 @@ __device__ __noinline__ void coop_vort_visc(const DevParams& P, const float4* __
     const SceneCtx S = scene_ctx(P, i);
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
     walk_coop(P, S, i, pa[i], p, cs, ce, vis);
-    if (lane_id() == 0) vort_visc_finish(P, i, vis, vout, fext, w);
+    if (lane_id() == 0) vort_visc_finish(P, i, vis, vis, vout, fext, w);
 }
 
 // vorticity + viscosity over a stored list (the full list with vorticity, else the omega pass's
@@ -1147,14 +1154,12 @@ vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* _
         walk_list<false, 2>(Lv, i, meta, p, vo);   // position + omega per entry: batches of 2 fit the registers
         VortViscVisitT<2u> vs(P, vin, omega, p[i], vin[i], oi, false, true);
         walk_near(Ln, i, nm, p, vs);
-        vo.sx = vs.sx; vo.sy = vs.sy; vo.sz = vs.sz; vo.sw = vs.sw;
-        vo.visc = true;
-        vort_visc_finish(P, i, vo, vout, fext, w);
+        vort_visc_finish(P, i, vo, vs, vout, fext, w);
         return;
     }
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
     walk_list<false, 2>(Lv, i, meta, p, vis);
-    vort_visc_finish(P, i, vis, vout, fext, w);
+    vort_visc_finish(P, i, vis, vis, vout, fext, w);
 }
 
 __global__ void __launch_bounds__(128)
