@@ -428,6 +428,18 @@ __device__ __forceinline__ uint32_t store_full_list(const DevParams& P, const Sc
             reach += len[c] - ((valid && s3[c] <= i && i < e) ? 1u : 0u);
         }
         const uint32_t l01 = len[0] + len[1], T = l01 + len[2];
+        if (reach < M && reach <= F.kmax) {   // the column fits below the cap and the list's room
+            uint32_t* o = out + (size_t)n * F.stride;
+#pragma unroll 1
+            for (uint32_t t = 0; t < T; ++t) {
+                const uint32_t j = t < len[0] ? s3[0] + t : (t < l01 ? s3[1] + (t - len[0]) : s3[2] + (t - l01));
+                if (j == i) continue;
+                *o = j;
+                o += F.stride;
+            }
+            n = reach;
+            continue;
+        }
 #pragma unroll 1
         for (uint32_t t = 0; t < T; ++t) {
             const uint32_t j = t < len[0] ? s3[0] + t : (t < l01 ? s3[1] + (t - len[0]) : s3[2] + (t - l01));
