@@ -129,3 +129,32 @@ def test_lists_with_a_small_cap(need_gpu, pbd, scenes, cap):
     a = _run(pbd, params, pos, vel, 12)
     b = _run(pbd, params, pos, vel, 12, full_walk=True)
     _same(a, b)
+
+
+def test_block_size_leaves_results_unchanged(need_gpu, pbd, scenes, tmp_path):
+    """pbd_autotune picks the neighbour passes' block size; every size gives the same bits (the
+    particles without a list are walked by whichever blocks, each on its own)"""
+    import json
+    params = scenes.workload_params(pbd, 32, 1000.0, vorticity=0.0005, viscosity=0.01)
+    params.lambda_epsilon = 0.1
+    params.flags |= pbd.FLAG_TRACK_IDS
+    pos, vel = scenes.lattice(20, 16, 20, spacing=0.9, seed=12)
+    probe = tmp_path / "probe.jsonl"
+    sim = pbd.Sim(params, len(pos))
+    sim.add_particles(pos, vel)
+    assert sim.autotune(str(probe)) in (64, 128, 256)
+    sim.close()
+    sig = json.loads(probe.read_text().splitlines()[0])["signature"]
+    states = []
+    for block in (64, 128, 256):
+        cache = tmp_path / f"b{block}.jsonl"
+        cache.write_text(json.dumps({"signature": sig, "block": block}) + "\n")
+        sim = pbd.Sim(params, len(pos))
+        sim.add_particles(pos, vel)
+        assert sim.autotune(str(cache)) == block          # served from the cache: no frames run
+        sim.step(10)
+        sim.sync()
+        states.append(sim.state())
+        sim.close()
+    for st in states[1:]:
+        _same(states[0], st)
