@@ -6,8 +6,9 @@ Our arm (default): 100^3 = 1,000,000 fluid particles in a 128^3-cell domain (see
 4 solver iterations, vorticity 5e-4, XSPH viscosity 0.01, FP32.  `value` is particle-steps/s
 with the state resident in HBM (K frames replayed as CUDA graphs, CUDA events on the
 launching stream); `e2e` drives the reference-facing C ABI with host buffers each frame
-(pbd_clear + pbd_add_particles from pinned memory, pbd_step, pbd_get_state), copies inside
-the timed region.  The roofline entry is for the dominant kernel, timed with CUDA event
+(pbd_clear + pbd_add_particles from pinned memory, then pbd_step_readback: one frame and the
+final positions and velocities back into pinned memory, the position copy beside the frame's
+last passes; the next frame starts from that output), copies inside the timed region.  The roofline entry is for the dominant kernel, timed with CUDA event
 pairs around each launch (pbd_profile_frames) over the same number of frames.
 
 Reference arm (--impl reference): the reference step has no CPU implementation and its CUDA
@@ -509,11 +510,17 @@ def run_ours(args):
     vp = hv.ctypes.data_as(pbd.C.POINTER(pbd.C.c_float))
     L = pbd.lib()
 
+    # each frame: the state in from pinned host memory, one step, the state out to pinned host
+    # memory (pbd_step_readback: the position copy runs beside the frame's last passes); the
+    # next frame's input is this frame's output
+    src = [xp, vp]
+    rx, rv = pbd.C.POINTER(pbd.C.c_float)(), pbd.C.POINTER(pbd.C.c_float)()
+
     def e2e_frame():
         pbd.check(L.pbd_clear(sim.h))
-        pbd.check(L.pbd_add_particles(sim.h, n, xp, vp, None))
-        pbd.check(L.pbd_step(sim.h, 1, pbd.C.c_void_p(sh)))
-        pbd.check(L.pbd_get_state(sim.h, xp, vp, None, None))
+        pbd.check(L.pbd_add_particles(sim.h, n, src[0], src[1], None))
+        pbd.check(L.pbd_step_readback(sim.h, 1, pbd.C.c_void_p(sh), pbd.C.byref(rx), pbd.C.byref(rv)))
+        src[0], src[1] = rx, rv
 
     e2e_frame()
     barrier()

@@ -138,6 +138,14 @@ struct pbd_sim {
     Cur exec_start[kMaxGraphs];
     Cur exec_end[kMaxGraphs];
     int nexec = 0;
+    // pbd_step_readback: pinned host copies of x and v (2 x capacity float4, allocated on first
+    // use), a side stream for the position copy, and frame graphs (one per entry of exec) that
+    // copy the positions beside the frame's omega / vorticity / viscosity passes
+    float4* rb_host = nullptr;
+    cudaStream_t rb_stream = nullptr;
+    cudaEvent_t rb_fork = nullptr, rb_join = nullptr;
+    cudaGraphExec_t rb_exec[kMaxGraphs]{};
+    int rb_n = 0;
     uint32_t graph_n = 0xFFFFFFFFu;
     bool dirty = true;
     uint32_t launches = 0;
@@ -271,8 +279,10 @@ static void launch_delta_list(uint32_t gn, int tn, cudaStream_t st, const DevPar
 }
 
 // Record (or run) one frame of Fluid::compute (Fluid.cu:14-97) on `st`.
+// readback: copy the final positions to s->rb_host on s->rb_stream once they are final (beside
+// the frame's remaining passes) and the final velocities at the end of the frame.
 cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only, uint32_t& nl,
-                          Profiler* prof = nullptr, const Tape* tape = nullptr) {
+                          Profiler* prof = nullptr, const Tape* tape = nullptr, bool readback = false) {
     const DevParams P = make_dev_params(s);
     const pbd_params& prm = s->prm;
     const uint32_t N = s->N;
@@ -483,6 +493,12 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         PROF_END();
         ++nl;
     }
+    if (readback) {   // x is final: copy it while omega, vorticity and viscosity run
+        cudaEventRecord(s->rb_fork, st);
+        cudaStreamWaitEvent(s->rb_stream, s->rb_fork, 0);
+        cudaMemcpyAsync(s->rb_host, s->x[cur.x], (size_t)N * 16, cudaMemcpyDeviceToHost, s->rb_stream);
+        cudaEventRecord(s->rb_join, s->rb_stream);
+    }
     const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
         PROF_BEGIN(use_full ? "omega_list" : "omega");
@@ -522,18 +538,25 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         PROF_END();
         if (visc) cur.v ^= 1;
     }
+    if (readback) {
+        cudaMemcpyAsync(s->rb_host + s->cap, s->v[cur.v], (size_t)N * 16, cudaMemcpyDeviceToHost, st);
+        cudaStreamWaitEvent(st, s->rb_join, 0);
+    }
     return cudaGetLastError();
 }
 
 void destroy_graphs(pbd_sim* s) {
-    for (int k = 0; k < kMaxGraphs; ++k)
+    for (int k = 0; k < kMaxGraphs; ++k) {
         if (s->exec[k]) { cudaGraphExecDestroy(s->exec[k]); s->exec[k] = nullptr; }
+        if (s->rb_exec[k]) { cudaGraphExecDestroy(s->rb_exec[k]); s->rb_exec[k] = nullptr; }
+    }
     s->nexec = 0;
+    s->rb_n = 0;
 }
 
-int capture_one(pbd_sim* s, Cur& c, cudaGraphExec_t* out, uint32_t& nl) {
+int capture_one(pbd_sim* s, Cur& c, cudaGraphExec_t* out, uint32_t& nl, bool readback = false) {
     CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = enqueue_frame(s, s->cap_stream, c, false, nl);
+    cudaError_t e = enqueue_frame(s, s->cap_stream, c, false, nl, nullptr, nullptr, readback);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(s->cap_stream, &g);
     if (e != cudaSuccess) { if (g) cudaGraphDestroy(g); return cuda_fail("frame capture", e); }
@@ -581,6 +604,18 @@ int build_graphs(pbd_sim* s) {
     }
     set_error("internal: the frame's buffer records do not cycle");
     return PBD_ERR_CUDA;
+}
+
+// The readback twin of every recorded frame graph (same start and end records).
+int build_rb_graphs(pbd_sim* s) {
+    for (int k = 0; k < s->nexec; ++k) {
+        Cur c = s->exec_start[k];
+        uint32_t nl = 0;
+        if (int rc = capture_one(s, c, &s->rb_exec[k], nl, true)) return rc;
+        if (!(c == s->exec_end[k])) { set_error("internal: readback frame ends elsewhere"); return PBD_ERR_CUDA; }
+    }
+    s->rb_n = s->nexec;
+    return PBD_OK;
 }
 
 int check_sim(const pbd_sim* s, const char* fn) {
@@ -730,6 +765,10 @@ int pbd_destroy(pbd_sim* s) {
     if (s->adj_arena) cudaFree(s->adj_arena);
     if (s->ct_arena) cudaFree(s->ct_arena);
     if (s->img_arena) cudaFree(s->img_arena);
+    if (s->rb_host) cudaFreeHost(s->rb_host);
+    if (s->rb_stream) cudaStreamDestroy(s->rb_stream);
+    if (s->rb_fork) cudaEventDestroy(s->rb_fork);
+    if (s->rb_join) cudaEventDestroy(s->rb_join);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     cudaError_t e = cudaFree(s->arena);
     delete s;
@@ -877,6 +916,48 @@ int pbd_step(pbd_sim* s, int nsteps, void* stream) {
     }
     s->table_hint = s->N;
     s->last_stream = st;
+    return PBD_OK;
+}
+
+int pbd_step_readback(pbd_sim* s, int nsteps, void* stream, const float** pos4, const float** vel4) {
+    clear_error();
+    if (int rc = check_sim(s, "pbd_step_readback")) return rc;
+    if (nsteps < 1) { set_error("pbd_step_readback: nsteps < 1"); return PBD_ERR_INVALID_ARG; }
+    if (s->batched) { set_error("pbd_step_readback: a batch reads its scenes with pbd_batch_get_state"); return PBD_ERR_INVALID_ARG; }
+    if (!s->rb_host) {
+        CK(cudaHostAlloc((void**)&s->rb_host, (size_t)2 * s->cap * 16, cudaHostAllocDefault));
+        CK(cudaStreamCreateWithFlags(&s->rb_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&s->rb_fork, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&s->rb_join, cudaEventDisableTiming));
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->N > 0) {
+        if (nsteps > 1)
+            if (int rc = pbd_step(s, nsteps - 1, stream)) return rc;
+        ++s->gen;
+        if (s->dirty || s->graph_n != s->N || s->table_passes != sort_passes(s)) {
+            if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
+            if (int rc = settle_tables(s, st)) return rc;
+            if (int rc = build_graphs(s)) return rc;
+        }
+        int g = -1;
+        for (int j = 0; j < s->nexec; ++j)
+            if (s->exec_start[j] == s->cur) { g = j; break; }
+        if (g < 0) {
+            if (int rc = build_graphs(s)) return rc;
+            g = 0;
+        }
+        if (s->rb_n != s->nexec)
+            if (int rc = build_rb_graphs(s)) return rc;
+        s->anchor = (s->cur.p + 1) % 3;
+        CK(cudaGraphLaunch(s->rb_exec[g], st));
+        s->cur = s->exec_end[g];
+        s->table_hint = s->N;
+        s->last_stream = st;
+        CK(cudaStreamSynchronize(st));
+    }
+    if (pos4) *pos4 = reinterpret_cast<const float*>(s->rb_host);
+    if (vel4) *vel4 = reinterpret_cast<const float*>(s->rb_host + s->cap);
     return PBD_OK;
 }
 

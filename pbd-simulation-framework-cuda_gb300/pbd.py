@@ -32,7 +32,7 @@ EXPORTED = [
     "pbd_autotune", "pbd_batch_create", "pbd_batch_destroy", "pbd_batch_add_particles", "pbd_batch_step",
     "pbd_batch_sync", "pbd_batch_num_particles", "pbd_batch_get_state", "pbd_batch_autotune",
     "pbd_batch_launches_per_step", "pbd_batch_profile_frames", "pbd_adjoint_forward", "pbd_adjoint_backward", "pbd_render_sprites",
-    "pbd_density_error",
+    "pbd_density_error", "pbd_step_readback",
 ]
 
 
@@ -149,7 +149,8 @@ def lib():
             "pbd_add_particles": [vp, u32, fp, fp, fp], "pbd_add_particles_device": [vp, u32, vp, vp, vp, vp],
             "pbd_add_particles_mass": [vp, u32, fp, fp, fp, fp],
             "pbd_add_particle": [vp, fp, fp], "pbd_clear": [vp], "pbd_step": [vp, i32, vp], "pbd_sync": [vp],
-            "pbd_get_state": [vp, fp, fp, fp, u32p], "pbd_get_device_state": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)],
+            "pbd_get_state": [vp, fp, fp, fp, u32p],
+            "pbd_step_readback": [vp, C.c_int, vp, C.POINTER(fp), C.POINTER(fp)], "pbd_get_device_state": [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)],
             "pbd_debug_dump": [vp, u32p, u32p, u32p, u32p, u32, fp, fp, fp],
             "pbd_debug_neighbours": [vp, u32, u32p, u32p, u32p, i32], "pbd_debug_front": [vp, vp],
             "pbd_launches_per_step": [vp, u32p],
@@ -277,6 +278,16 @@ class Sim:
 
     def sync(self):
         check(self.L.pbd_sync(self.h))
+
+    def step_readback(self, nsteps=1, stream=0, copy=True):
+        """pbd_step, then the final x and v ((n, 4) float32 each) from the library's pinned host
+        arrays (views valid until the next call unless `copy`)."""
+        px, pv = C.POINTER(C.c_float)(), C.POINTER(C.c_float)()
+        check(self.L.pbd_step_readback(self.h, nsteps, C.c_void_p(stream), C.byref(px), C.byref(pv)))
+        n = self.n
+        x = np.ctypeslib.as_array(px, shape=(n, 4))
+        v = np.ctypeslib.as_array(pv, shape=(n, 4))
+        return (x.copy(), v.copy()) if copy else (x, v)
 
     def state(self):
         n = self.n

@@ -158,3 +158,22 @@ def test_block_size_leaves_results_unchanged(need_gpu, pbd, scenes, tmp_path):
         sim.close()
     for st in states[1:]:
         _same(states[0], st)
+
+
+@pytest.mark.parametrize("vort,visc", [(0.0, 0.0), (0.0005, 0.01)])
+def test_step_readback_matches_step_and_get_state(need_gpu, pbd, scenes, vort, visc):
+    """pbd_step_readback (positions copied beside the last passes) returns the state pbd_step +
+    pbd_get_state return, and the simulation continues from it identically"""
+    params = scenes.workload_params(pbd, 32, 1000.0, vorticity=vort, viscosity=visc)
+    params.lambda_epsilon = 0.1
+    params.flags |= pbd.FLAG_TRACK_IDS
+    pos, vel = scenes.lattice(20, 16, 20, spacing=0.9, seed=13)
+    a = pbd.Sim(params, len(pos)); a.add_particles(pos, vel)
+    b = pbd.Sim(params, len(pos)); b.add_particles(pos, vel)
+    for n in (1, 3, 1):
+        xa, va = a.step_readback(n)
+        b.step(n)
+        sb = b.state()
+        assert np.array_equal(xa, sb["x"]) and np.array_equal(va, sb["v"])
+    _same(a.state(), b.state())
+    a.close(); b.close()
