@@ -208,12 +208,13 @@ __device__ __forceinline__ uint32_t walk_coop(const DevParams& P, const SceneCtx
 }
 
 // One thread per particle over a stored list (meta not kListOff): the contact entries, then
-// end_contacts, then the rest.  Entries go in batches of kListBatch: the batch's index loads,
-// then its position loads, are all in flight before the first contribution, instead of one
-// dependent pair per entry.
-// Every visitor adds its contributions with __fadd_rn: an explicitly rounded add is never
-// fused with the product that made the contribution, so the sums get the same bits whichever
-// walker (cells, stored list, cooperative warp) and whichever loop shape the compiler sees.
+// end_contacts, then the rest.  Entries go in batches of B: the batch's position (and extra)
+// loads are all in flight before the first contribution, and the next batch's indices are
+// loaded while this one is summed.
+// Every visitor adds its contributions with explicitly rounded operations (__fadd_rn, or
+// __fmaf_rn where a product goes into the sum), which the compiler never contracts, so the sums
+// get the same bits whichever walker (cells, stored list, cooperative warp) and whichever loop
+// shape the compiler sees.
 //
 // kOwn: the list was written by this thread in this kernel, so it is read with ordinary
 // (coherent) loads rather than through the read-only path.  Otherwise the list entries are
