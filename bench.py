@@ -69,6 +69,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, dev):
+    """The largest of a per-rank value over the job (the slowest replica's time)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(particles_per_rank, frames, world, seconds):
+    """Particle-steps/s of the whole job: every rank steps its own replica, the job takes as long
+    as its slowest rank."""
+    return particles_per_rank * frames * world / seconds
+
+
 def build_workload(pbd, scenes, name):
     w = scenes.WORKLOADS[name]
     params = scenes.workload_params(pbd, w["box"], REST_DENSITY, vorticity=w["vorticity"], viscosity=w["viscosity"])
@@ -454,13 +471,8 @@ def run_ours(args):
         barrier()
     sim.sync()
     ms = ev0.elapsed_time(ev1)
-    t_rank = ms / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_rank], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_rank = float(t.item())
-    value = n * args.steps * world / t_rank
+    t_rank = max_over_ranks(ms / 1e3, world, dev)
+    value = job_throughput(n, args.steps, world, t_rank)
 
     # ---- density constraint after the timed frames (mean / max |rho_i / rho0 - 1|)
     _, derr_mean, derr_max = sim.density_error(stream=sh)
@@ -528,13 +540,8 @@ def run_ours(args):
     for _ in range(e2e_steps):
         e2e_frame()
     torch.cuda.synchronize()
-    t_e2e = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_e2e], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
-    e2e_value = n * e2e_steps * world / t_e2e
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world, dev)
+    e2e_value = job_throughput(n, e2e_steps, world, t_e2e)
     sim.sync()
 
     sim.close()
