@@ -68,7 +68,24 @@ def build(force=False, verbose=False, extra_nvcc=()):
             print(" ".join(cmd), flush=True)
         subprocess.check_call(cmd)
         os.replace(LIB + ".tmp", LIB)
+    build_examples(force or bool(jobs))
     return LIB
+
+
+EXAMPLES = os.path.join(HERE, "examples")
+
+
+def build_examples(force=False):
+    """The C++ host examples, linked against libpbd.so (found beside them through the rpath)."""
+    for src in sorted(os.listdir(EXAMPLES)):
+        if not src.endswith(".cpp"):
+            continue
+        exe = os.path.join(EXAMPLES, src[:-4])
+        s = os.path.join(EXAMPLES, src)
+        if force or _newer(exe, [s, LIB, os.path.join(INCLUDE, "pbd.h")]):
+            # no FMA contraction: the host arithmetic (the spawn lattice) rounds as numpy does
+            subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", INCLUDE, s, "-o", exe,
+                                   "-L", HERE, "-lpbd", "-Wl,-rpath,$ORIGIN/.."])
 
 
 if __name__ == "__main__":

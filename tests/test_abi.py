@@ -173,3 +173,15 @@ def test_null_arguments(pbd):
     assert L.pbd_destroy(None) == pbd.OK
     p = pbd.default_params()
     assert L.pbd_create(C.byref(p), 16, None) == pbd.ERR_INVALID_ARG
+
+
+def test_cpp_host_example_links_and_parses_its_arguments(pbd):
+    """The C++ host example (examples/dam_break.cpp) is built against libpbd.so alone; without
+    arguments it prints its usage before touching the GPU."""
+    import subprocess
+    exe = os.path.join(ROOT, "pbd-simulation-framework-cuda_gb300", "examples", "dam_break")
+    if not os.path.exists(exe):
+        import build as pkg_build
+        pkg_build.build_examples(force=True)
+    r = subprocess.run([exe, "--bogus"], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 2 and "usage" in r.stderr
