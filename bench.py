@@ -360,6 +360,13 @@ def run_adjoint(torch, pbd, scenes, stream, sh, frames=60, every=10, fd_check=Tr
             for h in (1e-3, 1e-6):
                 fd, ad = fd_v0(h, horizon, gvh)
                 c[f"v0_direction@h={h:g}"] = {"adjoint": ad, "fd_fp64": fd, "rel": rel(ad, fd)}
+            # a check is conclusive only where the FP64 differences at the two steps agree with
+            # each other (the loss is smooth there); beyond that horizon the dynamics are not
+            ok = {}
+            for name, steps in (("rest_density", (1e-3, 1.25e-4)), ("eps", (1e-3, 1e-7)), ("v0_direction", (1e-3, 1e-6))):
+                a, b = (c[f"{name}@h={h:g}"]["fd_fp64"] / (h if name == "v0_direction" else 1.0) for h in steps)
+                ok[name] = rel(a, b) < 0.1
+            c["fd_steps_agree"] = ok
             checks[f"{horizon}_frames"] = c
         out["gradient_check"] = checks
         out["gradient_check_s"] = time.perf_counter() - t0
