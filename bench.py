@@ -94,13 +94,24 @@ def build_workload(pbd, scenes, name):
     return params, pos, vel, w
 
 
+def bench_out_dir():
+    d = os.environ.get("PBD_BENCH_OUT")
+    if not d:
+        import tempfile
+        d = os.path.join(tempfile.gettempdir(), "pbd_bench")
+    os.makedirs(d, exist_ok=True)
+    return d
+
+
 class ClockSampler:
     """nvidia-smi samples (200 ms) during the timed region."""
 
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # PBD_BENCH_OUT keeps the samples (and the autotuner's cache) in a folder of the caller's
+        # choosing; by default they go to a temporary folder
+        self.path = os.path.join(bench_out_dir(), f"clocks_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
@@ -186,7 +197,7 @@ def run_batched(torch, pbd, scenes, stream, sh, frames):
     shared.lambda_epsilon = LAMBDA_EPS
     descs = [pbd.scene_desc(sc["n"], sc["rest_density"], sc["gravity"], sc["box"]) for sc in sl]
     total = sum(sc["n"] for sc in sl)
-    tune_cache = os.environ.get("PBD_TUNE_CACHE", os.path.join(ROOT, "gpurun_out", "autotune.jsonl"))
+    tune_cache = os.environ.get("PBD_TUNE_CACHE", os.path.join(bench_out_dir(), "autotune.jsonl"))
     os.makedirs(os.path.dirname(tune_cache), exist_ok=True)
     with pbd.Batch(shared, descs) as tb:            # tuning copy: the autotuner advances frames
         for k, sc in enumerate(sl):
