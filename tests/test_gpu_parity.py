@@ -246,3 +246,27 @@ def test_sort_full_size_properties(need_gpu, pbd, scenes):
         occ, first = np.unique(keys, return_index=True)
         assert np.array_equal(d["cell_start"][occ], first.astype(np.uint32))
     sim.sync()
+
+
+def test_full_size_workload_vs_oracle(need_gpu, pbd, scenes, oracle_mod):
+    """The bench's own workload (fluid_1m: 1,000,000 particles, 128^3 cells, vorticity and XSPH,
+    the cell-end quirk's long range inside the fluid) against the FP32 oracle on the same inputs:
+    the front of the frame bit for bit, then 1 and 3 whole frames within the step's tolerances"""
+    import bench
+    params, pos, vel, _ = bench.build_workload(pbd, scenes, "fluid_1m")
+    params.flags |= pbd.FLAG_TRACK_IDS
+    sim, orc = setup_pair(pbd, oracle_mod, params, pos, vel)
+    sim.front()
+    orc.step_phase(oracle_mod.PHASE_FRONT)
+    g, o = sim.debug(0), orc.debug(0)
+    assert np.array_equal(g["keys"], o["keys"]) and np.array_equal(g["perm"], o["perm"])
+    gs, os_ = sim.state(), orc.state()
+    assert np.array_equal(gs["p"], os_["p"].astype(np.float32))
+    sim.close()
+    for frames, tx, tv in ((1, 10 * TOL_X1, 10 * TOL_V1), (3, TOL_X10, TOL_V10)):
+        g, o, sim, _ = _run_both(pbd, oracle_mod, params.copy(), pos, vel, frames)
+        assert np.array_equal(g["ids"], o["ids"])
+        dx = np.abs(g["x"][:, :3] - o["x"][:, :3]).max(axis=1)
+        dv = np.abs(g["v"][:, :3] - o["v"][:, :3]).max(axis=1)
+        assert dx.max() < tx and dv.max() < tv, (frames, dx.max(), dv.max())
+        sim.close()
