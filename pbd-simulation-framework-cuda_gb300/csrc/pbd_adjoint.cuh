@@ -10,8 +10,11 @@
 //             p <- p + c - Delta ;  x <- x + c
 //   update    v' = (p - x)/dt ; x' = p                                              (Update.h:11-32)
 // with r = p_i - p_j, G = spiky gradient g(|r|) r_hat, W = poly6.  The reverse passes scatter the
-// pair terms with atomic adds (so the neighbour relation need not be symmetric) and accumulate
-// dL/drest_density and dL/deps in double.
+// pair terms to the partner with atomic adds (so the neighbour relation need not be symmetric)
+// in 64-bit fixed point, which is associative, so the gradients do not depend on the order in
+// which the atomics land: a reverse pass gives the same bits every time.  A particle's own terms
+// are summed in its list's order; dL/drest_density and dL/deps are summed per block in double
+// and across blocks in fixed point.
 #pragma once
 #include "pbd_passes.cuh"
 
@@ -51,14 +54,36 @@ __device__ __forceinline__ float3 spiky_hess_mul(float g, float dg, float L, flo
                        dg * rv * rh.z + gl * (v.z - rv * rh.z));
 }
 
-__device__ __forceinline__ void atomic_sub3(float4* a, float3 v) {
-    atomicAdd(&a->x, -v.x);
-    atomicAdd(&a->y, -v.y);
-    atomicAdd(&a->z, -v.z);
+// Fixed point of the scattered terms: 2^32, which holds every float in (2^-33, 2^31) exactly
+// (the scaling is a power of two and the conversion saturates); of the two scalar gradients:
+// 2^36 (resolution 1.5e-11, range +-1.3e8).  A pass's scattered terms are taken up (and the
+// slots cleared) by the next kernel, which reads its own particle's slot first.
+constexpr float kFixScatter = 4294967296.0f;
+constexpr float kUnfixScatter = 2.3283064365386963e-10f;   // 2^-32
+constexpr double kFixScalar = 68719476736.0;
+__device__ __forceinline__ void fix_add(unsigned long long* a, float v) {
+    atomicAdd(a, (unsigned long long)__float2ll_rn(v * kFixScatter));
+}
+__device__ __forceinline__ void fix_add_scalar(unsigned long long* a, double v) {
+    const double q = fmin(fmax(v * kFixScalar, -9.0e18), 9.0e18);
+    atomicAdd(a, (unsigned long long)__double2ll_rn(q));
+}
+__device__ __forceinline__ void scatter_sub3(unsigned long long* sj, float3 v) {
+    fix_add(sj + 0, -v.x);
+    fix_add(sj + 1, -v.y);
+    fix_add(sj + 2, -v.z);
+}
+// Particle i's scattered terms as floats; the slot is cleared for the next pass.
+__device__ __forceinline__ float4 take_scattered(unsigned long long* scat, uint32_t i) {
+    unsigned long long* s = scat + 4 * (size_t)i;
+    const float4 r = make_float4(__ll2float_rn((long long)s[0]) * kUnfixScatter, __ll2float_rn((long long)s[1]) * kUnfixScatter,
+                                 __ll2float_rn((long long)s[2]) * kUnfixScatter, __ll2float_rn((long long)s[3]) * kUnfixScatter);
+    s[0] = s[1] = s[2] = s[3] = 0ull;
+    return r;
 }
 
-// Block-reduce two doubles and add them to the accumulators.
-__device__ __forceinline__ void block_add2(double a, double b, double* acc) {
+// Block-reduce two doubles (in a fixed order) and add them to the fixed-point accumulators.
+__device__ __forceinline__ void block_add2(double a, double b, unsigned long long* acc) {
     __shared__ double sa[32], sb[32];
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_down_sync(0xffffffffu, a, o);
@@ -70,8 +95,8 @@ __device__ __forceinline__ void block_add2(double a, double b, double* acc) {
     if (threadIdx.x == 0) {
         double ta = 0.0, tb = 0.0;
         for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) { ta += sa[w]; tb += sb[w]; }
-        if (ta != 0.0) atomicAdd(acc, ta);
-        if (tb != 0.0) atomicAdd(acc + 1, tb);
+        if (ta != 0.0) fix_add_scalar(acc, ta);
+        if (tb != 0.0) fix_add_scalar(acc + 1, tb);
     }
 }
 
@@ -96,8 +121,7 @@ struct AdjDeltaVisit {
     float li;
     float3 a;          // Delta-bar / rho0
     float3 cbar;       // dL/dc_i = gp_in + gx
-    float4* gp_out;
-    float* glam;
+    unsigned long long* scat;   // per particle: x, y, z of dL/dp, dL/dlambda (fixed point)
     float3 gpi;        // this particle's own accumulated term
     float3 sdelta;     // sum coef * G (for the rho0 term)
     float glami;
@@ -126,7 +150,7 @@ struct AdjDeltaVisit {
             const float3 G = make_float3(g * rh.x, g * rh.y, g * rh.z);
             const float gd = G.x * a.x + G.y * a.y + G.z * a.z;
             glami += gd;
-            atomicAdd(glam + j, gd);
+            fix_add(scat + 4 * (size_t)j + 3, gd);
             const float3 Ha = spiky_hess_mul(g, dg, L, rh, a);
             rbar.x += coef * Ha.x + gd * dsc * rh.x;
             rbar.y += coef * Ha.y + gd * dsc * rh.y;
@@ -146,7 +170,7 @@ struct AdjDeltaVisit {
             }
         }
         gpi.x += rbar.x; gpi.y += rbar.y; gpi.z += rbar.z;
-        atomic_sub3(gp_out + j, rbar);
+        scatter_sub3(scat + 4 * (size_t)j, rbar);
         return zero();
     }
     __device__ __forceinline__ void add(const Contrib&, bool) {}
@@ -155,27 +179,28 @@ struct AdjDeltaVisit {
 __global__ void __launch_bounds__(128)
 adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float* __restrict__ lambda,
                  const float4* __restrict__ gp_in, const float4* __restrict__ gx, float4* __restrict__ gp_out,
-                 float* __restrict__ glam, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, double* acc,
-                 bool collide, NbList Lt) {
+                 float* __restrict__ glam, unsigned long long* __restrict__ scat, unsigned long long* __restrict__ scat_in,
+                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, unsigned long long* acc, bool collide,
+                 NbList Lt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double drho = 0.0;
     if (i < P.N) {
         const SceneCtx S = scene_ctx(P, i);
-        const float4 gpin = gp_in[i], gxi = gx[i];
+        const float4 g0 = gp_in[i], t = take_scattered(scat_in, i), gxi = gx[i];   // + the pass after's partners
+        const float4 gpin = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
         const float inv = 1.0f / S.rho0;
         AdjDeltaVisit vis{P, lambda, p[i], lambda[i],
                           make_float3(-gpin.x * inv, -gpin.y * inv, -gpin.z * inv),
-                          make_float3(gpin.x + gxi.x, gpin.y + gxi.y, gpin.z + gxi.z), gp_out, glam,
+                          make_float3(gpin.x + gxi.x, gpin.y + gxi.y, gpin.z + gxi.z), scat,
                           make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), 0.f, collide};
         // the forward's near list of this iteration (the pairs within the cut), else the cells
         const uint32_t meta = Lt.list ? Lt.meta[i] : kListOff;
         bool deferred = false;
         if (meta != kListOff) walk_list(Lt, i, meta, p, vis);
         else walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
-        atomicAdd(&gp_out[i].x, vis.gpi.x);
-        atomicAdd(&gp_out[i].y, vis.gpi.y);
-        atomicAdd(&gp_out[i].z, vis.gpi.z);
-        atomicAdd(glam + i, vis.glami);
+        // own terms: this thread alone writes slot i (the partners' terms are in scat)
+        gp_out[i] = make_float4(gpin.x + vis.gpi.x, gpin.y + vis.gpi.y, gpin.z + vis.gpi.z, 0.f);
+        glam[i] = vis.glami;
         // Delta_i = sdelta / rho0: d/drho0 = -sdelta / rho0^2, Delta-bar = -gp_in
         drho = (double)(gpin.x * vis.sdelta.x + gpin.y * vis.sdelta.y + gpin.z * vis.sdelta.z) * (double)(inv * inv);
     }
@@ -192,7 +217,7 @@ struct AdjLambdaBwd {
     float cbar_w;      // Cbar / rho0
     float dbar2;       // 2 Dbar / rho0
     float3 Sg;
-    float4* gp_out;
+    unsigned long long* scat;
     float3 gpi;
     __device__ __forceinline__ void end_contacts(uint32_t) {}
     __device__ static Contrib zero() { return Contrib{0}; }
@@ -214,7 +239,7 @@ struct AdjLambdaBwd {
             rbar.x += dbar2 * Hv.x; rbar.y += dbar2 * Hv.y; rbar.z += dbar2 * Hv.z;
         }
         gpi.x += rbar.x; gpi.y += rbar.y; gpi.z += rbar.z;
-        atomic_sub3(gp_out + j, rbar);
+        scatter_sub3(scat + 4 * (size_t)j, rbar);
         return zero();
     }
     __device__ __forceinline__ void add(const Contrib&, bool) {}
@@ -222,13 +247,17 @@ struct AdjLambdaBwd {
 
 __global__ void __launch_bounds__(128)
 adj_lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ aux,
-                  const float* __restrict__ glam, float4* __restrict__ gp_out, const uint32_t* __restrict__ cs,
-                  const uint32_t* __restrict__ ce, double* acc, NbList Lt) {
+                  const float* __restrict__ glam, float4* __restrict__ gp_out, unsigned long long* __restrict__ scat,
+                  unsigned long long* __restrict__ scat_in, const uint32_t* __restrict__ cs,
+                  const uint32_t* __restrict__ ce, unsigned long long* acc, NbList Lt) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double drho = 0.0, deps = 0.0;
     if (i < P.N) {
         const SceneCtx S = scene_ctx(P, i);
-        const float lb = glam[i];
+        const float4 t = take_scattered(scat_in, i);   // the delta pass's partners' terms
+        const float4 g0 = gp_out[i];
+        const float4 g = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
+        const float lb = glam[i] + t.w;
         const float4 s0 = aux[i], s1 = aux[P.N + i];   // (rho, B, S.x, S.y), (S.z, S.w, 0, 0)
         const float rho0 = S.rho0;
         const float C = s0.x / rho0 - 1.0f;
@@ -240,15 +269,15 @@ adj_lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __res
         drho = (double)Cbar * (-(double)s0.x / r02) + (double)Dbar * (-(double)BS / r02);
         deps = (double)Dbar;
         if (lb != 0.0f) {
-            AdjLambdaBwd b{P, p[i], Cbar / rho0, 2.0f * Dbar / rho0, make_float3(s0.z, s0.w, s1.x), gp_out,
+            AdjLambdaBwd b{P, p[i], Cbar / rho0, 2.0f * Dbar / rho0, make_float3(s0.z, s0.w, s1.x), scat,
                            make_float3(0.f, 0.f, 0.f)};
             const uint32_t meta = Lt.list ? Lt.meta[i] : kListOff;
             bool deferred = false;
             if (meta != kListOff) walk_list(Lt, i, meta, p, b);
             else walk_seq(P, S, i, pa[i], p, cs, ce, b, false, &deferred);
-            atomicAdd(&gp_out[i].x, b.gpi.x);
-            atomicAdd(&gp_out[i].y, b.gpi.y);
-            atomicAdd(&gp_out[i].z, b.gpi.z);
+            gp_out[i] = make_float4(g.x + b.gpi.x, g.y + b.gpi.y, g.z + b.gpi.z, 0.f);   // this thread alone writes slot i
+        } else {
+            gp_out[i] = g;
         }
     }
     block_add2(drho, deps, acc);
@@ -259,7 +288,8 @@ adj_lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __res
 __global__ void adj_predict_kernel(DevParams P, const uint32_t* __restrict__ perm, const float4* __restrict__ x_in,
                                    const float4* __restrict__ v_in, const float4* __restrict__ fext,
                                    const float4* __restrict__ gp, const float4* __restrict__ gxp,
-                                   float4* __restrict__ gx_out, float4* __restrict__ gv_out) {
+                                   float4* __restrict__ gx_out, float4* __restrict__ gv_out,
+                                   unsigned long long* __restrict__ scat_in) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const uint32_t o = perm[i];
@@ -274,7 +304,8 @@ __global__ void adj_predict_kernel(DevParams P, const uint32_t* __restrict__ per
     const float mx = (px < P.bmin[0] || px > P.bmax[0]) ? 0.f : 1.f;
     const float my = (py < P.bmin[1] || py > P.bmax[1]) ? 0.f : 1.f;
     const float mz = (pz < P.bmin[2] || pz > P.bmax[2]) ? 0.f : 1.f;
-    const float4 g = gp[i], gx = gxp[i];
+    const float4 g0 = gp[i], t = take_scattered(scat_in, i), gx = gxp[i];   // + the last lambda pass's partners
+    const float4 g = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
     gx_out[o] = make_float4(gx.x + mx * g.x, gx.y + my * g.y, gx.z + mz * g.z, 0.f);
     gv_out[o] = make_float4(mx * g.x * dt, my * g.y * dt, mz * g.z * dt, 0.f);
 }

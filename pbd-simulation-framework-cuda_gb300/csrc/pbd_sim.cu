@@ -112,7 +112,9 @@ struct pbd_sim {
     std::vector<AdjGraph> adj_graphs;   // recorded segments of the adjoint
     uint64_t adj_graphs_pgen = ~0ull;
     void* adj_graphs_arena = nullptr;
-    double* adj_acc = nullptr;
+    unsigned long long* adj_acc = nullptr;   // dL/drest_density, dL/deps in fixed point
+    unsigned long long* adj_scat = nullptr;  // partners' terms of a delta reverse pass, fixed point (4 per particle)
+    unsigned long long* adj_scat2 = nullptr; // the same for the lambda reverse passes
     std::vector<uint32_t> scene_cap, scene_count;
     std::vector<SceneParams> h_scenes;
     float4 *fext = nullptr, *omega = nullptr, *delta = nullptr;
@@ -1400,7 +1402,7 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     // workspace: checkpoints, the final state, k frames of tape, gradient buffers
     const size_t per_tape = N * (16 + 16 + 4 + 4) + (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4);
     const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + 64 +
-                        (size_t)(16 + (4 + 5 * I) * k) * 256;
+                        N * 64 + (size_t)(18 + (4 + 5 * I) * k) * 256;
     if (need > s->adj_bytes) {
         if (s->adj_arena) CK(cudaStreamSynchronize(st));
         if (s->adj_arena) cudaFree(s->adj_arena);
@@ -1436,7 +1438,9 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     }
     for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
     s->adj_glam = (float*)take(N * 4);
-    s->adj_acc = (double*)take(64);
+    s->adj_acc = (unsigned long long*)take(64);
+    s->adj_scat = (unsigned long long*)take((size_t)N * 32);
+    s->adj_scat2 = (unsigned long long*)take((size_t)N * 32);
     s->adj_steps = nsteps;
     s->adj_every = k;
     s->adj_nck = nck;
@@ -1508,16 +1512,16 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
             const float4* p = T.p_it[it];
             const float4* pa = T.p_it[0];
             const NbList Lt = lists ? NbList{T.near[it], T.near_meta[it], N, kListMax} : NbList{nullptr, nullptr, 0u, 0u};
-            cudaError_t e = cudaMemcpyAsync(gp2, gp, (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
-            if (e == cudaSuccess) e = cudaMemsetAsync(s->adj_glam, 0, (size_t)N * 4, st);
-            if (e != cudaSuccess) return e;
-            adj_delta_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.lam[it], gp, gx, gp2, s->adj_glam, s->cell_start,
-                                                 s->cell_end, s->adj_acc, collide, Lt);
-            adj_lambda_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.aux[it], s->adj_glam, gp2, s->cell_start, s->cell_end,
-                                                  s->adj_acc, Lt);
+            // each pass writes every particle's own terms and scatters the partners' in fixed point;
+            // the next kernel adds a particle's scattered terms in one place: the same bits
+            // whatever order the atomics landed in
+            adj_delta_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.lam[it], gp, gx, gp2, s->adj_glam, s->adj_scat,
+                                                 s->adj_scat2, s->cell_start, s->cell_end, s->adj_acc, collide, Lt);
+            adj_lambda_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.aux[it], s->adj_glam, gp2, s->adj_scat2, s->adj_scat,
+                                                  s->cell_start, s->cell_end, s->adj_acc, Lt);
             std::swap(gp, gp2);
         }
-        adj_predict_kernel<<<ge, 256, 0, st>>>(P, T.perm, T.x_in, T.v_in, s->fext, gp, gx, gx_out, gv_out);
+        adj_predict_kernel<<<ge, 256, 0, st>>>(P, T.perm, T.x_in, T.v_in, s->fext, gp, gx, gx_out, gv_out, s->adj_scat2);
     }
     // back to the tables the next recompute's predict expects: the cells of keys[fin]
     retable(s, st, held, s->keys[fin], N);
@@ -1583,6 +1587,8 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
     CK(cudaMemcpyAsync(gx_out, dL_dx_final, (size_t)N * 16, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(gv_out, 0, (size_t)N * 16, st));
     CK(cudaMemsetAsync(s->adj_acc, 0, 64, st));
+    CK(cudaMemsetAsync(s->adj_scat, 0, (size_t)N * 32, st));
+    CK(cudaMemsetAsync(s->adj_scat2, 0, (size_t)N * 32, st));
     for (int ck = s->adj_nck - 1; ck >= 0; --ck) {
         const int f0 = ck * s->adj_every;
         const int nf = std::min(s->adj_every, s->adj_steps - f0);
@@ -1603,13 +1609,13 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
     CK(cudaMemcpyAsync(s->ids[s->cur.x], s->adj_fin_ids, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
     s->adj_last_taped = s->adj_nck == 1;       // else the tape now holds the first segment
     s->anchor = -1;
-    double acc[2] = {0.0, 0.0};
-    CK(cudaMemcpyAsync(acc, s->adj_acc, 16, cudaMemcpyDeviceToHost, st));
+    unsigned long long acc_fix[2] = {0ull, 0ull};
+    CK(cudaMemcpyAsync(acc_fix, s->adj_acc, 16, cudaMemcpyDeviceToHost, st));
     if (dL_dv0) CK(cudaMemcpyAsync(dL_dv0, gv_out, (size_t)N * 16, cudaMemcpyDeviceToHost, st));
     if (dL_dx0) CK(cudaMemcpyAsync(dL_dx0, gx_out, (size_t)N * 16, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (dL_drho0) *dL_drho0 = acc[0];
-    if (dL_deps) *dL_deps = acc[1];
+    if (dL_drho0) *dL_drho0 = (double)(long long)acc_fix[0] / kFixScalar;
+    if (dL_deps) *dL_deps = (double)(long long)acc_fix[1] / kFixScalar;
     s->last_stream = st;
     return PBD_OK;
 }
