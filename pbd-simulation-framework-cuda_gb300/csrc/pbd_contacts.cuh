@@ -26,10 +26,21 @@ struct ContactStore {
     uint32_t* list;      // M x stride partner indices, slot-major
     uint32_t* count;     // entries per particle
     uint32_t* solved;    // ceil(M / 32) x stride words: bit k of particle i = constraint (i, k) solved
-    unsigned long long* best;   // each particle's chosen constraint key (0: none)
+    unsigned long long* best;   // each particle's chosen constraint key in this batch (0: none)
+    unsigned long long* best_next;   // the next batch's keys: cleared by this batch's solve pass
+    uint32_t* long_items;   // particles with more than kClaimLong entries (any order)
+    uint32_t* long_count;   // zeroed before the frame's contact_list_kernel
     uint32_t stride;
     uint32_t M;
 };
+
+// Lanes per particle in the claim pass: entry k of a list goes to lane k mod kClaimLanes.  Lists
+// longer than kClaimLong (up to M = 512 entries where the cell-end quirk stretches a cell's
+// range, against ~26 on average) go to a whole warp in the pass's leading blocks instead, so they
+// do not hold up the pass.
+constexpr uint32_t kClaimLanes = 4;
+constexpr uint32_t kClaimLong = 64;
+constexpr uint32_t kClaimCoopBlocks = 4;
 
 __device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
     x ^= x >> 16;
@@ -99,61 +110,111 @@ contact_list_kernel(DevParams P, const float4* __restrict__ pa, const uint32_t* 
     bool deferred = false;
     walk_seq(P, scene_ctx(P, i), i, pa[i], pa, cs, ce, vis, false, &deferred);
     C.count[i] = vis.n;
+    if (vis.n > kClaimLong) C.long_items[atomicAdd(C.long_count, 1u)] = i;
 }
 
 __device__ __forceinline__ bool contact_solved(const ContactStore& C, uint32_t i, uint32_t k) {
     return (C.solved[(size_t)(k >> 5) * C.stride + i] >> (k & 31u)) & 1u;
 }
 
-// Each pending overlapping constraint offers its key to both of its particles.  Entries go in
-// batches of 4 (index loads, then position loads, in flight together); a cheap squared-distance
-// test (a superset of the overlap test, |r| < diameter) skips most entries before the exact one.
-__global__ void __launch_bounds__(256)
-contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, const float* __restrict__ w) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.N) return;
-    const uint32_t n = C.count[i];
+// Offer the keys of particle i's pending overlapping constraints k = t, t + L, t + 2L, ... (lane t
+// of L lanes) to both particles; returns the highest key offered to i itself.  Each lane takes
+// two entries per step (index loads, then position loads, in flight together, the next step's
+// indices loaded meanwhile); a cheap squared-distance test (a superset of the overlap test,
+// |r| < diameter) skips most entries before the exact one.
+template <uint32_t L>
+__device__ __forceinline__ unsigned long long claim_entries(const DevParams& P, const ContactStore& C,
+                                                            const float4* __restrict__ p, const float* __restrict__ w,
+                                                            uint32_t i, uint32_t t, uint32_t n) {
+    static_assert(L == 4 || L == 8 || L == 16 || L == 32, "lanes per particle");
+    constexpr uint32_t kStep = 2 * L;
     const float4 pi = p[i];
     const float reach2 = P.d * P.d * 1.0001f;
     const uint32_t* __restrict__ e = C.list + i;
-    uint32_t word = 0;
     unsigned long long own = 0ull;
-    uint32_t jn[4];   // the next batch's entries, loaded while this batch is tested
+    uint32_t word[2] = {0u, 0u};   // solved bits of the words holding this step's two entries
+    uint32_t jn[2];   // the next step's entries, loaded while this step is tested
 #pragma unroll
-    for (uint32_t b = 0; b < 4; ++b) jn[b] = (b < n) ? __ldcs(e + (size_t)b * C.stride) : i;
+    for (uint32_t b = 0; b < 2; ++b) jn[b] = (t + b * L < n) ? __ldcs(e + (size_t)(t + b * L) * C.stride) : i;
 #pragma unroll 1
-    for (uint32_t k0 = 0; k0 < n; k0 += 4) {
-        if ((k0 & 31u) == 0u) word = C.solved[(size_t)(k0 >> 5) * C.stride + i];
-        uint32_t j[4];
-        float4 pj[4];
+    for (uint32_t k0 = 0; k0 < n; k0 += kStep) {
+        if (kStep <= 32u) {                      // a step stays inside one 32-entry word
+            if ((k0 & 31u) == 0u) word[0] = word[1] = C.solved[(size_t)(k0 >> 5) * C.stride + i];
+        } else {                                 // 64 entries a step: entry b of a lane is in word k0/32 + b
+            word[0] = C.solved[(size_t)(k0 >> 5) * C.stride + i];
+            word[1] = (k0 + 32u < n) ? C.solved[(size_t)((k0 >> 5) + 1u) * C.stride + i] : 0u;
+        }
+        uint32_t j[2];
+        float4 pj[2];
 #pragma unroll
-        for (uint32_t b = 0; b < 4; ++b) j[b] = jn[b];
+        for (uint32_t b = 0; b < 2; ++b) j[b] = jn[b];
 #pragma unroll
-        for (uint32_t b = 0; b < 4; ++b) pj[b] = __ldg(p + j[b]);
+        for (uint32_t b = 0; b < 2; ++b) pj[b] = (k0 + t + b * L < n) ? __ldg(p + j[b]) : pi;
 #pragma unroll
-        for (uint32_t b = 0; b < 4; ++b) jn[b] = (k0 + 4 + b < n) ? __ldcs(e + (size_t)(k0 + 4 + b) * C.stride) : i;
+        for (uint32_t b = 0; b < 2; ++b) {
+            const uint32_t k = k0 + kStep + t + b * L;
+            jn[b] = (k < n) ? __ldcs(e + (size_t)k * C.stride) : i;
+        }
 #pragma unroll
-        for (uint32_t b = 0; b < 4; ++b) {
-            const uint32_t k = k0 + b;
-            if (k >= n || ((word >> (k & 31u)) & 1u)) continue;
+        for (uint32_t b = 0; b < 2; ++b) {
+            const uint32_t k = k0 + t + b * L;
+            if (k >= n || ((word[b] >> (k & 31u)) & 1u)) continue;
             const float dx = pj[b].x - pi.x, dy = pj[b].y - pi.y, dz = pj[b].z - pi.z;
             if (!(dx * dx + dy * dy + dz * dz < reach2)) continue;
             if (!contact_acts(P, w, i, j[b], contact_len(dx, dy, dz))) continue;
             const uint32_t c = i * C.M + k;
             const unsigned long long key = ((unsigned long long)lowbias32(c + 1u) << 32) | c;
-            own = key > own ? key : own;          // i's own offers: one atomic at the end
+            own = key > own ? key : own;          // i's own offers: one atomic per particle
             atomicMax(C.best + j[b], key);        // the partner's (no read first: fire and forget)
         }
     }
-    if (own) atomicMax(C.best + i, own);
+    return own;
 }
 
-// The constraint particle i took, if it is i's own and its partner took it too: solve it.
+// Maximum over groups of L lanes (L a power of two dividing 32); every lane of the warp calls it.
+template <uint32_t L>
+__device__ __forceinline__ unsigned long long group_max(unsigned long long v) {
+#pragma unroll
+    for (uint32_t s = 1; s < L; s <<= 1) {
+        const unsigned long long o = __shfl_xor_sync(0xffffffffu, v, s);
+        v = o > v ? o : v;
+    }
+    return v;
+}
+
+// Each pending overlapping constraint offers its key to both of its particles; the particle's
+// own offers are reduced over its lanes into one atomic.  The first kClaimCoopBlocks blocks take
+// the long lists, a warp each; the others take every other particle, kClaimLanes lanes each.
+__global__ void __launch_bounds__(256, 6)
+contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, const float* __restrict__ w) {
+    if (blockIdx.x < kClaimCoopBlocks) {
+        const uint32_t nl = *C.long_count;
+        const uint32_t wpb = blockDim.x >> 5, lane = threadIdx.x & 31u;
+        for (uint32_t q = blockIdx.x * wpb + (threadIdx.x >> 5); q < nl; q += kClaimCoopBlocks * wpb) {
+            const uint32_t i = C.long_items[q];
+            const unsigned long long own = group_max<32>(claim_entries<32>(P, C, p, w, i, lane, C.count[i]));
+            if (lane == 0 && own) atomicMax(C.best + i, own);
+        }
+        return;
+    }
+    constexpr uint32_t L = kClaimLanes;
+    const uint32_t i = (blockIdx.x - kClaimCoopBlocks) * (blockDim.x / L) + threadIdx.x / L, t = threadIdx.x % L;
+    uint32_t n = i < P.N ? C.count[i] : 0u;
+    if (n > kClaimLong) n = 0u;                  // a long list: a leading block's warp takes it
+    // no early exit: the lanes meet in the shuffles below
+    const unsigned long long own = group_max<L>(n ? claim_entries<L>(P, C, p, w, i, t, n) : 0ull);
+    if (t == 0 && own) atomicMax(C.best + i, own);
+}
+
+// The constraint particle i took, if it is i's own and its partner took it too: solve it.  Also
+// clears i's key for the next batch (that buffer was the previous batch's and is read by no one
+// here).
 __global__ void __launch_bounds__(256)
 contact_solve_kernel(DevParams P, ContactStore C, float4* __restrict__ p, float4* __restrict__ x,
                      const float* __restrict__ w) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
+    C.best_next[i] = 0ull;
     const unsigned long long key = C.best[i];
     if (key == 0ull) return;
     const uint32_t c = (uint32_t)key;

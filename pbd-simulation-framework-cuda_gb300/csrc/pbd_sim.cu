@@ -369,10 +369,13 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const bool batched_contacts = prm.collision_type == 1;
     if (batched_contacts) {   // every list entry of the frame is a constraint (Fluid.cu:37-47)
         PROF_BEGIN("contact_list");
+        cudaMemsetAsync(s->ct.long_count, 0, 4, st);
         contact_list_kernel<<<div_up(N, kThreadsParticle), kThreadsParticle, 0, st>>>(P, pa, s->cell_start, s->cell_end, s->ct);
         PROF_END();
         ++nl;
+        cudaMemsetAsync(s->ct.best, 0, (size_t)N * 8, st);   // the frame's first batch's keys
     }
+    uint32_t nbatch = 0;   // contact batches so far in this frame: their keys alternate buffers
     bool last_was_delta = false;
     for (uint32_t it = 0; it < I; ++it) {
         if (tape && it < (uint32_t)kMaxTapeIters)
@@ -422,14 +425,17 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
                 PROF_END();
                 cur.p = pout;
             }
-            const ContactStore& C = s->ct;
+            // the batches' keys alternate between two buffers; each solve pass clears the other
+            ContactStore C = s->ct;
+            unsigned long long* const keys[2] = {s->ct.best, s->ct.best + s->ct.stride};
             const size_t words = (C.M + 31) / 32;
             for (uint32_t k = 0; k < Sx; ++k) {
                 PROF_BEGIN("contact_batches");
                 cudaMemsetAsync(C.solved, 0, words * C.stride * 4, st);
-                for (uint32_t b = 0; b < prm.max_collision_batches; ++b) {
-                    cudaMemsetAsync(C.best, 0, (size_t)N * 8, st);
-                    contact_claim_kernel<<<div_up(N, kThreadsParticle), kThreadsParticle, 0, st>>>(P, C, s->p[cur.p], wf);
+                for (uint32_t b = 0; b < prm.max_collision_batches; ++b, ++nbatch) {
+                    C.best = keys[nbatch & 1u];
+                    C.best_next = keys[(nbatch + 1u) & 1u];
+                    contact_claim_kernel<<<kClaimCoopBlocks + div_up(N, kThreadsParticle / kClaimLanes), kThreadsParticle, 0, st>>>(P, C, s->p[cur.p], wf);
                     contact_solve_kernel<<<div_up(N, kThreadsParticle), kThreadsParticle, 0, st>>>(P, C, s->p[cur.p], s->x[cur.x], wf);
                     nl += 2;
                 }
@@ -653,7 +659,7 @@ int ensure_contacts(pbd_sim* s) {
         return PBD_ERR_UNSUPPORTED;
     }
     const size_t need = ((C * M * 4 + 255) & ~size_t(255)) + ((C * 4 + 255) & ~size_t(255)) +
-                        ((C * W * 4 + 255) & ~size_t(255)) + C * 8 + 256;
+                        ((C * W * 4 + 255) & ~size_t(255)) + C * 16 + ((C * 4 + 255) & ~size_t(255)) + 256 + 256;
     if (s->ct_arena && s->ct_bytes >= need && s->ct.M == M) return PBD_OK;
     if (s->ct_arena) {
         cudaDeviceSynchronize();
@@ -669,7 +675,10 @@ int ensure_contacts(pbd_sim* s) {
     s->ct.list = (uint32_t*)take(C * M * 4);
     s->ct.count = (uint32_t*)take(C * 4);
     s->ct.solved = (uint32_t*)take(C * W * 4);
-    s->ct.best = (unsigned long long*)take(C * 8);
+    s->ct.best = (unsigned long long*)take(C * 16);   // two buffers of C keys
+    s->ct.best_next = s->ct.best + C;
+    s->ct.long_items = (uint32_t*)take(C * 4);
+    s->ct.long_count = (uint32_t*)take(4);
     s->ct.stride = (uint32_t)C;
     s->ct.M = (uint32_t)M;
     return PBD_OK;

@@ -89,6 +89,22 @@ def test_gpu_contact_batches_match_oracle(need_gpu, pbd, scenes, oracle_mod, fra
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("density", [True, False])
+def test_gpu_contact_batches_long_lists(need_gpu, pbd, scenes, oracle_mod, density):
+    """a packed block (~8 particles per cell): most lists hold more than 64 entries, which the
+    claim pass hands to whole warps"""
+    p, pos, vel = contact_scene(pbd, scenes, shape=(9, 8, 9), spacing=0.45, density=density)
+    sim, orc = setup_pair(pbd, oracle_mod, p, pos, vel)
+    sim.step(1)
+    orc.step(1)
+    _, cnt, _ = sim.neighbours(512)
+    assert (cnt > 64).mean() > 0.5 and (cnt <= 64).sum() > 0
+    g, o = by_id(sim.state()), by_id(orc.state())
+    assert maxdiff(g["x"][:, :3], o["x"][:, :3]) <= TOL_X1
+    assert maxdiff(g["v"][:, :3], o["v"][:, :3]) <= TOL_X1 * 100
+
+
+@pytest.mark.gpu
 def test_gpu_contact_batches_on_isolated_pairs(need_gpu, pbd, scenes):
     p, pos, vel = pair_scene(pbd, scenes)
     sim = pbd.Sim(p, len(pos)); sim.add_particles(pos, vel); sim.step(1)
