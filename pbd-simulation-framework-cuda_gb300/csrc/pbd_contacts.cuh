@@ -38,7 +38,8 @@ struct ContactStore {
 // longer than kClaimLong (up to M = 512 entries where the cell-end quirk stretches a cell's
 // range, against ~26 on average) go to a whole warp in the pass's leading blocks instead, so they
 // do not hold up the pass.
-constexpr uint32_t kClaimLanes = 4;
+constexpr uint32_t kClaimLanes = 1;
+constexpr uint32_t kClaimBatch = 4;    // entries per lane per step
 constexpr uint32_t kClaimLong = 64;
 constexpr uint32_t kClaimCoopBlocks = 4;
 
@@ -113,50 +114,54 @@ contact_list_kernel(DevParams P, const float4* __restrict__ pa, const uint32_t* 
     if (vis.n > kClaimLong) C.long_items[atomicAdd(C.long_count, 1u)] = i;
 }
 
-__device__ __forceinline__ bool contact_solved(const ContactStore& C, uint32_t i, uint32_t k) {
-    return (C.solved[(size_t)(k >> 5) * C.stride + i] >> (k & 31u)) & 1u;
-}
-
 // Offer the keys of particle i's pending overlapping constraints k = t, t + L, t + 2L, ... (lane t
-// of L lanes) to both particles; returns the highest key offered to i itself.  Each lane takes
-// two entries per step (index loads, then position loads, in flight together, the next step's
+// of L lanes) to both particles; returns the highest key offered to i itself.  Each lane takes B
+// entries per step (index loads, then position loads, in flight together, the next step's
 // indices loaded meanwhile); a cheap squared-distance test (a superset of the overlap test,
 // |r| < diameter) skips most entries before the exact one.
-template <uint32_t L>
+template <uint32_t L, uint32_t B>
 __device__ __forceinline__ unsigned long long claim_entries(const DevParams& P, const ContactStore& C,
                                                             const float4* __restrict__ p, const float* __restrict__ w,
                                                             uint32_t i, uint32_t t, uint32_t n) {
-    static_assert(L == 4 || L == 8 || L == 16 || L == 32, "lanes per particle");
-    constexpr uint32_t kStep = 2 * L;
+    constexpr uint32_t kStep = B * L;
+    static_assert((kStep <= 32u && (32u % kStep) == 0u) || (L == 32u && B == 2u), "a step's solved words");
     const float4 pi = p[i];
     const float reach2 = P.d * P.d * 1.0001f;
     const uint32_t* __restrict__ e = C.list + i;
     unsigned long long own = 0ull;
-    uint32_t word[2] = {0u, 0u};   // solved bits of the words holding this step's two entries
-    uint32_t jn[2];   // the next step's entries, loaded while this step is tested
+    uint32_t word[B];   // solved bits of the word holding each of this step's entries
+    uint32_t jn[B];     // the next step's entries, loaded while this step is tested
 #pragma unroll
-    for (uint32_t b = 0; b < 2; ++b) jn[b] = (t + b * L < n) ? __ldcs(e + (size_t)(t + b * L) * C.stride) : i;
+    for (uint32_t b = 0; b < B; ++b) {
+        word[b] = 0u;
+        jn[b] = (t + b * L < n) ? __ldcs(e + (size_t)(t + b * L) * C.stride) : i;
+    }
 #pragma unroll 1
     for (uint32_t k0 = 0; k0 < n; k0 += kStep) {
         if (kStep <= 32u) {                      // a step stays inside one 32-entry word
-            if ((k0 & 31u) == 0u) word[0] = word[1] = C.solved[(size_t)(k0 >> 5) * C.stride + i];
+            if ((k0 & 31u) == 0u) {
+                const uint32_t v = C.solved[(size_t)(k0 >> 5) * C.stride + i];
+#pragma unroll
+                for (uint32_t b = 0; b < B; ++b) word[b] = v;
+            }
         } else {                                 // 64 entries a step: entry b of a lane is in word k0/32 + b
-            word[0] = C.solved[(size_t)(k0 >> 5) * C.stride + i];
-            word[1] = (k0 + 32u < n) ? C.solved[(size_t)((k0 >> 5) + 1u) * C.stride + i] : 0u;
+#pragma unroll
+            for (uint32_t b = 0; b < B; ++b)
+                word[b] = (k0 + b * 32u < n) ? C.solved[(size_t)((k0 >> 5) + b) * C.stride + i] : 0u;
         }
-        uint32_t j[2];
-        float4 pj[2];
+        uint32_t j[B];
+        float4 pj[B];
 #pragma unroll
-        for (uint32_t b = 0; b < 2; ++b) j[b] = jn[b];
+        for (uint32_t b = 0; b < B; ++b) j[b] = jn[b];
 #pragma unroll
-        for (uint32_t b = 0; b < 2; ++b) pj[b] = (k0 + t + b * L < n) ? __ldg(p + j[b]) : pi;
+        for (uint32_t b = 0; b < B; ++b) pj[b] = (k0 + t + b * L < n) ? __ldg(p + j[b]) : pi;
 #pragma unroll
-        for (uint32_t b = 0; b < 2; ++b) {
+        for (uint32_t b = 0; b < B; ++b) {
             const uint32_t k = k0 + kStep + t + b * L;
             jn[b] = (k < n) ? __ldcs(e + (size_t)k * C.stride) : i;
         }
 #pragma unroll
-        for (uint32_t b = 0; b < 2; ++b) {
+        for (uint32_t b = 0; b < B; ++b) {
             const uint32_t k = k0 + t + b * L;
             if (k >= n || ((word[b] >> (k & 31u)) & 1u)) continue;
             const float dx = pj[b].x - pi.x, dy = pj[b].y - pi.y, dz = pj[b].z - pi.z;
@@ -192,7 +197,7 @@ contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, 
         const uint32_t wpb = blockDim.x >> 5, lane = threadIdx.x & 31u;
         for (uint32_t q = blockIdx.x * wpb + (threadIdx.x >> 5); q < nl; q += kClaimCoopBlocks * wpb) {
             const uint32_t i = C.long_items[q];
-            const unsigned long long own = group_max<32>(claim_entries<32>(P, C, p, w, i, lane, C.count[i]));
+            const unsigned long long own = group_max<32>(claim_entries<32, 2>(P, C, p, w, i, lane, C.count[i]));
             if (lane == 0 && own) atomicMax(C.best + i, own);
         }
         return;
@@ -202,13 +207,14 @@ contact_claim_kernel(DevParams P, ContactStore C, const float4* __restrict__ p, 
     uint32_t n = i < P.N ? C.count[i] : 0u;
     if (n > kClaimLong) n = 0u;                  // a long list: a leading block's warp takes it
     // no early exit: the lanes meet in the shuffles below
-    const unsigned long long own = group_max<L>(n ? claim_entries<L>(P, C, p, w, i, t, n) : 0ull);
+    const unsigned long long own = group_max<L>(n ? claim_entries<L, kClaimBatch>(P, C, p, w, i, t, n) : 0ull);
     if (t == 0 && own) atomicMax(C.best + i, own);
 }
 
-// The constraint particle i took, if it is i's own and its partner took it too: solve it.  Also
-// clears i's key for the next batch (that buffer was the previous batch's and is read by no one
-// here).
+// A constraint both of whose particles took it is solved by its partner's thread: the key holds
+// the constraint c = a * M + k, so the partner finds the owner a without reading the list.  Each
+// thread also clears its particle's key for the next batch (that buffer was the previous batch's
+// and is read by no one here).
 __global__ void __launch_bounds__(256)
 contact_solve_kernel(DevParams P, ContactStore C, float4* __restrict__ p, float4* __restrict__ x,
                      const float* __restrict__ w) {
@@ -218,23 +224,22 @@ contact_solve_kernel(DevParams P, ContactStore C, float4* __restrict__ p, float4
     const unsigned long long key = C.best[i];
     if (key == 0ull) return;
     const uint32_t c = (uint32_t)key;
-    if (c / C.M != i) return;
-    const uint32_t k = c - i * C.M;
-    const uint32_t j = C.list[(size_t)k * C.stride + i];
-    if (C.best[j] != key) return;
-    C.solved[(size_t)(k >> 5) * C.stride + i] |= 1u << (k & 31u);   // only this thread writes i's words
+    const uint32_t a = c / C.M;                  // the owner; i is its partner unless a == i
+    if (a == i || C.best[a] != key) return;
+    const uint32_t k = c - a * C.M;
+    C.solved[(size_t)(k >> 5) * C.stride + a] |= 1u << (k & 31u);   // a is in one solved constraint
     float4 n;
     float h1, h2;
-    if (!contact_geometry(P, p, w, i, j, n, h1, h2)) return;
+    if (!contact_geometry(P, p, w, a, i, n, h1, h2)) return;
     const float om = P.one_minus_stiffness;
     const float4 a1 = make_float4(-n.x * h1 * om, -n.y * h1 * om, -n.z * h1 * om, -n.w * h1 * om);
     const float4 a2 = make_float4(n.x * h2 * om, n.y * h2 * om, n.z * h2 * om, n.w * h2 * om);
-    const float4 p1 = p[i], p2 = p[j];
-    p[i] = make_float4(p1.x + a1.x, p1.y + a1.y, p1.z + a1.z, 0.f + a1.w);
-    p[j] = make_float4(p2.x + a2.x, p2.y + a2.y, p2.z + a2.z, 0.f + a2.w);
-    const float4 x1 = x[i], x2 = x[j];
-    x[i] = make_float4(x1.x + a1.x, x1.y + a1.y, x1.z + a1.z, x1.w + a1.w);
-    x[j] = make_float4(x2.x + a2.x, x2.y + a2.y, x2.z + a2.z, x2.w + a2.w);
+    const float4 p1 = p[a], p2 = p[i];
+    p[a] = make_float4(p1.x + a1.x, p1.y + a1.y, p1.z + a1.z, 0.f + a1.w);
+    p[i] = make_float4(p2.x + a2.x, p2.y + a2.y, p2.z + a2.z, 0.f + a2.w);
+    const float4 x1 = x[a], x2 = x[i];
+    x[a] = make_float4(x1.x + a1.x, x1.y + a1.y, x1.z + a1.z, x1.w + a1.w);
+    x[i] = make_float4(x2.x + a2.x, x2.y + a2.y, x2.z + a2.z, x2.w + a2.w);
 }
 
 }  // namespace pbd
