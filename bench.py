@@ -104,11 +104,14 @@ def bench_out_dir():
 
 
 class ClockSampler:
-    """nvidia-smi samples (200 ms) during the timed region."""
+    """nvidia-smi samples (every 100 ms) during the timed region: entering waits for the first
+    sample, which is left out of the summary, so every sample counted was taken inside the
+    region."""
 
     def __init__(self, index):
         self.index = index
         self.proc = None
+        self.skip = 0
         # PBD_BENCH_OUT keeps the samples (and the autotuner's cache) in a folder of the caller's
         # choosing; by default they go to a temporary folder
         self.path = os.path.join(bench_out_dir(), f"clocks_{os.getpid()}.csv")
@@ -122,7 +125,12 @@ class ClockSampler:
                  "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
                  "clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 5.0 and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+                time.sleep(0.01)
+            with open(self.path) as f:
+                self.skip = len(f.readlines())
         except Exception:
             self.proc = None
         return self
@@ -142,7 +150,7 @@ class ClockSampler:
         sms, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         try:
-            for line in open(self.path):
+            for line in open(self.path).readlines()[self.skip:]:
                 f = [t.strip() for t in line.split(",")]
                 if len(f) < 7:
                     continue
@@ -616,7 +624,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fluid_1m")
