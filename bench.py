@@ -1,6 +1,7 @@
 """Benchmark of the GB300 PBD step: particle-steps/s on the 1M-particle fluid workload.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
+                    [--leg contacts|batched|solids|adjoint]
 
 Our arm (default): 100^3 = 1,000,000 fluid particles in a 128^3-cell domain (seed 2),
 4 solver iterations, vorticity 5e-4, XSPH viscosity 0.01, FP32.  `value` is particle-steps/s
@@ -621,6 +622,25 @@ def run_ours(args):
     return 0
 
 
+def run_leg(args):
+    """One secondary workload alone, e.g. as the target of a profiler."""
+    import torch
+    import pbd
+    import scenes
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    if args.leg == "contacts":
+        out = run_contacts(torch, pbd, scenes, stream, sh, frames=max(3, min(args.steps, 20)))
+    elif args.leg == "batched":
+        out = run_batched(torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 60)))
+    elif args.leg == "solids":
+        out = run_solids(torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 100)))
+    else:
+        out = run_adjoint(torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check)
+    print(json.dumps({"leg": args.leg, **out}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -630,9 +650,13 @@ def main():
     ap.add_argument("--workload", default="fluid_1m")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-fd-check", action="store_true", help="skip the FP64 finite-difference check of the adjoint")
+    ap.add_argument("--leg", choices=["contacts", "batched", "solids", "adjoint"],
+                    help="measure only this secondary workload and print its result (not the bench line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.leg:
+        return run_leg(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
