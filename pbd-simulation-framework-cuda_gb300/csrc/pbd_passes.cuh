@@ -1084,11 +1084,13 @@ using VortViscVisit = VortViscVisitT<3u>;
 
 // The vorticity force from the vorticity sums of `vo` and the viscosity update from the sums of
 // `vs` (the same visitor when one walk summed both terms).  Explicitly rounded, so every kernel
-// that finishes a particle stores the same bits.
+// that finishes a particle stores the same bits.  `vhost` (mapped pinned host memory, or null)
+// also receives the new velocity: a frame that reads its state back gets v without a copy after
+// the pass.
 template <class VO, class VS>
 __device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i, const VO& vo, const VS& vs,
                                                  float4* __restrict__ vout, float4* __restrict__ fext,
-                                                 const float* __restrict__ w) {
+                                                 const float* __restrict__ w, float4* __restrict__ vhost = nullptr) {
     if (vo.vort) {
         const float EPS = 0.00000001f;
         const float gl = sqrtf(__fmaf_rn(vo.gz, vo.gz, __fmaf_rn(vo.gy, vo.gy, __fmul_rn(vo.gx, vo.gx))));
@@ -1104,8 +1106,10 @@ __device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i,
     if (vs.visc) {
         const float c = w ? __fmul_rn(w[i], P.c_visc) : P.c_visc;   // a solid keeps its velocity
         const float4 vi = vs.vi;
-        vout[i] = make_float4(__fmaf_rn(c, vs.sx, vi.x), __fmaf_rn(c, vs.sy, vi.y), __fmaf_rn(c, vs.sz, vi.z),
-                              __fmaf_rn(c, vs.sw, vi.w));
+        const float4 vn = make_float4(__fmaf_rn(c, vs.sx, vi.x), __fmaf_rn(c, vs.sy, vi.y), __fmaf_rn(c, vs.sz, vi.z),
+                                      __fmaf_rn(c, vs.sw, vi.w));
+        vout[i] = vn;
+        if (vhost) vhost[i] = vn;
     }
 }
 
@@ -1134,12 +1138,13 @@ __device__ __noinline__ void coop_vort_visc(const DevParams& P, const float4* __
                                                const float4* __restrict__ vin, float4* __restrict__ vout,
                                                const float4* __restrict__ omega, float4* __restrict__ fext,
                                                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
-                                               int do_vort, int do_visc, const float* __restrict__ w, uint32_t i) {
+                                               int do_vort, int do_visc, const float* __restrict__ w, uint32_t i,
+                                               float4* __restrict__ vhost) {
     const float4 oi = do_vort ? omega[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const SceneCtx S = scene_ctx(P, i);
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
     walk_coop(P, S, i, pa[i], p, cs, ce, vis);
-    if (lane_id() == 0) vort_visc_finish(P, i, vis, vis, vout, fext, w);
+    if (lane_id() == 0) vort_visc_finish(P, i, vis, vis, vout, fext, w, vhost);
 }
 
 // vorticity + viscosity over a stored list (the full list with vorticity, else the omega pass's
@@ -1151,9 +1156,12 @@ __global__ void __launch_bounds__(256, 5)
 vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
                       const float4* __restrict__ vin, float4* __restrict__ vout, const float4* __restrict__ omega,
                       float4* __restrict__ fext, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
-                      int do_vort, int do_visc, const float* __restrict__ w, CoopSet C, NbList Lv, NbList Ln) {
+                      int do_vort, int do_visc, const float* __restrict__ w, CoopSet C, NbList Lv, NbList Ln,
+                      float4* __restrict__ vhost) {
     if (blockIdx.x < C.blocks) {
-        run_coop_set(C, [&](uint32_t i) { coop_vort_visc(P, p, pa, vin, vout, omega, fext, cs, ce, do_vort, do_visc, w, i); });
+        run_coop_set(C, [&](uint32_t i) {
+            coop_vort_visc(P, p, pa, vin, vout, omega, fext, cs, ce, do_vort, do_visc, w, i, vhost);
+        });
         return;
     }
     const uint32_t i = (blockIdx.x - C.blocks) * blockDim.x + threadIdx.x;
@@ -1167,12 +1175,12 @@ vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* _
         walk_list<false, 2>(Lv, i, meta, p, vo);   // position + omega per entry: batches of 2 fit the registers
         VortViscVisitT<2u> vs(P, vin, omega, p[i], vin[i], oi, false, true);
         walk_near(Ln, i, nm, p, vs);
-        vort_visc_finish(P, i, vo, vs, vout, fext, w);
+        vort_visc_finish(P, i, vo, vs, vout, fext, w, vhost);
         return;
     }
     VortViscVisit vis(P, vin, omega, p[i], vin[i], oi, do_vort != 0, do_visc != 0);
     walk_list<false, 2>(Lv, i, meta, p, vis);
-    vort_visc_finish(P, i, vis, vis, vout, fext, w);
+    vort_visc_finish(P, i, vis, vis, vout, fext, w, vhost);
 }
 
 __global__ void __launch_bounds__(128)
@@ -1181,7 +1189,7 @@ vort_visc_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* _
                       const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, int do_vort, int do_visc,
                       const float* __restrict__ w, DeferList D) {
     for_each_deferred(D, [&](uint32_t i) {
-        coop_vort_visc(P, p, pa, vin, vout, omega, fext, cs, ce, do_vort, do_visc, w, i);
+        coop_vort_visc(P, p, pa, vin, vout, omega, fext, cs, ce, do_vort, do_visc, w, i, nullptr);
     });
 }
 

@@ -141,9 +141,11 @@ struct pbd_sim {
     Cur exec_end[kMaxGraphs];
     int nexec = 0;
     // pbd_step_readback: pinned host copies of x and v (2 x capacity float4, allocated on first
-    // use), a side stream for the position copy, and frame graphs (one per entry of exec) that
-    // copy the positions beside the frame's omega / vorticity / viscosity passes
+    // use; rb_dev is the same memory as the device addresses it), a side stream for the position
+    // copy, and frame graphs (one per entry of exec) that copy the positions beside the frame's
+    // omega / vorticity / viscosity passes
     float4* rb_host = nullptr;
+    float4* rb_dev = nullptr;
     cudaStream_t rb_stream = nullptr;
     cudaEvent_t rb_fork = nullptr, rb_join = nullptr;
     cudaGraphExec_t rb_exec[kMaxGraphs]{};
@@ -282,7 +284,9 @@ static void launch_delta_list(uint32_t gn, int tn, cudaStream_t st, const DevPar
 
 // Record (or run) one frame of Fluid::compute (Fluid.cu:14-97) on `st`.
 // readback: copy the final positions to s->rb_host on s->rb_stream once they are final (beside
-// the frame's remaining passes) and the final velocities at the end of the frame.
+// the frame's remaining passes); the final velocities go with them when viscosity does not
+// change them, else the viscosity pass over the lists stores them into s->rb_host itself (other
+// paths copy them at the end of the frame).
 cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only, uint32_t& nl,
                           Profiler* prof = nullptr, const Tape* tape = nullptr, bool readback = false) {
     const DevParams P = make_dev_params(s);
@@ -501,13 +505,18 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         PROF_END();
         ++nl;
     }
-    if (readback) {   // x is final: copy it while omega, vorticity and viscosity run
+    const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
+    bool v_read = false;   // the frame's final velocities are on their way to s->rb_host
+    if (readback) {   // x (and v, unless viscosity follows) is final: copy it while the last passes run
         cudaEventRecord(s->rb_fork, st);
         cudaStreamWaitEvent(s->rb_stream, s->rb_fork, 0);
         cudaMemcpyAsync(s->rb_host, s->x[cur.x], (size_t)N * 16, cudaMemcpyDeviceToHost, s->rb_stream);
+        if (!visc) {
+            cudaMemcpyAsync(s->rb_host + s->cap, s->v[cur.v], (size_t)N * 16, cudaMemcpyDeviceToHost, s->rb_stream);
+            v_read = true;
+        }
         cudaEventRecord(s->rb_join, s->rb_stream);
     }
-    const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     if (act & PBD_ACTIVE_COMPUTE_OMEGAS) {
         PROF_BEGIN(use_full ? "omega_list" : "omega");
         // near lists for viscosity: read by viscosity alone, or beside the full list for vorticity
@@ -532,9 +541,11 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         const NbList Ln = (vort && use_full && (act & PBD_ACTIVE_COMPUTE_OMEGAS)) ? L : L0;
         PROF_BEGIN(Lv.list ? "vort_visc_list" : "vort_visc");
         if (Lv.list) {
+            float4* const vh = (readback && visc) ? s->rb_dev + s->cap : nullptr;
             vort_visc_list_kernel<<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
                                                                    s->fext, s->cell_start, s->cell_end, vort, visc, wf,
-                                                                   vort ? CF : CN, Lv, Ln);
+                                                                   vort ? CF : CN, Lv, Ln, vh);
+            v_read = v_read || vh != nullptr;
             nl += 1;
         } else {
             vort_visc_kernel<<<gn, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega, s->fext,
@@ -547,7 +558,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         if (visc) cur.v ^= 1;
     }
     if (readback) {
-        cudaMemcpyAsync(s->rb_host + s->cap, s->v[cur.v], (size_t)N * 16, cudaMemcpyDeviceToHost, st);
+        if (!v_read) cudaMemcpyAsync(s->rb_host + s->cap, s->v[cur.v], (size_t)N * 16, cudaMemcpyDeviceToHost, st);
         cudaStreamWaitEvent(st, s->rb_join, 0);
     }
     return cudaGetLastError();
@@ -936,7 +947,8 @@ int pbd_step_readback(pbd_sim* s, int nsteps, void* stream, const float** pos4, 
     if (nsteps < 1) { set_error("pbd_step_readback: nsteps < 1"); return PBD_ERR_INVALID_ARG; }
     if (s->batched) { set_error("pbd_step_readback: a batch reads its scenes with pbd_batch_get_state"); return PBD_ERR_INVALID_ARG; }
     if (!s->rb_host) {
-        CK(cudaHostAlloc((void**)&s->rb_host, (size_t)2 * s->cap * 16, cudaHostAllocDefault));
+        CK(cudaHostAlloc((void**)&s->rb_host, (size_t)2 * s->cap * 16, cudaHostAllocMapped));
+        CK(cudaHostGetDevicePointer((void**)&s->rb_dev, s->rb_host, 0));
         CK(cudaStreamCreateWithFlags(&s->rb_stream, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&s->rb_fork, cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&s->rb_join, cudaEventDisableTiming));

@@ -160,10 +160,11 @@ def test_block_size_leaves_results_unchanged(need_gpu, pbd, scenes, tmp_path):
         _same(states[0], st)
 
 
-@pytest.mark.parametrize("vort,visc", [(0.0, 0.0), (0.0005, 0.01)])
+@pytest.mark.parametrize("vort,visc", [(0.0, 0.0), (0.0005, 0.01), (0.0005, 0.0), (0.0, 0.01)])
 def test_step_readback_matches_step_and_get_state(need_gpu, pbd, scenes, vort, visc):
-    """pbd_step_readback (positions copied beside the last passes) returns the state pbd_step +
-    pbd_get_state return, and the simulation continues from it identically"""
+    """pbd_step_readback (positions, and velocities that viscosity leaves alone, copied beside the
+    last passes; velocities that viscosity changes stored into host memory by that pass) returns
+    the state pbd_step + pbd_get_state return, and the simulation continues from it identically"""
     params = scenes.workload_params(pbd, 32, 1000.0, vorticity=vort, viscosity=visc)
     params.lambda_epsilon = 0.1
     params.flags |= pbd.FLAG_TRACK_IDS
