@@ -176,7 +176,8 @@ int pbd_get_state(pbd_sim* sim, float* pos4, float* vel4, float* pred4, uint32_t
  * positions and velocities of the final state, in host memory the library owns (pinned; valid
  * until the next pbd_step_readback, pbd_destroy or a pbd_add_particles from these same arrays
  * is complete): the position copy runs beside the last frame's omega / vorticity / viscosity
- * passes.  Synchronous.  nsteps >= 1; with no particles the arrays are returned unchanged. */
+ * passes, and the viscosity pass stores the final velocities into that memory itself.
+ * Synchronous.  nsteps >= 1; with no particles the arrays are returned unchanged. */
 int pbd_step_readback(pbd_sim* sim, int nsteps, void* stream, const float** pos4, const float** vel4);
 /* Device pointers of the current state buffers (valid until the next pbd_step/add/clear). */
 int pbd_get_device_state(pbd_sim* sim, const float** d_pos4, const float** d_vel4,
