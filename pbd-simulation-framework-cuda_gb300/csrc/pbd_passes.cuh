@@ -1056,9 +1056,10 @@ struct VortViscVisitT {
             const float4 oj = ex.oj;
             const float dx = oj.x - oi.x, dy = oj.y - oi.y, dz = oj.z - oi.z;
             const float ol = sqrtf(dx * dx + dy * dy + dz * dz);
-            c.gx = ol / ((pj.x - pi.x) + 0.00000001f);
-            c.gy = ol / ((pj.y - pi.y) + 0.00000001f);
-            c.gz = ol / ((pj.z - pi.z) + 0.00000001f);
+            // the fast division: the divisors (position differences + 1e-8) stay far below 2^126
+            c.gx = __fdividef(ol, (pj.x - pi.x) + 0.00000001f);
+            c.gy = __fdividef(ol, (pj.y - pi.y) + 0.00000001f);
+            c.gz = __fdividef(ol, (pj.z - pi.z) + 0.00000001f);
             c.flags |= 1u;
         }
         if constexpr ((kTerms & 2u) != 0u) if (visc) {
