@@ -67,8 +67,10 @@ def test_oracle_batches_on_isolated_pairs(pbd, scenes, oracle_mod, batches, expe
     assert np.allclose(0.5 * (x[0::2, :3] + x[1::2, :3]), mid0, atol=1e-5)   # equal and opposite moves
 
 
-def test_oracle_precisions_agree(pbd, scenes, oracle_mod):
-    p, pos, vel = contact_scene(pbd, scenes)
+@pytest.mark.parametrize("shape,spacing", [((10, 8, 10), 0.8), ((9, 8, 9), 0.45)])
+def test_oracle_precisions_agree(pbd, scenes, oracle_mod, shape, spacing):
+    """FP32 and FP64 oracles agree, also on a packed block whose lists mostly exceed 64 entries"""
+    p, pos, vel = contact_scene(pbd, scenes, shape=shape, spacing=spacing)
     a = oracle_mod.Oracle(p, len(pos), "f32"); a.add_particles(pos, vel); a.step(1)
     b = oracle_mod.Oracle(p, len(pos), "f64"); b.add_particles(pos, vel); b.step(1)
     sa, sb = by_id(a.state()), by_id(b.state())
