@@ -101,17 +101,38 @@ struct ContactListVisit {
     __device__ __forceinline__ void add(const Contrib& c, bool) { list[(size_t)n * stride + i] = c.j; ++n; }
 };
 
-// After the re-order: each particle's constraint list (the walk stops at the cap M itself).
+__device__ __forceinline__ void contact_list_done(const ContactStore& C, uint32_t i, uint32_t n) {
+    C.count[i] = n;
+    if (n > kClaimLong) C.long_items[atomicAdd(C.long_count, 1u)] = i;
+}
+
+// After the re-order: each particle's constraint list (the walk stops at the cap M itself).  A
+// particle whose walk meets a cell range longer than one thread's walk takes is listed again by
+// a warp of its block (walk_coop: the same entries in the same order) once the block's threads
+// are done.  Blocks of 256 threads.
 __global__ void __launch_bounds__(256)
 contact_list_kernel(DevParams P, const float4* __restrict__ pa, const uint32_t* __restrict__ cs,
                     const uint32_t* __restrict__ ce, ContactStore C) {
+    __shared__ uint32_t left[256];
+    __shared__ uint32_t nleft;
+    if (threadIdx.x == 0) nleft = 0u;
+    __syncthreads();
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.N) return;
-    ContactListVisit vis(C.list, C.stride, i);
-    bool deferred = false;
-    walk_seq(P, scene_ctx(P, i), i, pa[i], pa, cs, ce, vis, false, &deferred);
-    C.count[i] = vis.n;
-    if (vis.n > kClaimLong) C.long_items[atomicAdd(C.long_count, 1u)] = i;
+    if (i < P.N) {
+        ContactListVisit vis(C.list, C.stride, i);
+        bool deferred = false;
+        walk_seq(P, scene_ctx(P, i), i, pa[i], pa, cs, ce, vis, true, &deferred);
+        if (deferred) left[atomicAdd(&nleft, 1u)] = i;
+        else contact_list_done(C, i, vis.n);
+    }
+    __syncthreads();
+    const uint32_t nl = nleft;
+    for (uint32_t k = threadIdx.x >> 5; k < nl; k += blockDim.x >> 5) {
+        const uint32_t q = left[k];
+        ContactListVisit vis(C.list, C.stride, q);
+        walk_coop(P, scene_ctx(P, q), q, pa[q], pa, cs, ce, vis);
+        if (lane_id() == 0) contact_list_done(C, q, vis.n);
+    }
 }
 
 // Offer the keys of particle i's pending overlapping constraints k = t, t + L, t + 2L, ... (lane t
