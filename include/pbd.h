@@ -260,6 +260,13 @@ int pbd_batch_profile_frames(pbd_batch* batch, int nsteps, void* stream, pbd_ker
  * the mean and maximum of |C_i| (nullable).  Needs a frame since the last add/clear
  * (PBD_ERR_INVALID_ARG otherwise); synchronises. */
 int pbd_density_error(pbd_sim* sim, float* err, double* mean_abs, double* max_abs, void* stream);
+/* The same C_i, averaged over the interior particles only: those whose list (the last frame's)
+ * holds at least `min_neighbours` entries and whose current position lies more than `margin`
+ * inside the enclosure on every axis -- the particles whose kernel support is filled with fluid
+ * rather than cut by the free surface or a wall.  `counted` receives how many there were.
+ * No counterpart in the reference; synchronises. */
+int pbd_density_error_interior(pbd_sim* sim, uint32_t min_neighbours, float margin, double* mean_abs,
+                               double* max_abs, uint32_t* counted, void* stream);
 
 /* ---- headless particle sprites -------------------------------------------------------- */
 /* The reference draws each particle as a shaded sphere sprite through OpenGL

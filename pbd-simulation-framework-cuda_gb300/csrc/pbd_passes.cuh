@@ -847,10 +847,11 @@ __device__ __noinline__ void coop_delta(const DevParams& P, uint32_t mode, const
     if (lane_id() == 0) delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
 }
 
-// delta pass 0 of an iteration over the near lists its lambda pass recorded; the particles
-// without one (the set C, which the leading blocks empty) walk the cells.  kMode != 0: the pass
+// delta pass 0 of an iteration over the near lists its lambda pass recorded (kB = kNearBatch), or
+// any delta pass over the frame's full list when there are no near lists (kB = kListBatch); the
+// particles without one (the set C) walk the cells.  kMode != 0: the pass
 // mode fixed at compile time (the two passes of a fluid frame), kMode = 0: `mode` at run time.
-template <uint32_t kMode>
+template <uint32_t kMode, uint32_t kB = kNearBatch>
 __global__ void __launch_bounds__(256, 5)
 delta_list_kernel(DevParams P, uint32_t mode_rt, const float4* __restrict__ pin, const float4* __restrict__ pa,
                   float4* __restrict__ pout, float4* __restrict__ x, float4* __restrict__ v,
@@ -871,7 +872,7 @@ delta_list_kernel(DevParams P, uint32_t mode_rt, const float4* __restrict__ pin,
     const float li = (mode & kDoDelta) ? lambda[i] : 0.f;
     const SceneCtx S = scene_ctx(P, i);
     DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, (mode & kDoDelta) != 0, (mode & kDoCollide) != 0, xi);
-    walk_near(L, i, meta, pin, vis);
+    walk_list<false, kB>(L, i, meta, pin, vis);
     delta_finish(P, S.rho0, mode, i, vis, pout, x, v, delta);
 }
 
@@ -1217,35 +1218,55 @@ struct DensityVisit {
     __device__ __forceinline__ void add(const Contrib& c, bool) { if (c.near) A = __fadd_rn(A, c.a); }
 };
 
-// err[i] = C_i; acc[0] += |C_i| (double), acc[1] = max |C_i| (double bits, non-negative)
+// err[i] = C_i; acc[0] += |C_i| (double), acc[1] = max |C_i| (double bits, non-negative); over the
+// interior particles (list length >= min_nb and position at least `margin` inside the enclosure on
+// every axis: their kernel support lies in the fluid) acc[2] += |C_i|, acc[3] = max |C_i|,
+// acc[4] += 1.
 __global__ void __launch_bounds__(128)
 density_error_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
                      const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float* __restrict__ err,
-                     double* acc) {
-    __shared__ double ssum[4], smax[4];
+                     double* acc, uint32_t min_nb, float margin) {
+    __shared__ double sred[5][4];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    double a = 0.0;
+    double a = 0.0, ai = 0.0, ni = 0.0;
     if (i < P.N) {
         const SceneCtx S = scene_ctx(P, i);
-        DensityVisit vis(P, p[i]);
+        const float4 pi = p[i];
+        DensityVisit vis(P, pi);
         bool deferred = false;
-        walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
+        const uint32_t n = walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
         const float c = vis.A / S.rho0 - 1.0f;
         err[i] = c;
         a = fabs((double)c);
+        const float* bmn = P.batched ? P.scenes[P.scene_of[i]].bmin : P.bmin;
+        const float* bmx = P.batched ? P.scenes[P.scene_of[i]].bmax : P.bmax;
+        const bool inside = pi.x > bmn[0] + margin && pi.x < bmx[0] - margin && pi.y > bmn[1] + margin &&
+                            pi.y < bmx[1] - margin && pi.z > bmn[2] + margin && pi.z < bmx[2] - margin;
+        if (inside && n >= min_nb) { ai = a; ni = 1.0; }
     }
-    double sm = a, mx = a;
+    double sm = a, mx = a, smi = ai, mxi = ai, cnt = ni;
     for (int o = 16; o > 0; o >>= 1) {
         sm += __shfl_down_sync(0xffffffffu, sm, o);
         mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+        smi += __shfl_down_sync(0xffffffffu, smi, o);
+        mxi = fmax(mxi, __shfl_down_sync(0xffffffffu, mxi, o));
+        cnt += __shfl_down_sync(0xffffffffu, cnt, o);
     }
-    if ((threadIdx.x & 31u) == 0u) { ssum[threadIdx.x >> 5] = sm; smax[threadIdx.x >> 5] = mx; }
+    if ((threadIdx.x & 31u) == 0u) {
+        const int w = threadIdx.x >> 5;
+        sred[0][w] = sm; sred[1][w] = mx; sred[2][w] = smi; sred[3][w] = mxi; sred[4][w] = cnt;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double t = 0.0, m = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t += ssum[w]; m = fmax(m, smax[w]); }
+        double t = 0.0, m = 0.0, ti = 0.0, mi = 0.0, c = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            t += sred[0][w]; m = fmax(m, sred[1][w]); ti += sred[2][w]; mi = fmax(mi, sred[3][w]); c += sred[4][w];
+        }
         atomicAdd(acc, t);
         atomicMax(reinterpret_cast<unsigned long long*>(acc + 1), (unsigned long long)__double_as_longlong(m));
+        atomicAdd(acc + 2, ti);
+        atomicMax(reinterpret_cast<unsigned long long*>(acc + 3), (unsigned long long)__double_as_longlong(mi));
+        atomicAdd(acc + 4, c);
     }
 }
 

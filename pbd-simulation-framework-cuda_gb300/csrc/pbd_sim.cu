@@ -43,7 +43,7 @@ constexpr int kMaxGraphs = 8;
 // Stored list capacities (slot-major, only the used slots are touched).  A particle whose list
 // is longer goes to the warp-cooperative cell walk.
 constexpr uint32_t kListMax = 64;    // near list: entries within the cut
-constexpr uint32_t kFullMax = 128;   // full list: every entry of the frame's list
+constexpr uint32_t kFullMax = 255;   // full list: every entry of the frame's list (meta holds 8-bit counts)
 
 constexpr int kThreadsParticle = 256;
 constexpr int kThreadsNeighbourDefault = 128;
@@ -262,18 +262,34 @@ struct Profiler {
 #define PROF_BEGIN(name) do { if (prof) prof->begin(name); } while (0)
 #define PROF_END() do { if (prof) prof->end(); } while (0)
 
-// Near lists need kernels that vanish beyond the cut (far_pairs_zero).
+// Near lists need kernels that vanish beyond the cut (far_pairs_zero), and they pay only when the
+// cut keeps a small part of the list: the cut's sphere against the cube of cells the list covers.
+// With kernel widths of a few cells (config.txt's 4.1 and 6.1 with kernelWidthNeighbours 2) the
+// sphere holds the whole cube, every entry is near, and the passes read the full list instead.
 static bool near_lists_on(const pbd_sim* s, const DevParams& P) {
-    return !(s->prm.flags & PBD_FLAG_FULL_WALK) && P.far_pairs_zero != 0u;
+    if ((s->prm.flags & PBD_FLAG_FULL_WALK) || P.far_pairs_zero == 0u) return false;
+    const bool shells = (P.active & PBD_ACTIVE_FIND_NEIGHBOURS) && P.K > 1;
+    const double side = (2.0 * (shells ? P.K : 1u) + 1.0) * P.d;
+    const double cut = std::sqrt((double)P.cut2 / 1.0001);
+    return (4.0 / 3.0) * 3.14159265358979 * cut * cut * cut < 0.5 * side * side * side;
 }
 
 // delta_list_kernel for `mode`: the fluid frame's two pass modes run specialised code.
 static void launch_delta_list(uint32_t gn, int tn, cudaStream_t st, const DevParams& P, uint32_t mode,
                               const float4* pin, const float4* pa, float4* pout, float4* x, float4* v, const float* lam,
                               const float* w, float4* delta, const uint32_t* cs, const uint32_t* ce, const CoopSet& C,
-                              const NbList& L) {
+                              const NbList& L, bool full) {
     constexpr uint32_t kFluid = kDoDelta | kDoCollide | kDoApply;
     const uint32_t g = gn + C.blocks;
+    if (full) {   // the frame's full list: entries in batches of kListBatch
+        if (mode == kFluid)
+            delta_list_kernel<kFluid, kListBatch><<<g, tn, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, L);
+        else if (mode == (kFluid | kDoUpdate))
+            delta_list_kernel<kFluid | kDoUpdate, kListBatch><<<g, tn, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, L);
+        else
+            delta_list_kernel<0, kListBatch><<<g, tn, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, L);
+        return;
+    }
     if (mode == kFluid)
         delta_list_kernel<kFluid><<<g, tn, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, L);
     else if (mode == (kFluid | kDoUpdate))
@@ -412,12 +428,12 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             const bool recorded = (act & PBD_ACTIVE_COMPUTE_LAMBDA) && (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS);
             if (do_delta) {
                 const uint32_t mode = kDoDelta | kStoreDelta;
-                const bool by_list = recorded && use_lists;
+                const bool by_list = use_lists ? recorded : use_full;
                 PROF_BEGIN(by_list ? "delta_list" : "delta");
                 const int pout = next_p(cur.p);
                 if (by_list) {
                     launch_delta_list(gn, tn, st, P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
-                                      s->delta, s->cell_start, s->cell_end, CN, L);
+                                      s->delta, s->cell_start, s->cell_end, use_lists ? CN : CF, use_lists ? L : F, !use_lists);
                     nl += 1;
                 } else {
                     delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
@@ -479,13 +495,14 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             const bool final_pass = last && (it + 1 == I);
             if (final_pass && do_update) mode |= kDoUpdate;
             const bool recorded = (act & PBD_ACTIVE_COMPUTE_LAMBDA) && (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS);
-            const bool by_list = k == 0 && recorded && use_lists;
+            // the near lists hold this iteration's lambda walk (same positions) on pass 0 only;
+            // without near lists every pass reads the frame's full list
+            const bool by_list = use_lists ? (k == 0 && recorded) : use_full;
             PROF_BEGIN(by_list ? "delta_list" : "delta");
             const int pout = next_p(cur.p);
-            // the near lists hold this iteration's lambda walk (same positions) on pass 0 only
             if (by_list) {
                 launch_delta_list(gn, tn, st, P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
-                                  s->delta, s->cell_start, s->cell_end, CN, L);
+                                  s->delta, s->cell_start, s->cell_end, use_lists ? CN : CF, use_lists ? L : F, !use_lists);
                 nl += 1;
             } else {
                 delta_kernel<<<gn, tn, 0, st>>>(P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
@@ -537,14 +554,16 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     }
     if (vort || visc) {
         // vorticity sums every list entry: the full list; viscosity alone: the omega pass's near list
-        const NbList Lv = vort ? F : ((act & PBD_ACTIVE_COMPUTE_OMEGAS) ? L : L0);
+        // (without near lists, viscosity alone reads the full list too)
+        const bool vfull = vort || (!use_lists && use_full);
+        const NbList Lv = vfull ? F : ((act & PBD_ACTIVE_COMPUTE_OMEGAS) ? L : L0);
         const NbList Ln = (vort && use_full && (act & PBD_ACTIVE_COMPUTE_OMEGAS)) ? L : L0;
         PROF_BEGIN(Lv.list ? "vort_visc_list" : "vort_visc");
         if (Lv.list) {
             float4* const vh = (readback && visc) ? s->rb_dev + s->cap : nullptr;
             vort_visc_list_kernel<<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
                                                                    s->fext, s->cell_start, s->cell_end, vort, visc, wf,
-                                                                   vort ? CF : CN, Lv, Ln, vh);
+                                                                   vfull ? CF : CN, Lv, Ln, vh);
             v_read = v_read || vh != nullptr;
             nl += 1;
         } else {
@@ -1126,30 +1145,48 @@ int pbd_profile_frames(pbd_sim* s, int nsteps, void* stream, pbd_kernel_stat* st
     return PBD_OK;
 }
 
-int pbd_density_error(pbd_sim* s, float* err, double* mean_abs, double* max_abs, void* stream) {
+static int density_error_impl(pbd_sim* s, const char* who, float* err, uint32_t min_nb, float margin, double* out,
+                              void* stream) {
     clear_error();
-    if (int rc = check_sim(s, "pbd_density_error")) return rc;
-    if (s->N == 0) {
-        if (mean_abs) *mean_abs = 0.0;
-        if (max_abs) *max_abs = 0.0;
-        return PBD_OK;
+    if (int rc = check_sim(s, who)) return rc;
+    for (int k = 0; k < 5; ++k) out[k] = 0.0;
+    if (s->N == 0) return PBD_OK;
+    if (s->anchor < 0) {
+        set_error(std::string(who) + ": run a frame (pbd_step) after the last change of the state");
+        return PBD_ERR_INVALID_ARG;
     }
-    if (s->anchor < 0) { set_error("pbd_density_error: run a frame (pbd_step) after the last change of the state"); return PBD_ERR_INVALID_ARG; }
     cudaStream_t st = (cudaStream_t)stream;
     if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
     const DevParams P = make_dev_params(s);
     const uint32_t N = s->N;
-    CK(cudaMemsetAsync(s->stats, 0, 16, st));
+    CK(cudaMemsetAsync(s->stats, 0, 40, st));
     density_error_kernel<<<div_up(N, 128), 128, 0, st>>>(P, s->p[s->cur.p], s->p[s->anchor], s->cell_start, s->cell_end,
-                                                          s->lambda, s->stats);
+                                                          s->lambda, s->stats, min_nb, margin);
     CK(cudaGetLastError());
-    double acc[2] = {0.0, 0.0};
-    CK(cudaMemcpyAsync(acc, s->stats, 16, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(out, s->stats, 40, cudaMemcpyDeviceToHost, st));
     if (err) CK(cudaMemcpyAsync(err, s->lambda, (size_t)N * 4, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (mean_abs) *mean_abs = acc[0] / (double)N;
-    if (max_abs) *max_abs = acc[1];
     s->last_stream = st;
+    return PBD_OK;
+}
+
+int pbd_density_error(pbd_sim* s, float* err, double* mean_abs, double* max_abs, void* stream) {
+    double acc[5];
+    if (int rc = density_error_impl(s, "pbd_density_error", err, 0xFFFFFFFFu, 0.0f, acc, stream)) return rc;
+    if (mean_abs) *mean_abs = s->N ? acc[0] / (double)s->N : 0.0;
+    if (max_abs) *max_abs = acc[1];
+    return PBD_OK;
+}
+
+int pbd_density_error_interior(pbd_sim* s, uint32_t min_neighbours, float margin, double* mean_abs, double* max_abs,
+                               uint32_t* counted, void* stream) {
+    if (!(margin >= 0.0f)) { set_error("pbd_density_error_interior: margin must be >= 0"); return PBD_ERR_INVALID_ARG; }
+    double acc[5];
+    if (int rc = density_error_impl(s, "pbd_density_error_interior", nullptr, min_neighbours, margin, acc, stream)) return rc;
+    const double n = acc[4];
+    if (mean_abs) *mean_abs = n > 0.0 ? acc[2] / n : 0.0;
+    if (max_abs) *max_abs = acc[3];
+    if (counted) *counted = (uint32_t)n;
     return PBD_OK;
 }
 

@@ -32,7 +32,7 @@ EXPORTED = [
     "pbd_autotune", "pbd_batch_create", "pbd_batch_destroy", "pbd_batch_add_particles", "pbd_batch_step",
     "pbd_batch_sync", "pbd_batch_num_particles", "pbd_batch_get_state", "pbd_batch_autotune",
     "pbd_batch_launches_per_step", "pbd_batch_profile_frames", "pbd_adjoint_forward", "pbd_adjoint_backward", "pbd_render_sprites",
-    "pbd_density_error", "pbd_step_readback",
+    "pbd_density_error", "pbd_density_error_interior", "pbd_step_readback",
 ]
 
 
@@ -166,6 +166,7 @@ def lib():
             "pbd_adjoint_forward": [vp, i32, i32, vp],
             "pbd_render_sprites": [vp, C.POINTER(Camera), C.POINTER(C.c_uint8), fp, vp],
             "pbd_density_error": [vp, fp, C.POINTER(C.c_double), C.POINTER(C.c_double), vp],
+            "pbd_density_error_interior": [vp, u32, C.c_float, C.POINTER(C.c_double), C.POINTER(C.c_double), u32p, vp],
             "pbd_adjoint_backward": [vp, fp, fp, fp, C.POINTER(C.c_double), C.POINTER(C.c_double), vp],
         }
         for name, args in sig.items():
@@ -352,6 +353,14 @@ class Sim:
         mean, mx = C.c_double(), C.c_double()
         check(self.L.pbd_density_error(self.h, _fp(err), C.byref(mean), C.byref(mx), C.c_void_p(stream)))
         return err, mean.value, mx.value
+
+    def density_error_interior(self, min_neighbours, margin, stream=0):
+        """(mean |C|, max |C|, particles counted) over the interior particles: list length >=
+        min_neighbours and more than `margin` inside the enclosure on every axis"""
+        mean, mx, n = C.c_double(), C.c_double(), C.c_uint32()
+        check(self.L.pbd_density_error_interior(self.h, min_neighbours, margin, C.byref(mean), C.byref(mx), C.byref(n),
+                                                C.c_void_p(stream)))
+        return mean.value, mx.value, n.value
 
     def adjoint_forward(self, nsteps, ckpt_every, stream=0):
         check(self.L.pbd_adjoint_forward(self.h, nsteps, ckpt_every, C.c_void_p(stream)))
