@@ -1,29 +1,36 @@
-"""Benchmark of the GB300 PBD step: particle-steps/s on the 1M-particle fluid workload.
+"""Benchmark of the GB300 PBD step: particle-steps/s on the 1M-particle fluid workloads.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
-                    [--leg contacts|batched|solids|adjoint]
+                    [--leg contacts|batched|solids|adjoint|dense]
 
-Our arm (default): 100^3 = 1,000,000 fluid particles in a 128^3-cell domain (seed 2),
-4 solver iterations, vorticity 5e-4, XSPH viscosity 0.01, FP32.  `value` is particle-steps/s
-with the state resident in HBM (K frames replayed as CUDA graphs, CUDA events on the
-launching stream); `e2e` drives the reference-facing C ABI with host buffers each frame
-(pbd_clear + pbd_add_particles from pinned memory, then pbd_step_readback: one frame and the
-final positions and velocities back into pinned memory, the position copy beside the frame's
-last passes; the next frame starts from that output), copies inside the timed region.  The roofline entry is for the dominant kernel, timed with CUDA event
-pairs around each launch (pbd_profile_frames) over the same number of frames.
+Our arm (default): the headline workload fluid_1m -- 100^3 = 1,000,000 fluid particles in a
+128^3-cell domain (seed 2), kernel radius 1, 4 solver iterations, vorticity 5e-4, XSPH 0.01,
+FP32 -- and beside it fluid_1m_dense, the same particles in the density regime of the
+reference's config.txt (poly6 width 4.1, spiky width 3.5, two cell shells, lambda eps 1e-4,
+~125 neighbours per particle), whose density constraint acts; its interior density error is
+reported.  For each: `value` is particle-steps/s with the state resident in HBM (K frames
+replayed as CUDA graphs, CUDA events on the launching stream); `e2e` drives the
+reference-facing C ABI with host buffers each frame (pbd_clear + pbd_add_particles from pinned
+memory, then pbd_step_readback: one frame and the final positions and velocities back into
+pinned memory), copies inside the timed region.  The roofline entry is for the dominant
+kernel, timed with CUDA event pairs around each launch (pbd_profile_frames) over K frames.
 
 Reference arm (--impl reference): the reference step has no CPU implementation and its CUDA
 code does not build with CUDA 13, so the arm times the oracle's FP32 OpenMP C
-transliteration of the reference kernels on the host cores, same workload and metric.
+transliteration of the reference kernels on all host cores: the same workload, W untimed
+frames, then exactly K timed frames -- the frames our arm times.  It never loads libpbd.so
+(its parameters are config.txt's values filled in Python).
 
 Under torchrun (N > 1) every rank steps its own replica of the workload ("replicas only":
 the step has no exchange); value = particles x frames of all ranks / max rank time.
 """
 import argparse
+import ctypes
 import json
 import os
 import subprocess
 import sys
+import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -36,9 +43,11 @@ import numpy as np  # noqa: E402
 
 METRIC = "particle-steps/s (plain 1M-particle PBD step)"
 UNIT = "particle-steps/s"
-REST_DENSITY = 1000.0
-LAMBDA_EPS = 0.1
 L2_BYTES = 129 * 2 ** 20
+DENSE = "fluid_1m_dense"
+# interior particles of the density error: list length >= this share of the workload's bulk
+# list length (the 90th percentile after the warm-up), kernel support clear of the walls
+INTERIOR_SHARE = 0.9
 
 
 def algorithmic_bytes_per_particle_step(iterations=4, passes=3, vort_visc=True):
@@ -87,12 +96,20 @@ def job_throughput(particles_per_rank, frames, world, seconds):
     return particles_per_rank * frames * world / seconds
 
 
-def build_workload(pbd, scenes, name):
-    w = scenes.WORKLOADS[name]
-    params = scenes.workload_params(pbd, w["box"], REST_DENSITY, vorticity=w["vorticity"], viscosity=w["viscosity"])
-    params.lambda_epsilon = LAMBDA_EPS
-    pos, vel = scenes.lattice(*w["shape"], seed=w["seed"])
-    return params, pos, vel, w
+def build_workload(pbd, scenes, name, base=None):
+    return scenes.workload(name, pbd, base=base)
+
+
+def workload_config(name, params, n, world):
+    """The bench line's `config`: the same dict for our arm and the reference arm."""
+    w_set = n * (16 * 3 + 16 * 3 + 4 + 16 + 16 * 2) + 2 * params.max_grid * 4
+    return {"workload": name, "particles": n, "domain_cells": int(round(params.bounds_max[0] + 1.5)),
+            "solver_iterations": int(params.solver_iterations), "vorticity": float(params.e_vorticity),
+            "xsph_viscosity": float(params.c_viscosity), "rest_density": float(params.rest_density),
+            "lambda_epsilon": float(params.lambda_epsilon), "kernel_width_poly": float(params.kernel_width_poly),
+            "kernel_width_spiky": float(params.kernel_width_spiky),
+            "kernel_width_neighbours": int(params.kernel_width_neighbours), "parallelism": f"replicas x{world}",
+            "l2": f"working set {w_set / 2**20:.0f} MiB > L2 {L2_BYTES / 2**20:.0f} MiB (no flush)"}
 
 
 def bench_out_dir():
@@ -104,10 +121,112 @@ def bench_out_dir():
     return d
 
 
+_REASON_BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
+
+
+class NvmlApi:
+    """The three NVML reads the clock record needs (libnvidia-ml through ctypes; reads only)."""
+
+    class _Pci(ctypes.Structure):
+        _fields_ = [("busIdLegacy", ctypes.c_char * 16), ("domain", ctypes.c_uint), ("bus", ctypes.c_uint),
+                    ("device", ctypes.c_uint), ("pciDeviceId", ctypes.c_uint), ("pciSubSystemId", ctypes.c_uint),
+                    ("busId", ctypes.c_char * 32)]
+
+    def __init__(self, pci):
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        count = ctypes.c_uint()
+        self.lib.nvmlDeviceGetCount_v2(ctypes.byref(count))
+        self.h = None
+        for k in range(count.value):
+            h = ctypes.c_void_p()
+            if self.lib.nvmlDeviceGetHandleByIndex_v2(k, ctypes.byref(h)) != 0:
+                continue
+            info = NvmlApi._Pci()
+            if self.lib.nvmlDeviceGetPciInfo_v3(h, ctypes.byref(info)) == 0 and \
+                    (info.domain, info.bus, info.device) == tuple(pci):
+                self.h = h
+                break
+        if self.h is None:
+            raise RuntimeError("no NVML device with the CUDA device's PCI address")
+        try:
+            self._reasons = self.lib.nvmlDeviceGetCurrentClocksEventReasons
+        except AttributeError:
+            self._reasons = self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def sm_mhz(self):
+        v = ctypes.c_uint()
+        return v.value if self.lib.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(v)) == 0 else None
+
+    def sm_max_mhz(self):
+        v = ctypes.c_uint()
+        return v.value if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(v)) == 0 else None
+
+    def reasons(self):
+        v = ctypes.c_ulonglong()
+        return v.value if self._reasons(self.h, ctypes.byref(v)) == 0 else 0
+
+    def close(self):
+        self.lib.nvmlShutdown()
+
+
+class NvmlClocks:
+    """SM clock and clock-event reasons sampled every `period` s by a thread while the timed
+    region runs (entering takes one sample first, so every sample counted lies in the region)."""
+
+    def __init__(self, api, period=0.002):
+        self.api = api
+        self.period = period
+        self.samples = []
+        self.stop = threading.Event()
+        self.thread = None
+        self.max_mhz = None
+
+    def _sample(self):
+        self.samples.append((self.api.sm_mhz(), self.api.reasons()))
+
+    def _run(self):
+        while not self.stop.is_set():
+            self._sample()
+            self.stop.wait(self.period)
+
+    def __enter__(self):
+        self.max_mhz = self.api.sm_max_mhz()
+        self.api.sm_mhz()
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.thread.join(timeout=5)
+        self._sample()
+
+    def summary(self):
+        sms = [m for m, _ in self.samples if m is not None]
+        reasons = set()
+        for _, bits in self.samples:
+            for name, b in _REASON_BITS.items():
+                if bits & b:
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sms)) if sms else None, "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(reasons), "samples": len(sms), "source": f"nvml every {self.period * 1e3:.0f} ms"}
+
+
+def clock_sampler(torch, local):
+    """NVML sampling of the CUDA device `local`, else nvidia-smi's."""
+    try:
+        pr = torch.cuda.get_device_properties(local)
+        return NvmlClocks(NvmlApi((pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)))
+    except Exception:  # noqa: BLE001
+        return ClockSampler(local)
+
+
 class ClockSampler:
     """nvidia-smi samples (every 50 ms) during the timed region: entering waits for the first
     sample, which is left out of the summary, so every sample counted was taken inside the
-    region."""
+    region.  The fallback when NVML cannot be loaded."""
 
     def __init__(self, index):
         self.index = index
@@ -166,15 +285,21 @@ class ClockSampler:
         except OSError:
             pass
         return {"sm_mhz": float(np.median(sms)) if sms else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sms)}
+                "reasons": sorted(reasons), "samples": len(sms), "source": "nvidia-smi every 50 ms"}
+
+
+def oracle_params(scenes, name):
+    """The workload's parameters and lattice for the CPU oracle, without the library."""
+    import pbd   # the Params structure only: pbd.py loads libpbd.so on first use, never here
+    return scenes.workload(name, pbd, base=scenes.config_txt_params(pbd.Params))
 
 
 def cpu_baseline(name, max_seconds, threads=None):
-    """FP32 OpenMP transliteration of the reference step (oracle build), timed on host cores."""
-    import pbd
+    """FP32 OpenMP transliteration of the reference step (oracle build), timed on host cores over
+    a bounded sample: frames after one untimed frame until `max_seconds` have passed."""
     import scenes
     from oracle import oracle as orc_mod
-    params, pos, vel, w = build_workload(pbd, scenes, name)
+    params, pos, vel, w = oracle_params(scenes, name)
     if threads:
         orc_mod.set_threads(threads)
     cores = orc_mod.max_threads()
@@ -202,8 +327,8 @@ def run_batched(torch, pbd, scenes, stream, sh, frames):
     """256 seeded dam-break scenes (4K-65K particles, rest density 900-1100, |g| 8-11, domains
     32-96 cells): scenes/s advanced as one batch vs the same scenes stepped one by one."""
     sl = scenes.batched_scenes()
-    shared = scenes.workload_params(pbd, 64, REST_DENSITY)
-    shared.lambda_epsilon = LAMBDA_EPS
+    shared = scenes.workload_params(pbd, 64, 1000.0)
+    shared.lambda_epsilon = 0.1
     descs = [pbd.scene_desc(sc["n"], sc["rest_density"], sc["gravity"], sc["box"]) for sc in sl]
     total = sum(sc["n"] for sc in sl)
     tune_cache = os.environ.get("PBD_TUNE_CACHE", os.path.join(bench_out_dir(), "autotune.jsonl"))
@@ -265,8 +390,8 @@ def run_batched(torch, pbd, scenes, stream, sh, frames):
 def run_solids(torch, pbd, scenes, stream, sh, frames):
     """64^3 fluid + 8 static solid boxes (65,536 solids), 128^3 domain: particle-steps/s."""
     pos, vel, w = scenes.solids_scene()
-    p = scenes.workload_params(pbd, 128, REST_DENSITY)
-    p.lambda_epsilon = LAMBDA_EPS
+    p = scenes.workload_params(pbd, 128, 1000.0)
+    p.lambda_epsilon = 0.1
     with pbd.Sim(p, len(pos)) as sim:
         sim.add_particles_mass(pos, vel, w)
         sim.step(3, stream=sh)
@@ -293,8 +418,8 @@ def run_adjoint(torch, pbd, scenes, stream, sh, frames=60, every=10, fd_check=Tr
     resolution of the parameter), at the full horizon and at a short one."""
     pos, vel, target = scenes.adjoint_dam_break()
     n = len(pos)
-    p = scenes.workload_params(pbd, 72, REST_DENSITY)
-    p.lambda_epsilon = LAMBDA_EPS
+    p = scenes.workload_params(pbd, 72, 1000.0)
+    p.lambda_epsilon = 0.1
     p.flags &= ~pbd.FLAG_CELL_END_QUIRK
     p.flags |= pbd.FLAG_TRACK_IDS
 
@@ -441,54 +566,77 @@ def run_render(torch, pbd, sim, stream, sh, reps=10):
 
 
 def run_reference(args):
+    """The oracle's FP32 OpenMP port of the reference kernels on all host cores, the workload our
+    arm times: W untimed frames, then exactly K timed frames (rank 0 only)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    budget = max(5.0, min(120.0, 3.0 * (args.steps + args.warmup)))
-    cb = cpu_baseline(args.workload, budget)
-    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded lattice)",
-            "config": {"workload": args.workload, "particles": 1000000 if args.workload == "fluid_1m" else None},
-            "cpu_baseline": cb,
-            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    import scenes
+    from oracle import oracle as orc_mod
+    params, pos, vel, w = oracle_params(scenes, args.workload)
+    n = len(pos)
+    cores = orc_mod.max_threads()
+    o = orc_mod.Oracle(params, n, "f32")
+    o.add_particles(pos, vel)
+    o.step(args.warmup)
+    t0 = time.perf_counter()
+    o.step(args.steps)
+    el = time.perf_counter() - t0
+    o.close()
+    value = job_throughput(n, args.steps, 1, el)
+    sample = (f"{args.workload}: {n} particles, frames {args.warmup + 1}-{args.warmup + args.steps} "
+              f"(after {args.warmup} untimed), {el:.1f} s, FP32 OpenMP")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice, SplitMix64)",
+            "config": workload_config(args.workload, params, n, args.gpus),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_ours(args):
-    import torch
-    import pbd
-    import scenes
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:  # noqa: BLE001
+        return {}
 
-    rank, world, local = dist_env()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
 
-    params, pos, vel, w = build_workload(pbd, scenes, args.workload)
+def traffic_of(name, kernel):
+    """ncu DRAM bytes of one launch of `kernel` on workload `name` (profiles/traffic.json)."""
+    try:
+        t = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        return t.get(name, {}).get(kernel)
+    except Exception:  # noqa: BLE001
+        return None
+
+
+def measure_workload(torch, pbd, scenes, name, args, stream, sh, world, dev, local, extra=None):
+    """value, e2e, clocks, roofline, per-kernel time and density error of one workload: W warm-up
+    frames, K timed frames (graph replays, CUDA events), K profiled frames, then e2e over the
+    same frames as the timed ones on a fresh simulation."""
+    params, pos, vel, w = build_workload(pbd, scenes, name)
     n = len(pos)
     sim = pbd.Sim(params, n)
     sim.add_particles(pos, vel)
-    stream = torch.cuda.Stream(device=dev)
-    sh = stream.cuda_stream
 
     def barrier():
         if world > 1:
             import torch.distributed as dist
             dist.barrier()
 
-    # ---- warm-up (also records the CUDA graphs)
+    # ---- warm-up (also records the CUDA graphs); the bulk list length for the interior
     sim.step(args.warmup, stream=sh)
     stream.synchronize()
     sim.sync()
     launches_per_step = sim.launches_per_step()
+    _, cnt, _ = sim.neighbours(0)
+    min_nb = int(INTERIOR_SHARE * np.percentile(cnt, 90))
 
     # ---- device-resident timing
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
+    ev0, ev1 = _events(torch)
+    with clock_sampler(torch, local) as clocks:
         barrier()
         torch.cuda.synchronize()
         ev0.record(stream)
@@ -501,16 +649,17 @@ def run_ours(args):
     t_rank = max_over_ranks(ms / 1e3, world, dev)
     value = job_throughput(n, args.steps, world, t_rank)
 
-    # ---- density constraint after the timed frames (mean / max |rho_i / rho0 - 1|)
+    # ---- density constraint after the timed frames: all particles, and the interior ones
     _, derr_mean, derr_max = sim.density_error(stream=sh)
+    margin = float(max(params.kernel_width_poly, 1.0))
+    imean, imax, icount = sim.density_error_interior(min_nb, margin, stream=sh)
+    density = {"mean": derr_mean, "max": derr_max, "interior_mean": imean, "interior_max": imax,
+               "interior_particles": icount, "interior_rule": f"list length >= {min_nb} "
+               f"({INTERIOR_SHARE} x the 90th percentile after the warm-up), more than {margin} inside every wall",
+               "after_frames": args.warmup + args.steps}
+    out_extra = extra(sim) if extra else {}
 
-    # ---- headless sprites of this state
-    try:
-        render = run_render(torch, pbd, sim, stream, sh)
-    except Exception as e:  # noqa: BLE001
-        render = {"error": f"{type(e).__name__}: {e}"}
-
-    # ---- per-kernel device time over the same number of frames (direct launches)
+    # ---- per-kernel device time over the next K frames (direct launches)
     prof = sim.profile(args.steps, stream=sh)
     stream.synchronize()
     sim.sync()
@@ -523,24 +672,12 @@ def run_ours(args):
         # one of I delta launches also writes v: average the extra 16 B over the I launches
         bytes_per += 16 * n / params.solver_iterations
     achieved = bytes_per / per_launch_s / 1e9
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
+    peaks = load_peaks()
     peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    traffic = None
-    tfile = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tfile):
-        try:
-            traffic = json.load(open(tfile)).get(top)
-        except Exception:
-            traffic = None
 
     # ---- end to end through the reference-facing ABI with host buffers, over the same frames
-    # of the dam break as the timed ones: a fresh simulation from the initial state, after the
-    # same warm-up, for K frames
+    # of the run as the timed ones: a fresh simulation from the initial state, the same warm-up
     sim.close()
     sim = pbd.Sim(params, n)
     sim.add_particles(pos, vel)
@@ -556,10 +693,8 @@ def run_ours(args):
     xp = hx.ctypes.data_as(pbd.C.POINTER(pbd.C.c_float))
     vp = hv.ctypes.data_as(pbd.C.POINTER(pbd.C.c_float))
     L = pbd.lib()
-
     # each frame: the state in from pinned host memory, one step, the state out to pinned host
-    # memory (pbd_step_readback: the position copy runs beside the frame's last passes); the
-    # next frame's input is this frame's output
+    # memory (pbd_step_readback); the next frame's input is this frame's output
     src = [xp, vp]
     rx, rv = pbd.C.POINTER(pbd.C.c_float)(), pbd.C.POINTER(pbd.C.c_float)()
 
@@ -569,7 +704,6 @@ def run_ours(args):
         pbd.check(L.pbd_step_readback(sim.h, 1, pbd.C.c_void_p(sh), pbd.C.byref(rx), pbd.C.byref(rv)))
         src[0], src[1] = rx, rv
 
-    e2e_frame()
     barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -578,9 +712,51 @@ def run_ours(args):
     t_e2e = max_over_ranks(time.perf_counter() - t0, world, dev)
     e2e_value = job_throughput(n, e2e_steps, world, t_e2e)
     sim.sync()
-
     sim.close()
-    # ---- batched scenes and unified solids (same GPU, after the headline measurement)
+
+    bps = algorithmic_bytes_per_particle_step(params.solver_iterations, 3,
+                                              bool(params.active & (pbd.ACTIVE["computeOmegas"] | pbd.ACTIVE["computeViscosity"])))
+    return {
+        "value": value, "ms_per_step": ms / args.steps, "particles": n,
+        "config": workload_config(name, params, n, world),
+        "clocks": clocks.summary(),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
+                "frames": e2e_steps, "first_frame": args.warmup + 1},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic_of(name, top),
+                     "algorithmic_bytes_per_launch": bytes_per, "launch_ms": per_launch_s * 1e3},
+        "step_roofline": {"bytes_per_particle_step": bps, "achieved_gbs": bps * value / world / 1e9,
+                          "frac": bps * value / world / 1e9 / peak},
+        "kernel_ms_per_frame": {k: v[1] / args.steps for k, v in prof.items()},
+        "density_error": density,
+        **out_extra,
+    }
+
+
+def run_ours(args):
+    import torch
+    import pbd
+    import scenes
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    sh = stream.cuda_stream
+
+    def render_of(sim):
+        # headless sprites of the state after the timed frames
+        try:
+            return {"render": run_render(torch, pbd, sim, stream, sh)}
+        except Exception as e:  # noqa: BLE001
+            return {"render": {"error": f"{type(e).__name__}: {e}"}}
+
+    head = measure_workload(torch, pbd, scenes, args.workload, args, stream, sh, world, dev, local, extra=render_of)
+
     def leg(fn, *a, **k):
         # a failing secondary leg is reported in the line instead of losing the headline number
         try:
@@ -588,41 +764,26 @@ def run_ours(args):
         except Exception as e:  # noqa: BLE001
             return {"error": f"{type(e).__name__}: {e}"}
 
+    dense = None
+    if args.workload != DENSE:
+        dense = leg(measure_workload, torch, pbd, scenes, DENSE, args, stream, sh, world, dev, local)
     batched = leg(run_batched, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 60)))
     solids = leg(run_solids, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 100)))
     adjoint = leg(run_adjoint, torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check)
     contacts = leg(run_contacts, torch, pbd, scenes, stream, sh, frames=20)
 
-    working_set = n * (16 * 3 + 16 * 3 + 4 + 16 + 16 * 2) + 2 * params.max_grid * 4
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic (seeded jittered lattice, SplitMix64)",
-        "config": {"workload": args.workload, "particles": n, "domain_cells": w["box"], "solver_iterations": 4,
-                   "vorticity": w["vorticity"], "xsph_viscosity": w["viscosity"], "rest_density": REST_DENSITY,
-                   "lambda_epsilon": LAMBDA_EPS, "parallelism": f"replicas x{world}",
-                   "l2": f"working set {working_set / 2**20:.0f} MiB > L2 {L2_BYTES / 2**20:.0f} MiB (no flush)"},
-        "clocks": clocks.summary(),
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 32 * n, "d2h_bytes_per_step": 32 * n,
-                "frames": e2e_steps},
-        "gpu_launches": launches_per_step * args.steps,
-        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": bytes_per, "launch_ms": per_launch_s * 1e3},
-        "step_roofline": {"bytes_per_particle_step": algorithmic_bytes_per_particle_step(),
-                          "achieved_gbs": algorithmic_bytes_per_particle_step() * value / world / 1e9,
-                          "frac": algorithmic_bytes_per_particle_step() * value / world / 1e9 / peak},
-        "kernel_ms_per_frame": {k: v[1] / args.steps for k, v in prof.items()},
-        "density_error": {"mean": derr_mean, "max": derr_max, "after_frames": args.warmup + args.steps},
-        "batched": batched,
-        "solids": solids,
-        "adjoint": adjoint,
-        "contacts": contacts,
-        "render": render,
+        "metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded jittered lattice, SplitMix64)",
+        "config": head["config"], "clocks": head["clocks"], "e2e": head["e2e"], "gpu_launches": head["gpu_launches"],
+        "roofline": head["roofline"], "step_roofline": head["step_roofline"],
+        "kernel_ms_per_frame": head["kernel_ms_per_frame"], "density_error": head["density_error"],
+        "dense": dense, "batched": batched, "solids": solids, "adjoint": adjoint, "contacts": contacts,
+        "render": head.get("render"),
     }
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(args.workload, args.cpu_seconds)
-    if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
@@ -643,6 +804,8 @@ def run_leg(args):
         out = run_batched(torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 60)))
     elif args.leg == "solids":
         out = run_solids(torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 100)))
+    elif args.leg == "dense":
+        out = measure_workload(torch, pbd, scenes, DENSE, args, stream, sh, 1, torch.device("cuda", 0), 0)
     else:
         out = run_adjoint(torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check)
     print(json.dumps({"leg": args.leg, **out}), flush=True)
@@ -658,7 +821,7 @@ def main():
     ap.add_argument("--workload", default="fluid_1m")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-fd-check", action="store_true", help="skip the FP64 finite-difference check of the adjoint")
-    ap.add_argument("--leg", choices=["contacts", "batched", "solids", "adjoint"],
+    ap.add_argument("--leg", choices=["contacts", "batched", "solids", "adjoint", "dense"],
                     help="measure only this secondary workload and print its result (not the bench line)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -5,12 +5,22 @@ The reference spawns a lattice box from config.txt's Particles.Box keys
 jittered by SplitMix64 (Vigna's published 64-bit mixer, restated below), so every backend
 (GPU library, CPU oracle) is fed the same bytes.
 
-Workloads (kernel radius h = 1 = particle diameter, dt = 1/60, 4 solver iterations):
-  dam_break_32k   32^3 fluid particles in a 64^3-cell box, seed 1
-  fluid_1m        100^3 fluid particles in a 128^3-cell domain, vorticity 5e-4, XSPH 0.01, seed 2
+Workloads (dt = 1/60, gravity -9.82, 4 solver iterations):
+  dam_break_32k   32^3 unit lattice in a 64^3-cell box, kernel radius h = 1, seed 1
+  fluid_1m        100^3 unit lattice in a 128^3-cell domain, h = 1, vorticity 5e-4, XSPH 0.01, seed 2
+  fluid_1m_dense  the same 1,000,000 particles with the density regime of the reference's own
+                  config.txt: poly6 width 4.1, spiky width 3.5 particle diameters, two cell shells
+                  (kernelWidthNeighbours 2, ~125 list entries per particle), rest density 1995 (the
+                  lattice's own poly6 density), lambda eps 1e-4 as Density.h:90 hard-codes it,
+                  vorticity 5e-4, XSPH 1.5e-4 (c * rest density = 0.3)
   solids_328k     64^3 fluid particles + 8 static solid boxes of 8,192 particles (inverse mass 0)
                   in a 128^3-cell domain, seed 3
   adjoint_64k     32 x 64 x 32 fluid column in a 72^3-cell box with a seeded target, seed 5
+
+With h = 1 on a unit lattice the reference's density (no self term, unit mass, Density.h:67-84)
+is ~0, so the h = 1 workloads run with lambda eps 0.1 and their density constraint is inactive
+(C ~ -1): they measure gravity, contacts, vorticity and viscosity.  fluid_1m_dense is the
+workload whose density solve acts.
 """
 import numpy as np
 
@@ -47,11 +57,53 @@ def lattice(nx, ny, nz, origin=(2.5, 2.5, 2.5), spacing=1.0, jitter=0.05, seed=1
     return pos, vel
 
 
-def workload_params(pbd, box, rest_density, vorticity=0.0, viscosity=0.0, iterations=4, max_neighbours=512):
+def config_txt_params(params_type):
+    """A `params_type` (pbd.Params) holding the reference's config.txt values (config.txt:9-131,
+    Particles.cc:8 for maxGrid, Density.h:90 for eps) -- the same values pbd_params_default
+    writes, filled here without loading the library (the CPU reference arm uses it)."""
+    p = params_type()
+    p.struct_size = 128
+    p.threads_per_block = 512
+    p.particle_radius = 0.5
+    p.max_neighbours_per_particle = 512
+    p.delta_t = 0.01
+    p.gravity = -29.82
+    p.rest_density = 1200.0
+    p.kernel_width_spiky = 6.1
+    p.k_scorr = 0.2
+    p.n_scorr = 4
+    p.q_scorr = 0.2
+    p.c_viscosity = 0.0001
+    p.kernel_width_poly = 4.1
+    p.e_vorticity = 1.0
+    p.collision_type = 0
+    p.kernel_width_neighbours = 2
+    p.max_collision_batches = 16
+    p.stiffness = 0.3
+    p.enclosure_position_damping = 0.0
+    p.enclosure_velocity_damping = 1.0
+    for a in range(3):
+        p.bounds_min[a] = 1.5
+        p.bounds_max[a] = 62.5
+    p.solver_iterations = 1
+    p.stabilization_iterations = 1
+    p.active = 0x3FF
+    p.max_grid = 128 ** 3
+    p.lambda_epsilon = 0.0001
+    p.flags = 1            # PBD_FLAG_CELL_END_QUIRK
+    return p
+
+
+_ACTIVE_OMEGAS, _ACTIVE_VORTICITY, _ACTIVE_VISCOSITY = 1 << 7, 1 << 8, 1 << 9
+
+
+def workload_params(pbd, box, rest_density, vorticity=0.0, viscosity=0.0, iterations=4, max_neighbours=512,
+                    base=None):
     """pbd_params for the standard workloads: radius 0.5 (diameter 1 = cell width), kernel widths
     1.0 (spiky factor 1 x diameter, poly 1.0 absolute), q = 0.2 h, gravity -9.82, dt = 1/60,
-    walls at 1.5 and box - 1.5, 27-cell neighbourhood (kernelWidthNeighbours = 1)."""
-    p = pbd.default_params()
+    walls at 1.5 and box - 1.5, 27-cell neighbourhood (kernelWidthNeighbours = 1).  `base` (a
+    filled pbd.Params) replaces the library's defaults as the starting point."""
+    p = base.copy() if base is not None else pbd.default_params()
     p.particle_radius = 0.5
     p.kernel_width_spiky = 1.0
     p.kernel_width_poly = 1.0
@@ -68,11 +120,11 @@ def workload_params(pbd, box, rest_density, vorticity=0.0, viscosity=0.0, iterat
         p.bounds_max[a] = float(box) - 1.5
     p.e_vorticity = vorticity
     p.c_viscosity = viscosity
-    act = pbd.ACTIVE_ALL
+    act = 0x3FF
     if vorticity == 0.0:
-        act &= ~(pbd.ACTIVE["computeOmegas"] | pbd.ACTIVE["computeVorticity"])
+        act &= ~(_ACTIVE_OMEGAS | _ACTIVE_VORTICITY)
     if viscosity == 0.0:
-        act &= ~pbd.ACTIVE["computeViscosity"]
+        act &= ~_ACTIVE_VISCOSITY
     p.active = act
     return p
 
@@ -156,7 +208,26 @@ def adjoint_dam_break(shape=(32, 64, 32), box=72, seed=5):
 
 
 WORKLOADS = {
-    "dam_break_32k": dict(shape=(32, 32, 32), box=64, seed=1, vorticity=0.0, viscosity=0.0),
-    "fluid_1m": dict(shape=(100, 100, 100), box=128, seed=2, vorticity=0.0005, viscosity=0.01),
-    "solids_328k": dict(shape=(64, 64, 64), box=128, seed=3, vorticity=0.0, viscosity=0.0, solids=(8, (16, 16, 32))),
+    "dam_break_32k": dict(shape=(32, 32, 32), box=64, seed=1, vorticity=0.0, viscosity=0.0,
+                          rest_density=1000.0, lambda_epsilon=0.1),
+    "fluid_1m": dict(shape=(100, 100, 100), box=128, seed=2, vorticity=0.0005, viscosity=0.01,
+                     rest_density=1000.0, lambda_epsilon=0.1),
+    "fluid_1m_dense": dict(shape=(100, 100, 100), box=128, seed=2, vorticity=0.0005, viscosity=0.00015,
+                           rest_density=1995.0, lambda_epsilon=0.0001, kernel_width_poly=4.1,
+                           kernel_width_spiky=3.5, kernel_width_neighbours=2),
+    "solids_328k": dict(shape=(64, 64, 64), box=128, seed=3, vorticity=0.0, viscosity=0.0, solids=(8, (16, 16, 32)),
+                        rest_density=1000.0, lambda_epsilon=0.1),
 }
+
+
+def workload(name, pbd, base=None, shape=None):
+    """(params, pos, vel, spec) of a standard workload; `base` as in workload_params; `shape`
+    overrides the lattice (a smaller case of the same parameters, for the oracle)."""
+    w = WORKLOADS[name]
+    p = workload_params(pbd, w["box"], w["rest_density"], vorticity=w["vorticity"], viscosity=w["viscosity"], base=base)
+    p.lambda_epsilon = w["lambda_epsilon"]
+    for key in ("kernel_width_poly", "kernel_width_spiky", "kernel_width_neighbours"):
+        if key in w:
+            setattr(p, key, w[key])
+    pos, vel = lattice(*(shape or w["shape"]), spacing=w.get("spacing", 1.0), seed=w["seed"])
+    return p, pos, vel, w
