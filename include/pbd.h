@@ -321,16 +321,33 @@ int pbd_adjoint_backward(pbd_sim* sim, const float* dL_dx_final, float* dL_dv0, 
  * (engines that own all device memory from start-up, frame loops that must not stall on an
  * allocation): the step's stable radix sort of uint32 keys, with every byte of working memory
  * taken from one fixed array inside the library.  Inputs and outputs are the caller's device
- * buffers: d_keys_out receives the keys in ascending order and d_perm_out the input index of
- * each output key (a stable sort, so equal keys keep their input order).  Only the low
- * `key_bits` bits (1..32) are sorted.  d_keys_out and d_perm_out must not overlap d_keys_in.
- * Limit: n <= 1,048,576 keys (the fixed array is about 9 MiB and stays on every GPU that loads
- * the library until the process exits); larger n returns PBD_ERR_CAPACITY.  The first call on
- * each device looks up the array's device address (make it before any stream capture).  All
+ * buffers: d_keys_out receives the keys in ascending order of their low `key_bits` bits (1..32;
+ * higher bits do not take part in the order, as with cub's end_bit) and d_perm_out the input
+ * index of each output key (a stable sort, so keys equal in those bits keep their input order).
+ * d_keys_out and d_perm_out must not overlap d_keys_in.
+ * Limit: n <= 1,048,576 keys (the fixed array is 9,441,536 bytes and stays on every GPU that
+ * loads the library until the process exits); larger n returns PBD_ERR_CAPACITY.  The first call
+ * on each device looks up the array's device address (make it before any stream capture).  All
  * calls share the array: calls whose GPU work overlaps race and must be serialised by the
- * caller.  Asynchronous on `stream`. */
+ * caller.  Asynchronous on `stream`; pbd_sort_noalloc_status reports how the last call ended. */
 int pbd_sort_keys_noalloc(const uint32_t* d_keys_in, uint32_t* d_keys_out, uint32_t* d_perm_out,
                           uint32_t n, uint32_t key_bits, void* stream);
+/* Waits for `stream` and returns PBD_ERR_TIMEOUT if the last pbd_sort_keys_noalloc on the current
+ * device had a bounded look-back wait give up (its output is then not sorted), else PBD_OK. */
+int pbd_sort_noalloc_status(void* stream);
+
+/* ---- failure injection for tests (no counterpart in the reference) --------------------- */
+/* After `skip` more device or pinned-host allocations of the library succeed, the next `fail`
+ * allocations fail as on a GPU that is out of memory: the call that meets one returns
+ * PBD_ERR_ALLOC and frees whatever it had taken.  (0, 0) switches it off.  Process-wide. */
+int pbd_debug_fail_allocations(uint32_t skip, uint32_t fail);
+/* The radix sort's look-back waits give up after `spins` polls (0 = the default, a few seconds)
+ * and then set the device error word that pbd_sync (or pbd_sort_noalloc_status) reports as
+ * PBD_ERR_TIMEOUT.  With hold_first_tile the first tile of every sort pass never publishes its
+ * counts, so every wait on it runs out -- the failure path, exercised without a hang or a trap.
+ * `sim` NULL sets the no-allocation sort's settings; otherwise the simulation's frames use them
+ * from the next pbd_step or pbd_debug_front on. */
+int pbd_debug_set_wait_limit(pbd_sim* sim, uint32_t spins, int hold_first_tile);
 
 /* Text of the last error on this thread ("" if none). */
 const char* pbd_last_error(void);

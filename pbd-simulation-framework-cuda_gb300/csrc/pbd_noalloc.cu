@@ -8,10 +8,12 @@
 // byte of working memory taken from one fixed array compiled into this library.
 //
 // The working memory is the file-scope array below: kNoAllocMaxKeys keys at most
-// (1,048,576), about 10 MiB.  Every GPU that loads the library keeps that array until the
-// process exits.  All calls share it and it keeps the last call's contents, so each call first
-// zeroes the parts that must start at zero; calls whose GPU work overlaps (different streams,
-// or different host threads) race on it and must be serialised by the caller.
+// (1,048,576), kScratchWords * 4 = 9,441,536 bytes (9.0 MiB).  Every GPU that loads the library
+// keeps that array until the process exits.  All calls share it and it keeps the last call's
+// contents, so each call first zeroes the parts that must start at zero; calls whose GPU work
+// overlaps (different streams, or different host threads) race on it and must be serialised by
+// the caller.  Its error word holds the outcome of the last call on the device:
+// pbd_sort_noalloc_status reads it.
 //
 // Host code cannot use the array's name as a device address.  The first call on each device,
 // with that device current, looks the address up with cudaGetSymbolAddress and caches it;
@@ -43,11 +45,15 @@ constexpr size_t kOffTiles = kOffStatus + (size_t)kMaxPasses * kNoAllocMaxTiles 
 constexpr size_t kOffErr = kOffTiles + kMaxPasses;
 constexpr size_t kScratchWords = (kOffErr + 1 + 63) & ~size_t(63);
 
+static_assert(kScratchWords * 4 == 9441536, "the fixed array's size is stated in pbd.h");
 static __device__ __align__(256) uint32_t g_sort_scratch[kScratchWords];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 uint32_t* g_scratch_ptr[kMaxDevices] = {};
+// look-back wait settings (pbd_debug_set_wait_limit with a null simulation)
+uint32_t g_spin_limit = kSpinLimit;
+uint32_t g_hold = 0;
 
 // Zero the histograms, the look-back rows the call will use, the tile counters and the error word.
 __global__ void noalloc_clear_kernel(uint32_t* base, uint32_t ntiles) {
@@ -62,13 +68,13 @@ __global__ void noalloc_clear_kernel(uint32_t* base, uint32_t ntiles) {
 
 // Digit histograms of every pass (the sim counts them in its predict kernel).
 __global__ void noalloc_hist_kernel(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ hist,
-                                    int npasses) {
+                                    int npasses, uint32_t key_bits) {
     __shared__ uint32_t sh[kMaxPasses * kRadix];
     for (int b = threadIdx.x; b < kMaxPasses * kRadix; b += blockDim.x) sh[b] = 0u;
     __syncthreads();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t key = keys[i];
-        for (int ps = 0; ps < npasses; ++ps) atomicAdd(&sh[ps * kRadix + ((key >> (ps * kRadixBits)) & (kRadix - 1))], 1u);
+        for (int ps = 0; ps < npasses; ++ps) atomicAdd(&sh[ps * kRadix + sort_digit(key, ps, key_bits)], 1u);
     }
     __syncthreads();
     for (int b = threadIdx.x; b < npasses * kRadix; b += blockDim.x)
@@ -99,6 +105,13 @@ int scratch_for_current_device(uint32_t** out) {
 using pbd::clear_error;
 using pbd::set_error;
 
+int pbd_noalloc_set_wait_limit(unsigned int spins, int hold_first_tile) {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    g_spin_limit = spins ? spins : kSpinLimit;
+    g_hold = hold_first_tile ? 1u : 0u;
+    return PBD_OK;
+}
+
 extern "C" int pbd_sort_keys_noalloc(const uint32_t* d_keys_in, uint32_t* d_keys_out, uint32_t* d_perm_out,
                                      uint32_t n, uint32_t key_bits, void* stream) {
     clear_error();
@@ -122,10 +135,16 @@ extern "C" int pbd_sort_keys_noalloc(const uint32_t* d_keys_in, uint32_t* d_keys
     const int npasses = (int)((key_bits + kRadixBits - 1) / kRadixBits);
     const uint32_t ntiles = (n + kSortTile - 1) / kSortTile;
     SortScratch S{base + kOffHist, base + kOffStatus, base + kOffTiles, base + kOffErr, kNoAllocMaxTiles};
+    {
+        std::lock_guard<std::mutex> lock(g_setup_mutex);
+        S.spin_limit = g_spin_limit;
+        S.hold = g_hold;
+    }
+    S.key_bits = key_bits;
 
     noalloc_clear_kernel<<<32, 256, 0, st>>>(base, ntiles);
     const uint32_t gh = std::min<uint32_t>((n + 255) / 256, 1024u);
-    noalloc_hist_kernel<<<gh, 256, 0, st>>>(d_keys_in, n, S.hist, npasses);
+    noalloc_hist_kernel<<<gh, 256, 0, st>>>(d_keys_in, n, S.hist, npasses, key_bits);
     // Ping-pong between the caller's outputs and the fixed array so that the last pass
     // writes the outputs: pass p writes the outputs when (npasses - 1 - p) is even.
     uint32_t* tmp_k = base + kOffKeys;
@@ -147,6 +166,24 @@ extern "C" int pbd_sort_keys_noalloc(const uint32_t* d_keys_in, uint32_t* d_keys
     if (e != cudaSuccess) {
         set_error(std::string("pbd_sort_keys_noalloc: launch: ") + cudaGetErrorString(e));
         return PBD_ERR_CUDA;
+    }
+    return PBD_OK;
+}
+
+extern "C" int pbd_sort_noalloc_status(void* stream) {
+    clear_error();
+    uint32_t* base = nullptr;
+    if (int rc = scratch_for_current_device(&base)) return rc;
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    uint32_t err = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&err, base + kOffErr, sizeof(err), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        set_error(std::string("pbd_sort_noalloc_status: ") + cudaGetErrorString(e));
+        return PBD_ERR_CUDA;
+    }
+    if (err & kErrSortTimeout) {
+        set_error("pbd_sort_keys_noalloc: a bounded look-back wait gave up; the output is not sorted");
+        return PBD_ERR_TIMEOUT;
     }
     return PBD_OK;
 }

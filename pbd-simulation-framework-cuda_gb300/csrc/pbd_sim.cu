@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -29,6 +30,25 @@ namespace pbd {
 thread_local std::string g_last_error;
 void set_error(const std::string& m) { g_last_error = m; }
 void clear_error() { g_last_error.clear(); }
+
+// Allocation-failure injection (pbd_debug_fail_allocations): `skip` more allocations succeed,
+// then `fail` allocations fail.
+static std::mutex g_alloc_mutex;
+static uint32_t g_alloc_skip = 0, g_alloc_fail = 0;
+static bool injected_failure() {
+    std::lock_guard<std::mutex> lock(g_alloc_mutex);
+    if (g_alloc_skip > 0) { --g_alloc_skip; return false; }
+    if (g_alloc_fail > 0) { --g_alloc_fail; return true; }
+    return false;
+}
+cudaError_t lib_malloc(void** p, size_t bytes) {
+    if (injected_failure()) { *p = nullptr; return cudaErrorMemoryAllocation; }
+    return cudaMalloc(p, bytes);
+}
+cudaError_t lib_host_alloc(void** p, size_t bytes, unsigned int flags) {
+    if (injected_failure()) { *p = nullptr; return cudaErrorMemoryAllocation; }
+    return cudaHostAlloc(p, bytes, flags);
+}
 }  // namespace pbd
 
 using namespace pbd;
@@ -153,6 +173,8 @@ struct pbd_sim {
     uint32_t graph_n = 0xFFFFFFFFu;
     bool dirty = true;
     uint32_t launches = 0;
+    uint32_t sort_spin_limit = kSpinLimit;   // pbd_debug_set_wait_limit
+    uint32_t sort_hold = 0;
 };
 
 namespace {
@@ -310,7 +332,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const uint32_t N = s->N;
     const int np = sort_passes(s);
     const int tn = s->tpb_nbr;
-    SortScratch S{s->hist, s->status, s->tile_counter, s->err, s->max_tiles};
+    SortScratch S{s->hist, s->status, s->tile_counter, s->err, s->max_tiles, s->sort_spin_limit, s->sort_hold};
     nl = 0;
 
     // applyForces + initializeCellIds (+ histograms, + clearing last frame's cells)
@@ -697,7 +719,7 @@ int ensure_contacts(pbd_sim* s) {
         s->ct_arena = nullptr;
         s->ct_bytes = 0;
     }
-    cudaError_t e = cudaMalloc(&s->ct_arena, need);
+    cudaError_t e = lib_malloc(&s->ct_arena, need);
     if (e != cudaSuccess) { set_error(std::string("collisionType 1 workspace: ") + cudaGetErrorString(e)); return PBD_ERR_ALLOC; }
     s->ct_bytes = need;
     char* c = static_cast<char*>(s->ct_arena);
@@ -768,7 +790,7 @@ int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<Scene
     }
     size_t total = 0;
     for (auto& pt : parts) total += (pt.second + 255) & ~size_t(255);
-    e = cudaMalloc(&s->arena, total);
+    e = lib_malloc(&s->arena, total);
     if (e != cudaSuccess) { delete s; set_error(std::string("cudaMalloc arena: ") + cudaGetErrorString(e)); return PBD_ERR_ALLOC; }
     char* cur = static_cast<char*>(s->arena);
     for (auto& pt : parts) { *pt.first = cur; cur += (pt.second + 255) & ~size_t(255); }
@@ -782,8 +804,13 @@ int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<Scene
         e = cudaMemcpy(s->d_scenes, s->h_scenes.data(), s->nscenes * sizeof(SceneParams), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    if (e != cudaSuccess) { cudaFree(s->arena); delete s; return cuda_fail("pbd_create init", e); }
-    if (int rc2 = ensure_contacts(s)) { cudaFree(s->arena); delete s; return rc2; }
+    auto undo = [&]() {   // a failed create leaves nothing behind
+        if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+        cudaFree(s->arena);
+        delete s;
+    };
+    if (e != cudaSuccess) { undo(); return cuda_fail("pbd_create init", e); }
+    if (int rc2 = ensure_contacts(s)) { undo(); return rc2; }
     *out = s;
     return PBD_OK;
 }
@@ -966,7 +993,11 @@ int pbd_step_readback(pbd_sim* s, int nsteps, void* stream, const float** pos4, 
     if (nsteps < 1) { set_error("pbd_step_readback: nsteps < 1"); return PBD_ERR_INVALID_ARG; }
     if (s->batched) { set_error("pbd_step_readback: a batch reads its scenes with pbd_batch_get_state"); return PBD_ERR_INVALID_ARG; }
     if (!s->rb_host) {
-        CK(cudaHostAlloc((void**)&s->rb_host, (size_t)2 * s->cap * 16, cudaHostAllocMapped));
+        if (cudaError_t ea = lib_host_alloc((void**)&s->rb_host, (size_t)2 * s->cap * 16, cudaHostAllocMapped)) {
+            s->rb_host = nullptr;
+            set_error(std::string("pbd_step_readback: pinned host buffers: ") + cudaGetErrorString(ea));
+            return PBD_ERR_ALLOC;
+        }
         CK(cudaHostGetDevicePointer((void**)&s->rb_dev, s->rb_host, 0));
         CK(cudaStreamCreateWithFlags(&s->rb_stream, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&s->rb_fork, cudaEventDisableTiming));
@@ -1066,9 +1097,15 @@ int pbd_debug_neighbours(pbd_sim* s, uint32_t max_entries, uint32_t* list, uint3
     if (n == 0) return PBD_OK;
     uint32_t *dl = nullptr, *dc = nullptr, *dk = nullptr;
     const size_t lb = std::max<size_t>(1, n * (size_t)max_entries) * 4;
-    CK(cudaMalloc(&dl, lb));
-    CK(cudaMalloc(&dc, n * 4));
-    CK(cudaMalloc(&dk, n * 4));
+    cudaError_t ea = lib_malloc((void**)&dl, lb);
+    if (ea == cudaSuccess) ea = lib_malloc((void**)&dc, n * 4);
+    if (ea == cudaSuccess) ea = lib_malloc((void**)&dk, n * 4);
+    if (ea != cudaSuccess) {
+        if (dl) cudaFree(dl);
+        if (dc) cudaFree(dc);
+        set_error(std::string("pbd_debug_neighbours: ") + cudaGetErrorString(ea));
+        return PBD_ERR_ALLOC;
+    }
     CK(cudaMemsetAsync(dl, 0, lb, s->last_stream));   // slots past each count read back as 0
     const DevParams P = make_dev_params(s);
     const bool cols = (s->prm.flags & PBD_FLAG_COLORS) && (s->prm.active & PBD_ACTIVE_FIND_NEIGHBOURS);
@@ -1083,6 +1120,23 @@ int pbd_debug_neighbours(pbd_sim* s, uint32_t max_entries, uint32_t* list, uint3
     if (e == cudaSuccess && contacts) e = cudaMemcpy(contacts, dk, n * 4, cudaMemcpyDeviceToHost);
     cudaFree(dl); cudaFree(dc); cudaFree(dk);
     if (e != cudaSuccess) return cuda_fail("pbd_debug_neighbours", e);
+    return PBD_OK;
+}
+
+int pbd_debug_fail_allocations(uint32_t skip, uint32_t fail) {
+    std::lock_guard<std::mutex> lock(pbd::g_alloc_mutex);
+    pbd::g_alloc_skip = fail ? skip : 0u;
+    pbd::g_alloc_fail = fail;
+    return PBD_OK;
+}
+
+int pbd_debug_set_wait_limit(pbd_sim* s, uint32_t spins, int hold_first_tile) {
+    clear_error();
+    if (!s) return pbd_noalloc_set_wait_limit(spins, hold_first_tile);
+    if (int rc = check_sim(s, "pbd_debug_set_wait_limit")) return rc;
+    s->sort_spin_limit = spins ? spins : kSpinLimit;
+    s->sort_hold = hold_first_tile ? 1u : 0u;
+    s->dirty = true;   // the frame graphs hold the sort's settings
     return PBD_OK;
 }
 
@@ -1205,7 +1259,7 @@ int pbd_render_sprites(pbd_sim* s, const pbd_camera* cam, uint8_t* rgba, float* 
         CK(cudaStreamSynchronize(st));
         if (s->img_arena) cudaFree(s->img_arena);
         s->img_arena = nullptr;
-        cudaError_t e = cudaMalloc(&s->img_arena, need);
+        cudaError_t e = lib_malloc(&s->img_arena, need);
         if (e != cudaSuccess) { s->img_bytes = 0; set_error(std::string("sprite image: ") + cudaGetErrorString(e)); return PBD_ERR_ALLOC; }
         s->img_bytes = need;
     }
@@ -1465,7 +1519,7 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
         if (s->adj_arena) CK(cudaStreamSynchronize(st));
         if (s->adj_arena) cudaFree(s->adj_arena);
         s->adj_arena = nullptr;
-        cudaError_t e = cudaMalloc(&s->adj_arena, need);
+        cudaError_t e = lib_malloc(&s->adj_arena, need);
         if (e != cudaSuccess) { s->adj_bytes = 0; set_error(std::string("adjoint workspace: ") + cudaGetErrorString(e)); return PBD_ERR_ALLOC; }
         s->adj_bytes = need;
     }

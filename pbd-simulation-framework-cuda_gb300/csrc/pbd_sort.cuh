@@ -13,9 +13,11 @@
 //    warp, then register slot, then lane); warp counts are scanned per digit in shared
 //    memory.
 //  - Tile digit counts are chained across tiles with decoupled look-back (status word =
-//    2 flag bits + 30 count bits).  Every wait is bounded: after kSpinLimit polls the tile
-//    records PBD device error bit kErrSortTimeout and carries on, so a lost predecessor can
-//    never hang the GPU.
+//    2 flag bits + 30 count bits).  Every wait is bounded: after SortScratch::spin_limit polls
+//    (kSpinLimit by default, a few seconds) the tile records PBD device error bit
+//    kErrSortTimeout and carries on, so a lost predecessor can never hang the GPU.  For tests
+//    of that path, SortScratch::hold makes the first tile of every pass withhold its status
+//    (a predecessor that never publishes): every wait on it runs out.
 //  - Keys are scattered to shared memory in tile order first, then written out so that
 //    each digit's run lands on consecutive global addresses.
 #pragma once
@@ -46,7 +48,18 @@ struct SortScratch {
     uint32_t* tile_counter;  // [kMaxPasses]
     uint32_t* err;           // device error word
     uint32_t max_tiles;
+    uint32_t spin_limit = kSpinLimit;   // polls of one look-back wait before it gives up
+    uint32_t hold = 0;                  // 1: the first tile of each pass never publishes (tests)
+    uint32_t key_bits = 32;             // only bits [0, key_bits) order the keys
 };
+
+// The digit of `key` in pass `pass`, counting only the bits below key_bits.
+__device__ __forceinline__ uint32_t sort_digit(uint32_t key, int pass, uint32_t key_bits) {
+    const uint32_t shift = (uint32_t)pass * kRadixBits;
+    const uint32_t bits = key_bits - shift;          // >= 1 for every pass the sort runs
+    const uint32_t mask = bits >= (uint32_t)kRadixBits ? (uint32_t)(kRadix - 1) : ((1u << bits) - 1u);
+    return (key >> shift) & mask;
+}
 
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
     uint32_t v;
@@ -113,7 +126,6 @@ onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin
     if (pass > 0) S.status[((size_t)(pass - 1) * S.max_tiles + tile) * kRadix + tid] = 0u;
 
     const uint32_t base = tile * (uint32_t)kSortTile;
-    const int shift = pass * kRadixBits;
     uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
 #pragma unroll
     for (int k = 0; k < kSortItems; ++k) {
@@ -129,7 +141,7 @@ onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin
     for (int k = 0; k < kSortItems; ++k) {
         const uint32_t idx = base + warp * (32 * kSortItems) + k * 32 + lane;
         const bool valid = idx < n;
-        const uint32_t digit = (key[k] >> shift) & (kRadix - 1);
+        const uint32_t digit = sort_digit(key[k], pass, S.key_bits);
         const uint32_t peers = __match_any_sync(0xffffffffu, valid ? digit : (uint32_t)kRadix);
         const uint32_t before = valid ? wh[digit] : 0u;
         __syncwarp();
@@ -150,7 +162,7 @@ onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin
     uint32_t* st = S.status + (size_t)pass * S.max_tiles * kRadix;
     uint32_t excl = 0;
     if (tile == 0) {
-        st_relaxed(&st[d], kFlagPrefix | run);
+        if (!S.hold) st_relaxed(&st[d], kFlagPrefix | run);
     } else {
         st_relaxed(&st[(size_t)tile * kRadix + d], kFlagAggregate | run);
         int t = (int)tile - 1;
@@ -159,7 +171,7 @@ onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin
             for (;;) {
                 w = ld_relaxed(&st[(size_t)t * kRadix + d]);
                 if (w >> 30) break;
-                if (++spins > kSpinLimit) {
+                if (++spins > S.spin_limit) {
                     atomicOr(S.err, kErrSortTimeout);
                     w = kFlagPrefix;
                     break;
@@ -184,7 +196,7 @@ onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin
     for (int k = 0; k < kSortItems; ++k) {
         const uint32_t idx = base + warp * (32 * kSortItems) + k * 32 + lane;
         if (idx < n) {
-            const uint32_t digit = (key[k] >> shift) & (kRadix - 1);
+            const uint32_t digit = sort_digit(key[k], pass, S.key_bits);
             const uint32_t pos = s_start[digit] + s_whist[warp][digit] + rank[k];
             s_keys[pos] = key[k];
             s_vals[pos] = val[k];
@@ -194,7 +206,7 @@ onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin
     const uint32_t tile_n = (n - base) < (uint32_t)kSortTile ? (n - base) : (uint32_t)kSortTile;
     for (uint32_t i = tid; i < tile_n; i += kSortThreads) {
         const uint32_t kk = s_keys[i];
-        const uint32_t o = s_goff[(kk >> shift) & (kRadix - 1)] + i;
+        const uint32_t o = s_goff[sort_digit(kk, pass, S.key_bits)] + i;
         if (o < n) {            // always true unless a look-back wait gave up (error word set)
             kout[o] = kk;
             vout[o] = s_vals[i];

@@ -32,7 +32,8 @@ EXPORTED = [
     "pbd_autotune", "pbd_batch_create", "pbd_batch_destroy", "pbd_batch_add_particles", "pbd_batch_step",
     "pbd_batch_sync", "pbd_batch_num_particles", "pbd_batch_get_state", "pbd_batch_autotune",
     "pbd_batch_launches_per_step", "pbd_batch_profile_frames", "pbd_adjoint_forward", "pbd_adjoint_backward", "pbd_render_sprites",
-    "pbd_density_error", "pbd_density_error_interior", "pbd_step_readback",
+    "pbd_density_error", "pbd_density_error_interior", "pbd_step_readback", "pbd_sort_noalloc_status",
+    "pbd_debug_fail_allocations", "pbd_debug_set_wait_limit",
 ]
 
 
@@ -155,7 +156,8 @@ def lib():
             "pbd_debug_neighbours": [vp, u32, u32p, u32p, u32p, i32], "pbd_debug_front": [vp, vp],
             "pbd_launches_per_step": [vp, u32p],
             "pbd_profile_frames": [vp, i32, vp, C.POINTER(KernelStat), u32, u32p],
-            "pbd_sort_keys_noalloc": [vp, vp, vp, u32, u32, vp],
+            "pbd_sort_keys_noalloc": [vp, vp, vp, u32, u32, vp], "pbd_sort_noalloc_status": [vp],
+            "pbd_debug_fail_allocations": [u32, u32], "pbd_debug_set_wait_limit": [vp, u32, i32],
             "pbd_autotune": [vp, C.c_char_p, vp, u32p],
             "pbd_batch_create": [P, u32, C.POINTER(SceneDesc), C.POINTER(vp)], "pbd_batch_destroy": [vp],
             "pbd_batch_add_particles": [vp, u32, u32, fp, fp], "pbd_batch_step": [vp, i32, vp],

@@ -54,6 +54,41 @@ def test_noalloc_sort_matches_the_step_sort_twice(need_gpu, pbd, scenes):
         assert np.array_equal(p, perm)
 
 
+@pytest.mark.parametrize("key_bits", [1, 8, 16, 20, 24, 32])
+@pytest.mark.parametrize("n", [1, 100, 4097, 65537, 1 << 20])
+def test_noalloc_sort_orders_by_the_low_key_bits(need_gpu, pbd, key_bits, n):
+    # every pass count (1 to 4, so both ends of the ping-pong through the fixed array), partial
+    # last tiles, one key, the 1,048,576-key limit; keys carry bits above key_bits, which must
+    # not take part in the order (a stable sort by the low bits)
+    rng = np.random.default_rng(key_bits * 1000003 + n)
+    keys = rng.integers(0, 1 << 32, size=n, dtype=np.uint64).astype(np.uint32)
+    keys[::2] &= np.uint32(0xFFFF003F)   # plenty of equal low bits, so stability is exercised
+    mask = np.uint32(0xFFFFFFFF if key_bits == 32 else (1 << key_bits) - 1)
+    order = np.argsort(keys & mask, kind="stable")
+    k, p = _sort_noalloc(pbd, keys, key_bits=key_bits)
+    assert np.array_equal(p, order.astype(np.uint32))
+    assert np.array_equal(k, keys[order])
+    assert pbd.lib().pbd_sort_noalloc_status(None) == pbd.OK
+
+
+def test_noalloc_sort_reports_a_wait_that_ran_out(need_gpu, pbd):
+    # a short wait limit and a first tile that never publishes its counts: every look-back wait
+    # on it gives up (no hang, no trap), the status says so, and the next call is clean again
+    L = pbd.lib()
+    keys = np.random.default_rng(7).integers(0, 1 << 24, size=50000, dtype=np.uint64).astype(np.uint32)
+    try:
+        pbd.check(L.pbd_debug_set_wait_limit(None, 2000, 1))
+        _sort_noalloc(pbd, keys)
+        assert L.pbd_sort_noalloc_status(None) == pbd.ERR_TIMEOUT
+        assert b"gave up" in L.pbd_last_error()
+    finally:
+        pbd.check(L.pbd_debug_set_wait_limit(None, 0, 0))
+    k, p = _sort_noalloc(pbd, keys)
+    assert L.pbd_sort_noalloc_status(None) == pbd.OK
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(p, order.astype(np.uint32)) and np.array_equal(k, keys[order])
+
+
 def test_noalloc_sort_rejects_more_keys_than_its_fixed_memory(need_gpu, pbd):
     import torch
     buf = torch.zeros(16, dtype=torch.int32, device="cuda")
