@@ -132,7 +132,7 @@ struct AdjDeltaVisit {
     __device__ static Contrib shfl(const Contrib& c, int) { return c; }
     __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool contact) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        const float r2 = rx * rx + ry * ry + rz * rz;
+        const float r2 = dist2(rx, ry, rz);
         if (r2 >= P.cut2 || r2 <= 0.0f) return zero();
         const float L = sqrtf(r2);
         const float3 rh = make_float3(rx / L, ry / L, rz / L);
@@ -225,7 +225,7 @@ struct AdjLambdaBwd {
     __device__ static Contrib shfl(const Contrib& c, int) { return c; }
     __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool) {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        const float r2 = rx * rx + ry * ry + rz * rz;
+        const float r2 = dist2(rx, ry, rz);
         if (r2 >= P.cut2 || r2 <= 0.0f) return zero();
         const float L = sqrtf(r2);
         const float3 rh = make_float3(rx / L, ry / L, rz / L);

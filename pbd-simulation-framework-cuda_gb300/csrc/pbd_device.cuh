@@ -93,6 +93,13 @@ __device__ __forceinline__ uint32_t morton(float x, float y, float z) {
     return (morton_axis(x) << 2) + (morton_axis(y) << 1) + morton_axis(z);
 }
 
+// |r|^2 over xyz with explicit rounding: x*x, then + y*y and + z*z as fused multiply-adds, in that
+// order.  The compiler may contract a plain x*x + y*y + z*z differently from one kernel to
+// another; this spelling gives every walker (cells, lists, staged copies) the same bits.
+__device__ __forceinline__ float dist2(float rx, float ry, float rz) {
+    return __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, __fmul_rn(rx, rx)));
+}
+
 // ---------------------------------------------------------- pair kernels (Density.h) --
 // poly6Viscosity: W = 315 t^3 t^3 / den, t = hp^2 - d^2, for 0.001 < d < hp - 0.001.
 __device__ __forceinline__ float poly6(const DevParams& P, float dist) {

@@ -305,7 +305,7 @@ __device__ __forceinline__ uint32_t filter_list(const NbList& F, uint32_t fm, co
             if (kb + b == nc) mc = m;
             if (kb + b < n) {
                 const float rx = pi.x - pj[b].x, ry = pi.y - pj[b].y, rz = pi.z - pj[b].z;
-                if (rx * rx + ry * ry + rz * rz < cut2) {
+                if (dist2(rx, ry, rz) < cut2) {
                     if (m < L.kmax) L.list[(size_t)m * L.stride + i] = j[b];
                     ++m;
                 }
@@ -343,7 +343,7 @@ struct Recorder {
         }
         if (list) {
             const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            if (rx * rx + ry * ry + rz * rz < cut2) {
+            if (dist2(rx, ry, rz) < cut2) {
                 if (n < kmax) list[(size_t)n * stride + i] = j;
                 ++n;
             }
@@ -548,10 +548,10 @@ struct LambdaVisit {
     __device__ __forceinline__ void end_contacts(uint32_t) {}
     __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, bool) const {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z, rw = pi.w - pj.w;
-        const float r2 = rx * rx + ry * ry + rz * rz;
+        const float r2 = dist2(rx, ry, rz);
         if (r2 >= P.cut2) return zero();      // every kernel is exactly 0 there
         const float dist = sqrtf(r2);
-        const float r2w = r2 + rw * rw;
+        const float r2w = __fmaf_rn(rw, rw, r2);
         const float s = spiky_scale(P, dist, r2w);
         return Contrib{poly6(P, dist), __fmul_rn(__fmul_rn(s, s), r2w), s, rx, ry, rz, rw, 1u};
     }
@@ -741,15 +741,15 @@ struct DeltaVisit {
         Contrib c = zero();
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z, rw = pi.w - pj.w;
         c.rx = rx; c.ry = ry; c.rz = rz; c.rw = rw;
-        const float r2 = rx * rx + ry * ry + rz * rz;
+        const float r2 = dist2(rx, ry, rz);
         if (!all_pairs && r2 >= P.cut2) return c;
         const float dist = sqrtf(r2);
         if (do_delta) {
-            const float s = spiky_scale(P, dist, r2 + rw * rw);
+            const float s = spiky_scale(P, dist, __fmaf_rn(rw, rw, r2));
             if (s != 0.0f || all_pairs) {
                 const float W = poly6(P, dist);
-                const float sc = -P.k_scorr * powi(W * P.inv_wq, P.n_scorr);
-                c.coef = (li + lj + sc) * s;
+                const float sc = __fmul_rn(-P.k_scorr, powi(__fmul_rn(W, P.inv_wq), P.n_scorr));
+                c.coef = __fmul_rn(__fadd_rn(__fadd_rn(li, lj), sc), s);
                 c.flags |= 1u;
             }
         }
@@ -916,14 +916,15 @@ struct OmegaVisit {
     __device__ __forceinline__ float4 fetch(uint32_t j) const { return __ldg(v + j); }
     __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, const float4& vj, bool) const {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z, rw = pi.w - pj.w;
-        const float r2 = rx * rx + ry * ry + rz * rz;
+        const float r2 = dist2(rx, ry, rz);
         if (r2 >= P.cut2) return zero();
         const float dist = sqrtf(r2);
-        const float s = spiky_scale(P, dist, r2 + rw * rw);
+        const float s = spiky_scale(P, dist, __fmaf_rn(rw, rw, r2));
         if (s == 0.0f) return zero();
         const float wx = vj.x - vi.x, wy = vj.y - vi.y, wz = vj.z - vi.z;
         const float gx = s * rx, gy = s * ry, gz = s * rz;
-        return Contrib{wy * gz - wz * gy, wz * gx - wx * gz, wx * gy - wy * gx, 1u};
+        return Contrib{__fsub_rn(__fmul_rn(wy, gz), __fmul_rn(wz, gy)), __fsub_rn(__fmul_rn(wz, gx), __fmul_rn(wx, gz)),
+                       __fsub_rn(__fmul_rn(wx, gy), __fmul_rn(wy, gx)), 1u};
     }
     __device__ __forceinline__ void add(const Contrib& c, bool) {
         if (!c.near) return;
@@ -1056,7 +1057,7 @@ struct VortViscVisitT {
         if constexpr ((kTerms & 1u) != 0u) if (vort) {
             const float4 oj = ex.oj;
             const float dx = oj.x - oi.x, dy = oj.y - oi.y, dz = oj.z - oi.z;
-            const float ol = sqrtf(dx * dx + dy * dy + dz * dz);
+            const float ol = sqrtf(dist2(dx, dy, dz));
             // the fast division: the divisors (position differences + 1e-8) stay far below 2^126
             c.gx = __fdividef(ol, (pj.x - pi.x) + 0.00000001f);
             c.gy = __fdividef(ol, (pj.y - pi.y) + 0.00000001f);
@@ -1065,7 +1066,7 @@ struct VortViscVisitT {
         }
         if constexpr ((kTerms & 2u) != 0u) if (visc) {
             const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            const float r2 = rx * rx + ry * ry + rz * rz;
+            const float r2 = dist2(rx, ry, rz);
             if (r2 >= P.hp2) return c;
             const float W = poly6(P, sqrtf(r2));
             if (W == 0.0f) return c;
@@ -1211,7 +1212,7 @@ struct DensityVisit {
     __device__ __forceinline__ void end_contacts(uint32_t) {}
     __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, bool) const {
         const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        const float r2 = rx * rx + ry * ry + rz * rz;
+        const float r2 = dist2(rx, ry, rz);
         if (r2 >= P.cut2) return zero();
         return Contrib{poly6(P, sqrtf(r2)), 1u};
     }

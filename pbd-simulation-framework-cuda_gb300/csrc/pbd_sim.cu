@@ -22,6 +22,7 @@
 
 #include "pbd_internal.h"
 #include "pbd_kernels.cuh"
+#include "pbd_staged.cuh"
 #include "pbd_adjoint.cuh"
 #include "pbd_contacts.cuh"
 #include "pbd_sprites.cuh"
@@ -296,6 +297,20 @@ static bool near_lists_on(const pbd_sim* s, const DevParams& P) {
     return (4.0 / 3.0) * 3.14159265358979 * cut * cut * cut < 0.5 * side * side * side;
 }
 
+// delta_staged_kernel for `mode`, as launch_delta_list.
+static void launch_delta_staged(uint32_t N, cudaStream_t st, const DevParams& P, uint32_t mode, const float4* pin,
+                                const float4* pa, float4* pout, float4* x, float4* v, const float* lam, const float* w,
+                                float4* delta, const uint32_t* cs, const uint32_t* ce, const CoopSet& C, const NbList& F) {
+    constexpr uint32_t kFluid = kDoDelta | kDoCollide | kDoApply;
+    const uint32_t g = C.blocks + (N + kStageThreads - 1) / kStageThreads;
+    if (mode == kFluid)
+        delta_staged_kernel<kFluid><<<g, kStageThreads, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, F);
+    else if (mode == (kFluid | kDoUpdate))
+        delta_staged_kernel<kFluid | kDoUpdate><<<g, kStageThreads, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, F);
+    else
+        delta_staged_kernel<0><<<g, kStageThreads, 0, st>>>(P, mode, pin, pa, pout, x, v, lam, w, delta, cs, ce, C, F);
+}
+
 // delta_list_kernel for `mode`: the fluid frame's two pass modes run specialised code.
 static void launch_delta_list(uint32_t gn, int tn, cudaStream_t st, const DevParams& P, uint32_t mode,
                               const float4* pin, const float4* pa, float4* pout, float4* x, float4* v, const float* lam,
@@ -398,13 +413,16 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const uint32_t I = prm.solver_iterations, Sx = prm.stabilization_iterations;
     // near lists: recorded by a walking pass for the pass after it at the same positions; they
     // need kernels that vanish beyond the cut (far_pairs_zero)
-    const bool use_lists = near_lists_on(s, P);
+    const bool use_lists = near_lists_on(s, P) && !(prm.flags & PBD_FLAG_STAGED_PASSES);
     const NbList Lf = use_lists ? NbList{s->nb_list, s->nb_meta, s->cap, kListMax} : NbList{nullptr, nullptr, 0u, 0u};
     const NbList L = Lf;
     const NbList L0{nullptr, nullptr, 0u, 0u};
     // full lists: stored by the first lambda pass of the frame (its walk of the anchor cells)
     const bool use_full = !(prm.flags & PBD_FLAG_FULL_WALK) && (act & PBD_ACTIVE_COMPUTE_LAMBDA) && I > 0;
     const NbList F = use_full ? NbList{s->fl_list, s->fl_meta, s->cap, kFullMax} : L0;
+    // without near lists the later lambda passes and the delta passes stage each block's
+    // neighbourhood in shared memory (the full list stays the fallback)
+    const bool staged_ok = use_full && !use_lists && !(prm.flags & PBD_FLAG_LIST_PASSES) && staged_supported(P);
     const bool do_delta = act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS, do_apply = act & PBD_ACTIVE_APPLY_DELTA_POSITIONS;
     const bool do_update = act & PBD_ACTIVE_UPDATE_POSITIONS;
     const bool collide = prm.collision_type == 0;
@@ -429,9 +447,14 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         // a taped frame records the iteration's near lists into the tape (the delta pass reads them there)
         const NbList L = (taped && use_lists) ? NbList{tape->near[it], tape->near_meta[it], N, kListMax} : Lf;
         if (act & PBD_ACTIVE_COMPUTE_LAMBDA) {
-            PROF_BEGIN((use_full && it > 0) ? "lambda_list" : "lambda");
+            const bool lstaged = staged_ok && it > 0 && !aux;
+            PROF_BEGIN(lstaged ? "lambda_staged" : ((use_full && it > 0) ? "lambda_list" : "lambda"));
             const NbList Lr = (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS) ? L : L0;
-            if (use_full && it > 0) {
+            if (lstaged) {
+                lambda_staged_kernel<<<kCoopBlocks + div_up(N, kStageThreads), kStageThreads, 0, st>>>(
+                    P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam, CF, F);
+                nl += 1;
+            } else if (use_full && it > 0) {
                 lambda_list_kernel<<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->cell_start, s->cell_end, lam,
                                                                     CF, Lr.list ? DN : DX, aux, Lr, F);
                 nl += 1;
@@ -520,9 +543,14 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             // the near lists hold this iteration's lambda walk (same positions) on pass 0 only;
             // without near lists every pass reads the frame's full list
             const bool by_list = use_lists ? (k == 0 && recorded) : use_full;
-            PROF_BEGIN(by_list ? "delta_list" : "delta");
+            const bool dstaged = by_list && staged_ok && !taped;
+            PROF_BEGIN(dstaged ? "delta_staged" : (by_list ? "delta_list" : "delta"));
             const int pout = next_p(cur.p);
-            if (by_list) {
+            if (dstaged) {
+                launch_delta_staged(N, st, P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
+                                    s->delta, s->cell_start, s->cell_end, CF, F);
+                nl += 1;
+            } else if (by_list) {
                 launch_delta_list(gn, tn, st, P, mode, s->p[cur.p], pa, s->p[pout], s->x[cur.x], s->v[cur.v], lam, wf,
                                   s->delta, s->cell_start, s->cell_end, use_lists ? CN : CF, use_lists ? L : F, !use_lists);
                 nl += 1;
