@@ -74,12 +74,10 @@ extern "C" {
  * vorticity) reads only those; the entries left out add exact zeros there, so both ways give
  * identical results: this flag exists for testing and measurement. */
 #define PBD_FLAG_FULL_WALK       (1u << 3)
-/* Where the kernel cut covers a particle's whole list (no near lists), the later lambda passes
- * and the delta passes copy each block's neighbourhood into shared memory and walk it there; the
- * results are the same bits as the walk over the stored lists.  LIST_PASSES keeps the stored
- * lists; STAGED_PASSES stages those passes also where near lists would be kept.  Both exist for
- * testing and measurement. */
-#define PBD_FLAG_LIST_PASSES     (1u << 4)
+/* The later lambda passes and the delta passes copy each block's neighbourhood (the particles of
+ * every cell its members' lists reach) into shared memory and walk it there instead of reading
+ * the stored lists; the results are the same bits.  Measured slower than the stored lists on
+ * GB300 (kept for testing and measurement).  Bit 4 is reserved. */
 #define PBD_FLAG_STAGED_PASSES   (1u << 5)
 
 /* ---- parameters: mirrors SimulationParameters (kernel/Globals.h:50-75) plus the

@@ -29,6 +29,7 @@ def _lib(precision):
         lib.orc_add_particle.argtypes = [vp, f32p, f32p]
         lib.orc_add_particles_mass.argtypes = [vp, u32, f32p, f32p, f32p, f32p]
         lib.orc_clear.argtypes = [vp]
+        lib.orc_set_fext.argtypes = [vp, f32p]
         lib.orc_step.argtypes = [vp, i32]
         lib.orc_step_phase.argtypes = [vp, i32]
         lib.orc_num_particles.restype = u32
@@ -113,6 +114,12 @@ class Oracle:
 
     def clear(self):
         self.lib.orc_clear(self.h)
+
+    def set_fext(self, fext4):
+        """f_ext of the current particles in their current order (n, 4)."""
+        f = np.ascontiguousarray(fext4, dtype=np.float32)
+        assert f.shape == (self.n, 4)
+        self.lib.orc_set_fext(self.h, _ptr(f, C.c_float))
 
     def step(self, nsteps=1):
         rc = self.lib.orc_step(self.h, nsteps)

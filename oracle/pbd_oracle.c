@@ -272,6 +272,13 @@ int orc_add_particle(orc_sim* s, const float pos[3], const float dir[3]) {
 
 void orc_clear(orc_sim* s) { s->N = 0; }
 
+/* The external force of the current particles, in their current order (test hook: lets a frame
+ * start from another implementation's state, whose f_ext the previous frame's vorticity left,
+ * Forces.h:82, Fluid.cu:21-29). */
+void orc_set_fext(orc_sim* s, const float* f4) {
+    for (uint32_t i = 0; i < s->N; ++i) s->fext[i] = mk4(f4[4 * i], f4[4 * i + 1], f4[4 * i + 2], f4[4 * i + 3]);
+}
+
 /* ------------------------------------------------------------ Forces.h:19-101 ------- */
 static void apply_forces(orc_sim* s) {
     const pbd_params* P = &s->prm;

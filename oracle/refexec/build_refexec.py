@@ -1,13 +1,14 @@
 """Build recipe of oracle/_ref/librefexec.so: the reference's own kernel code, run on the CPU.
 
 TEST INFRASTRUCTURE ONLY.  Reads the reference's kernel headers where they lie
-(/root/reference/PBD-Simulation-Framework-CUDA/src/app/simulation/kernel), rewrites in memory
+(<reference>/src/app/simulation/kernel, <reference> = $PBD_REFERENCE_ROOT or the
+reference/PBD-Simulation-Framework-CUDA checkout beside this repository), rewrites in memory
 the one construct a host compiler cannot parse -- the launch syntax `kernel<<<grid, block>>>(args);`
 becomes `refx::launch(grid, block, [&]{ kernel(args); });` -- drops the includes of sibling
 headers that are concatenated in order, and pipes the result, between refexec_shim.h and
 refexec_harness.cpp, to g++ on standard input.  Nothing derived from the reference is written to
-disk except the shared library in oracle/_ref/ (git-ignored).  Needs /root/reference, so it runs
-only where the reference is mounted; the golden fixtures it produces are committed.
+disk except the shared library in oracle/_ref/ (git-ignored).  Needs the reference sources, so it
+runs only where they are mounted; the golden fixtures it produces are committed.
 """
 import os
 import re
@@ -16,7 +17,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("PBD_REFERENCE_ROOT", "/root/reference/PBD-Simulation-Framework-CUDA")
+# the reference checkout: PBD_REFERENCE_ROOT, else reference/PBD-Simulation-Framework-CUDA beside this repository
+REF = os.environ.get("PBD_REFERENCE_ROOT") or os.path.join(os.path.dirname(ROOT), "reference", "PBD-Simulation-Framework-CUDA")
 KDIR = os.path.join(REF, "src", "app", "simulation", "kernel")
 OUT_DIR = os.path.join(ROOT, "oracle", "_ref")
 OUT = os.path.join(OUT_DIR, "librefexec.so")

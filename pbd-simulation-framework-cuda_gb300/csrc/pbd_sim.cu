@@ -420,9 +420,11 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     // full lists: stored by the first lambda pass of the frame (its walk of the anchor cells)
     const bool use_full = !(prm.flags & PBD_FLAG_FULL_WALK) && (act & PBD_ACTIVE_COMPUTE_LAMBDA) && I > 0;
     const NbList F = use_full ? NbList{s->fl_list, s->fl_meta, s->cap, kFullMax} : L0;
-    // without near lists the later lambda passes and the delta passes stage each block's
-    // neighbourhood in shared memory (the full list stays the fallback)
-    const bool staged_ok = use_full && !use_lists && !(prm.flags & PBD_FLAG_LIST_PASSES) && staged_supported(P);
+    // PBD_FLAG_STAGED_PASSES: the later lambda passes and the delta passes stage each block's
+    // neighbourhood in shared memory (the full list stays the fallback); inverse masses are not
+    // staged, so simulations with solids read the lists
+    const bool staged_ok = (prm.flags & PBD_FLAG_STAGED_PASSES) && use_full && !use_lists && staged_supported(P) &&
+                           !s->mass_used;
     const bool do_delta = act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS, do_apply = act & PBD_ACTIVE_APPLY_DELTA_POSITIONS;
     const bool do_update = act & PBD_ACTIVE_UPDATE_POSITIONS;
     const bool collide = prm.collision_type == 0;

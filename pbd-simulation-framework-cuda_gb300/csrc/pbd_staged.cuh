@@ -24,7 +24,7 @@ namespace pbd {
 
 constexpr int kStageThreads = 128;
 constexpr uint32_t kStageMaxCells = 2048;     // box cells a block may stage
-constexpr uint32_t kStageMaxParts = 1280;     // particles a block may stage
+constexpr uint32_t kStageMaxParts = 1216;     // particles a block may stage (6 blocks of 128 threads per SM)
 constexpr int kStageMaxReach = 3;             // shells the staged walk supports
 
 // Integer cell coordinate of a position component, as morton_axis computes it before spreading.
@@ -40,13 +40,7 @@ __device__ __forceinline__ int list_reach(const DevParams& P) {
 template <class Ex>
 struct StageSmem {
     uint16_t off[kStageMaxCells + 1];   // first staged slot of each box cell (z fastest); off[n] = total
-    union {
-        uint32_t start[kStageMaxCells];  // while staging: the cell's first sorted index
-        // while walking: each thread's box-relative cell coordinate per axis and offset
-        // -kStageMaxReach..kStageMaxReach (thread-minor: no bank conflicts)
-        int coord[3][2 * kStageMaxReach + 1][kStageThreads];
-    };
-    uint32_t idx[kStageMaxParts];       // sorted index of each staged particle
+    uint32_t start[kStageMaxCells];     // the cell's first sorted index
     float4 pos[kStageMaxParts];
     Ex ex[kStageMaxParts];
     int box[6];                         // x0, y0, z0, nx, ny, nz
@@ -62,7 +56,8 @@ struct StageSmem {
 template <class Ex, class Fetch>
 __device__ __forceinline__ bool stage_block(const DevParams& P, uint32_t i0, const float4* __restrict__ pa,
                                             const float4* __restrict__ p, const uint32_t* __restrict__ cs,
-                                            const uint32_t* __restrict__ ce, StageSmem<Ex>& sm, Fetch fetch) {
+                                            const uint32_t* __restrict__ ce, StageSmem<Ex>& sm, Fetch fetch,
+                                            uint32_t& own) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const uint32_t N = P.N;
     const uint32_t i = i0 + tid;
@@ -154,65 +149,96 @@ __device__ __forceinline__ bool stage_block(const DevParams& P, uint32_t i0, con
     }
     if (tid == kStageThreads - 1) sm.off[ncells] = (uint16_t)total;
     __syncthreads();
-    // copy: one thread per cell (consecutive z cells sit at nearby sorted indices)
-    for (uint32_t c = tid; c < ncells; c += kStageThreads) {
-        const uint32_t o0 = sm.off[c], o1 = sm.off[c + 1], s = sm.start[c];
-        for (uint32_t k = 0; k < o1 - o0; ++k) {
-            const uint32_t j = s + k;
-            sm.idx[o0 + k] = j;
-            sm.pos[o0 + k] = __ldg(p + j);
-            sm.ex[o0 + k] = fetch(j);
+    // copy: one thread per slot (its cell by binary search over the offsets), loads of four slots
+    // in flight at once
+    for (uint32_t k0 = tid; k0 < total; k0 += 4 * kStageThreads) {
+        uint32_t j[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t k = k0 + u * kStageThreads;
+            j[u] = 0xFFFFFFFFu;
+            if (k < total) {
+                uint32_t lo = 0, hi = ncells;   // the last cell with off <= k
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (sm.off[mid] <= k) lo = mid; else hi = mid;
+                }
+                j[u] = sm.start[lo] + (k - sm.off[lo]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t k = k0 + u * kStageThreads;
+            if (k < total) {
+                sm.pos[k] = __ldg(p + j[u]);
+                sm.ex[k] = fetch(j[u]);
+            }
         }
     }
-    __syncthreads();   // sm.start is dead from here on (its space holds the walk's coordinates)
+    // this thread's own slot (its list skips it): its cell's first slot + its place in the cell
+    own = 0xFFFFu;
+    if (i < N) {
+        const float4 a = pa[i];
+        const int cx = cell_coord(a.x) - x0, cy = cell_coord(a.y) - y0, cz = cell_coord(a.z) - z0;
+        const uint32_t c = (uint32_t)((cx * ny + cy) * nz + cz);
+        const uint32_t st = sm.start[c];
+        if (st <= i && i - st < (uint32_t)(sm.off[c + 1] - sm.off[c])) own = sm.off[c] + (i - st);
+    }
+    __syncthreads();
     return true;
 }
 
 // Particle i's list over the staged box, in the reference's order, with the cap M.  `pa_i` is
 // the particle's anchor.  Returns the list length.
+// Box-relative cell coordinate at offsets -R..R of one axis: base + a + R where every offset lands
+// one cell after the previous one (the usual case), else computed with the reference's float rule.
+struct AxisCells {
+    int base;        // coordinate at offset -R
+    bool regular;
+    float p;
+    int o;           // box origin
+    __device__ __forceinline__ int at(const DevParams& P, int a, int R) const {
+        return regular ? base + a + R : cell_coord(__fmaf_rn((float)a, P.d, p)) - o;
+    }
+};
+__device__ __forceinline__ AxisCells axis_cells(const DevParams& P, float p, int o, int R) {
+    AxisCells ax{cell_coord(__fmaf_rn((float)-R, P.d, p)) - o, true, p, o};
+    for (int a = -R; a < R; ++a)
+        ax.regular = ax.regular && cell_coord(__fmaf_rn((float)(a + 1), P.d, p)) == cell_coord(__fmaf_rn((float)a, P.d, p)) + 1;
+    return ax;
+}
+
+// Particle i's list over the staged box, in the reference's order, with the cap M.  `pa_i` is
+// the particle's anchor, `own` its staged slot.  Returns the list length.
 template <class V, class Ex>
-__device__ __forceinline__ uint32_t walk_staged(const DevParams& P, uint32_t i, float4 pa_i, StageSmem<Ex>& sm,
+__device__ __forceinline__ uint32_t walk_staged(const DevParams& P, float4 pa_i, uint32_t own, const StageSmem<Ex>& sm,
                                                 V& vis) {
     const uint32_t M = P.M;
     if (M == 0) return 0;
     const int R = list_reach(P);
     const int ny = sm.box[4], nz = sm.box[5];
-    // box-relative coordinates of the cells at offsets -R..R on each axis (the reference's float
-    // cell rule: morton(p + a * d)); this thread's column of sm.coord
-    const int t = threadIdx.x;
-    for (int a = -R; a <= R; ++a) {
-        sm.coord[0][a + kStageMaxReach][t] = cell_coord(__fmaf_rn((float)a, P.d, pa_i.x)) - sm.box[0];
-        sm.coord[1][a + kStageMaxReach][t] = cell_coord(__fmaf_rn((float)a, P.d, pa_i.y)) - sm.box[1];
-        sm.coord[2][a + kStageMaxReach][t] = cell_coord(__fmaf_rn((float)a, P.d, pa_i.z)) - sm.box[2];
-    }
-#define CX(a) sm.coord[0][(a) + kStageMaxReach][t]
-#define CY(a) sm.coord[1][(a) + kStageMaxReach][t]
-#define CZ(a) sm.coord[2][(a) + kStageMaxReach][t]
+    const AxisCells X = axis_cells(P, pa_i.x, sm.box[0], R), Y = axis_cells(P, pa_i.y, sm.box[1], R),
+                    Z = axis_cells(P, pa_i.z, sm.box[2], R);
     uint32_t cnt = 0;
     // the staged slots [s0, s1); returns true when the cap is reached
     auto run = [&](uint32_t s0, uint32_t s1, bool contact) -> bool {
 #pragma unroll 2
         for (uint32_t k = s0; k < s1; ++k) {
-            const uint32_t j = sm.idx[k];
-            if (j == i) continue;
-            vis.add(contrib_of(vis, j, sm.pos[k], sm.ex[k], contact), contact);
+            if (k == own) continue;
+            vis.add(contrib_of(vis, 0u, sm.pos[k], sm.ex[k], contact), contact);
             if (++cnt == M) return true;
         }
         return false;
     };
     // cells c_lo..c_hi (offsets) of column (a, b): one run when their cells follow each other
-    // every z offset lands exactly one cell after the previous one (not so near 0, where offsets
-    // clamp to cell 0, or where p + a rounds across a cell boundary)
-    bool zregular = true;
-    for (int c = -R; c < R; ++c) zregular = zregular && CZ(c + 1) == CZ(c) + 1;
     auto column = [&](int a, int b, int c_lo, int c_hi, bool contact) -> bool {
-        const int col = (CX(a) * ny + CY(b)) * nz;
-        if (zregular || c_lo == c_hi) {
-            const int f = col + CZ(c_lo), l = col + CZ(c_hi);
+        const int col = (X.at(P, a, R) * ny + Y.at(P, b, R)) * nz;
+        if (Z.regular || c_lo == c_hi) {
+            const int f = col + Z.at(P, c_lo, R), l = col + Z.at(P, c_hi, R);
             return run(sm.off[f], sm.off[l + 1], contact);
         }
         for (int c = c_lo; c <= c_hi; ++c) {
-            const int f = col + CZ(c);
+            const int f = col + Z.at(P, c, R);
             if (run(sm.off[f], sm.off[f + 1], contact)) return true;
         }
         return false;
@@ -237,9 +263,6 @@ __device__ __forceinline__ uint32_t walk_staged(const DevParams& P, uint32_t i, 
                 }
     }
     return cnt;
-#undef CX
-#undef CY
-#undef CZ
 }
 
 // Whether the staged kernels may take a frame's passes: one scene, reach within kStageMaxReach.
@@ -250,7 +273,7 @@ __host__ __forceinline__ bool staged_supported(const DevParams& P) {
 }
 
 // computeLambda over the staged neighbourhood (the frame's later lambda passes).
-__global__ void __launch_bounds__(kStageThreads)
+__global__ void __launch_bounds__(kStageThreads, 6)
 lambda_staged_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
                      const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float* __restrict__ lambda,
                      CoopSet C, NbList F) {
@@ -260,14 +283,15 @@ lambda_staged_kernel(DevParams P, const float4* __restrict__ p, const float4* __
         return;
     }
     const uint32_t i0 = (blockIdx.x - C.blocks) * kStageThreads;
-    const bool staged = stage_block(P, i0, pa, p, cs, ce, sm, [&](uint32_t) { return NoExtra{}; });
+    uint32_t own;
+    const bool staged = stage_block(P, i0, pa, p, cs, ce, sm, [&](uint32_t) { return NoExtra{}; }, own);
     const uint32_t i = i0 + threadIdx.x;
     if (i >= P.N) return;
     const uint32_t fm = F.meta[i];
     if (fm == kListOff) return;   // walked by the cooperative blocks
     const float4 pi = p[i];
     LambdaVisit vis(P, pi);
-    if (staged) walk_staged(P, i, pa[i], sm, vis);
+    if (staged) walk_staged(P, pa[i], own, sm, vis);
     else walk_list(F, i, fm, p, vis);
     lambda[i] = vis.finish(P.rho0);
 }
@@ -275,7 +299,7 @@ lambda_staged_kernel(DevParams P, const float4* __restrict__ p, const float4* __
 // computeDeltaPositions + solveCollisions + applyDeltaPositions (+ updatePositions) over the
 // staged neighbourhood.
 template <uint32_t kMode>
-__global__ void __launch_bounds__(kStageThreads)
+__global__ void __launch_bounds__(kStageThreads, 6)
 delta_staged_kernel(DevParams P, uint32_t mode_rt, const float4* __restrict__ pin, const float4* __restrict__ pa,
                     float4* __restrict__ pout, float4* __restrict__ x, float4* __restrict__ v,
                     const float* __restrict__ lambda, const float* __restrict__ w, float4* __restrict__ delta,
@@ -288,8 +312,9 @@ delta_staged_kernel(DevParams P, uint32_t mode_rt, const float4* __restrict__ pi
     }
     const uint32_t i0 = (blockIdx.x - C.blocks) * kStageThreads;
     const bool dd = (mode & kDoDelta) != 0;
+    uint32_t own;
     const bool staged = stage_block(P, i0, pa, pin, cs, ce, sm,
-                                    [&](uint32_t j) { return dd ? __ldg(lambda + j) : 0.0f; });
+                                    [&](uint32_t j) { return dd ? __ldg(lambda + j) : 0.0f; }, own);
     const uint32_t i = i0 + threadIdx.x;
     if (i >= P.N) return;
     const uint32_t fm = F.meta[i];
@@ -299,7 +324,7 @@ delta_staged_kernel(DevParams P, uint32_t mode_rt, const float4* __restrict__ pi
     const float4 xi = need_x ? x[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float li = dd ? lambda[i] : 0.f;
     DeltaVisit vis(P, lambda, w, pi, li, w ? w[i] : 1.0f, dd, (mode & kDoCollide) != 0, xi);
-    if (staged) walk_staged(P, i, pa[i], sm, vis);
+    if (staged) walk_staged(P, pa[i], own, sm, vis);
     else walk_list<false, kListBatch>(F, i, fm, pin, vis);
     delta_finish(P, P.rho0, mode, i, vis, pout, x, v, delta);
 }

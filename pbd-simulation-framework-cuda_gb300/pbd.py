@@ -21,7 +21,7 @@ ACTIVE = {
     "computeOmegas": 1 << 7, "computeVorticity": 1 << 8, "computeViscosity": 1 << 9,
 }
 ACTIVE_ALL = 0x3FF
-FLAG_CELL_END_QUIRK, FLAG_TRACK_IDS, FLAG_COLORS, FLAG_FULL_WALK, FLAG_LIST_PASSES, FLAG_STAGED_PASSES = 1, 2, 4, 8, 16, 32
+FLAG_CELL_END_QUIRK, FLAG_TRACK_IDS, FLAG_COLORS, FLAG_FULL_WALK, FLAG_STAGED_PASSES = 1, 2, 4, 8, 32
 
 EXPORTED = [
     "pbd_params_default", "pbd_load_config", "pbd_parse_config", "pbd_write_config", "pbd_validate_params",

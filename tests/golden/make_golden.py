@@ -13,8 +13,11 @@ Scenes:
   h1_quirk    the h = 1 workload parameters with rest density 1e5, vorticity 5e-4 and XSPH 0.01,
               8^3 particles with random velocities (seed 8): cell N-1 = 511 is occupied, so
               SortReorder.h:183-184 stretches its range to N
+  dense       the density-active workload's parameters (fluid_1m_dense: poly6 width 4.1, spiky
+              3.5 diameters, two shells, rest density 1995, eps 1e-4, 4 iterations, dt 1/60,
+              vorticity 5e-4, XSPH 1.5e-4) on a 10^3 unit lattice in a 24^3-cell box, seed 9
 For each: the front of a frame (keys, permutation, state), the neighbour lists, and the state,
-lambda, omega and f_ext after 1 and 3 frames.
+lambda, omega and f_ext after 1, 3 and 10 frames.
 """
 import os
 import sys
@@ -48,7 +51,16 @@ def scene_h1_quirk():
     return p, pos, vel
 
 
-SCENES = {"config_txt": scene_config_txt, "h1_quirk": scene_h1_quirk}
+def scene_dense():
+    p, pos, vel, _ = scenes.workload("fluid_1m_dense", pbd, shape=(10, 10, 10))
+    for a in range(3):
+        p.bounds_max[a] = 22.5
+    pos, vel = scenes.lattice(10, 10, 10, seed=9)
+    return p, pos, vel
+
+
+SCENES = {"config_txt": scene_config_txt, "h1_quirk": scene_h1_quirk, "dense": scene_dense}
+FRAMES = (1, 3, 10)
 
 
 def params_array(p):
@@ -71,16 +83,23 @@ def generate(name):
     out["list_count"], out["list_contacts"] = cnt, con
     out["list_entries"] = np.concatenate([lst[i, :cnt[i]] for i in range(len(cnt))]).astype(np.uint32)
     r.close()
-    for frames in (1, 3):
-        r = RefExec(p, WIDTH)
-        r.add_particles(pos, vel)
-        r.step(frames)
-        d, s = r.debug(), r.state()
-        for k in ("x", "v", "p"):
-            out[f"f{frames}_{k}"] = s[k]
-        for k in ("perm", "lambda", "omega", "fext"):
-            out[f"f{frames}_{k}"] = d[k]
-        r.close()
+    # one frame at a time: each frame's sort permutation carries the particles' input indices
+    # along (ids), so later frames can be compared particle by particle
+    r = RefExec(p, WIDTH)
+    r.add_particles(pos, vel)
+    ids = np.arange(len(pos), dtype=np.uint32)
+    for frame in range(1, max(FRAMES) + 1):
+        r.step(1)
+        d = r.debug()
+        ids = ids[d["perm"]]
+        if frame in FRAMES:
+            s = r.state()
+            for k in ("x", "v", "p"):
+                out[f"f{frame}_{k}"] = s[k]
+            for k in ("perm", "lambda", "omega", "fext"):
+                out[f"f{frame}_{k}"] = d[k]
+            out[f"f{frame}_ids"] = ids.copy()
+    r.close()
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
     return out
 

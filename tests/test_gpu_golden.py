@@ -2,11 +2,11 @@
 
 Bit-exact: keys, permutation and state after the front of a frame; neighbour lists with both
 walkers.  Tolerance: state after 1 and 3 frames (FP32 with hardware sqrt/rsqrt/division in the
-neighbour passes), lambda, omega."""
+neighbour passes), lambda, omega, f_ext; the state after 10 frames particle by particle."""
 import numpy as np
 import pytest
 
-from helpers import GOLDEN_SCENES, golden_lists, load_golden, scale
+from helpers import GOLDEN_SCENES, check_fext, check_ten_frames, golden_frame_tolerances, golden_lists, load_golden, scale
 
 pytestmark = pytest.mark.gpu
 CAP = 1024
@@ -43,7 +43,7 @@ def test_gpu_lists_match_reference(need_gpu, pbd, name, walker):
 @pytest.mark.parametrize("name", GOLDEN_SCENES)
 def test_gpu_frames_match_reference(need_gpu, pbd, name):
     g = load_golden(pbd, name)
-    for frames, tx, tv in ((1, 2e-5, 3e-3), (3, 1e-4, 2e-2)):
+    for frames, tx, tv in golden_frame_tolerances(name):
         with pbd.Sim(g["params_struct"], CAP) as sim:
             sim.add_particles(g["pos"], g["vel"])
             sim.step(frames)
@@ -56,3 +56,16 @@ def test_gpu_frames_match_reference(need_gpu, pbd, name):
         assert np.max(np.abs(d["lambda"] - lam)) < 1e-3 * scale(lam)
         om = g[f"f{frames}_omega"]
         assert np.max(np.abs(d["omega"][:, :3] - om[:, :3])) < 1e-2 * scale(om)
+        check_fext(d["fext"], g[f"f{frames}_fext"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_SCENES)
+def test_gpu_ten_frames_match_reference(need_gpu, pbd, name):
+    g = load_golden(pbd, name)
+    p = g["params_struct"].copy()
+    p.flags |= pbd.FLAG_TRACK_IDS
+    with pbd.Sim(p, CAP) as sim:
+        sim.add_particles(g["pos"], g["vel"])
+        sim.step(10)
+        sim.sync()
+        check_ten_frames(name, sim.state(), g)

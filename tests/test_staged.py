@@ -1,12 +1,12 @@
-"""Shared-memory-staged neighbour passes against the stored lists and the full cell walk.
+"""Shared-memory-staged neighbour passes (PBD_FLAG_STAGED_PASSES) against the stored lists and
+the full cell walk.
 
-Where the kernel cut covers a particle's whole list (kernel widths of a few cells, as in the
-reference's config.txt), the later lambda passes and the delta passes stage each block's
-neighbourhood in shared memory and walk it in the reference's list order; the results must be
-the same bits as the walk over the stored full lists (PBD_FLAG_LIST_PASSES) and as the cell walk
-of every pass (PBD_FLAG_FULL_WALK), over many frames: the dense regime with its cell-end quirk,
-vorticity and viscosity, fast motion, three shells, unified solids, and the h = 1 regime with
-staging forced (PBD_FLAG_STAGED_PASSES)."""
+With the flag, the later lambda passes and the delta passes stage each block's neighbourhood in
+shared memory and walk it in the reference's list order; the results must be the same bits as
+the default walk over the stored lists and as the cell walk of every pass (PBD_FLAG_FULL_WALK),
+over many frames: the dense regime (kernel widths of a few cells, as in the reference's
+config.txt) with its cell-end quirk, vorticity and viscosity, fast motion, three shells, and the
+h = 1 regime; solids keep the lists."""
 import numpy as np
 import pytest
 
@@ -59,24 +59,26 @@ def test_staged_passes_bit_identical_to_lists_and_walk(need_gpu, pbd, scenes, sh
     pos, vel = scenes.lattice(*shape, seed=5)
     if sigma:
         vel[:, :3] = np.random.default_rng(5).normal(0, sigma, size=(len(vel), 3)).astype(np.float32)
-    a, prof = _run(pbd, params, pos, vel, 30)
+    a, prof = _run(pbd, params, pos, vel, 30, pbd.FLAG_STAGED_PASSES)
     assert "delta_staged" in prof and "lambda_staged" in prof      # the staged kernels ran
-    b, prof_b = _run(pbd, params, pos, vel, 30, pbd.FLAG_LIST_PASSES)
+    b, prof_b = _run(pbd, params, pos, vel, 30)
     assert "delta_staged" not in prof_b
     _same(a, b)
     c, _ = _run(pbd, params, pos, vel, 30, pbd.FLAG_FULL_WALK)
     _same(a, c)
 
 
-def test_staged_passes_with_solids(need_gpu, pbd, scenes):
+def test_solids_keep_the_lists(need_gpu, pbd, scenes):
+    # inverse masses are not staged: a simulation with solids runs the list passes, same bits
     params = dense_params(pbd, scenes, 40)
     fpos, fvel = scenes.lattice(16, 20, 16, seed=6)
     spos = scenes.solid_boxes(2, (4, 4, 6), (22.0, 1.5, 2.0), (38.0, 38.0, 38.0), 9)
     pos = np.concatenate([fpos, spos])
     vel = np.zeros_like(pos)
     w = np.concatenate([np.ones(len(fpos), np.float32), np.zeros(len(spos), np.float32)])
-    a, _ = _run(pbd, params, pos, vel, 20, inv_mass=w)
-    b, _ = _run(pbd, params, pos, vel, 20, pbd.FLAG_LIST_PASSES, inv_mass=w)
+    a, prof = _run(pbd, params, pos, vel, 20, pbd.FLAG_STAGED_PASSES, inv_mass=w)
+    assert "delta_staged" not in prof
+    b, _ = _run(pbd, params, pos, vel, 20, pbd.FLAG_FULL_WALK, inv_mass=w)
     _same(a, b)
 
 
@@ -98,7 +100,7 @@ def test_staged_dense_against_the_oracle(need_gpu, pbd, scenes, oracle_mod):
     params = dense_params(pbd, scenes, 32)
     pos, vel = scenes.lattice(16, 16, 16, seed=8)
     for frames, tol_x, tol_v in ((1, 2e-5, 2e-3), (5, 2e-3, 0.2)):
-        g, prof = _run(pbd, params, pos, vel, frames)
+        g, prof = _run(pbd, params, pos, vel, frames, pbd.FLAG_STAGED_PASSES)
         assert "delta_staged" in prof
         o = oracle_mod.Oracle(params, len(pos), "f32")
         o.add_particles(pos, vel)
