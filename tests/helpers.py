@@ -87,3 +87,22 @@ def check_fext(fext, ref):
     sc = max(float(np.abs(ref[:, :3]).max()), 1e-30)
     d = np.abs(np.asarray(fext)[:, :3] - ref[:, :3]).max(axis=1)
     assert np.percentile(d, 99) < 0.02 * sc and np.mean(d > 0.02 * sc) <= 0.01, (float(np.percentile(d, 99)), float(d.max()), sc)
+
+
+def load_golden(pbd, name):
+    """Inputs and the reference's own outputs (tests/golden/make_golden.py)."""
+    import os
+    d = dict(np.load(os.path.join(GOLDEN_DIR, f"{name}.npz")))
+    d["params_struct"] = pbd.Params.from_buffer_copy(d["params"].tobytes())
+    return d
+
+
+def golden_lists(g):
+    """Per-particle lists from the flattened fixture."""
+    cnt = g["list_count"].astype(np.int64)
+    offs = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+    return [g["list_entries"][int(offs[i]):int(offs[i + 1])] for i in range(len(cnt))]
+
+
+def scale(a):
+    return max(1.0, float(np.max(np.abs(a))))
