@@ -1,7 +1,7 @@
 """Benchmark of the GB300 PBD step: particle-steps/s on the 1M-particle fluid workloads.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
-                    [--leg contacts|batched|solids|adjoint|dense]
+                    [--leg contacts|batched|batched_frames|solids|adjoint|dense|render]
 
 Our arm (default): the headline workload fluid_1m -- 100^3 = 1,000,000 fluid particles in a
 128^3-cell domain (seed 2), kernel radius 1, 4 solver iterations, vorticity 5e-4, XSPH 0.01,
@@ -612,7 +612,7 @@ def traffic_of(name, kernel):
         return None
 
 
-def measure_workload(torch, pbd, scenes, name, args, stream, sh, world, dev, local, extra=None):
+def measure_workload(torch, pbd, scenes, name, args, stream, sh, world, dev, local, extra=None, staged_compare=False):
     """value, e2e, clocks, roofline, per-kernel time and density error of one workload: W warm-up
     frames, K timed frames (graph replays, CUDA events), K profiled frames, then e2e over the
     same frames as the timed ones on a fresh simulation."""
@@ -714,6 +714,29 @@ def measure_workload(torch, pbd, scenes, name, args, stream, sh, world, dev, loc
     sim.sync()
     sim.close()
 
+    staged = None
+    if staged_compare:
+        # the same K frames with the shared-memory-staged lambda and delta passes
+        # (PBD_FLAG_STAGED_PASSES), on a fresh simulation after the same warm-up
+        ps = params.copy()
+        ps.flags |= pbd.FLAG_STAGED_PASSES
+        with pbd.Sim(ps, n) as sim:
+            sim.add_particles(pos, vel)
+            sim.step(args.warmup, stream=sh)
+            stream.synchronize()
+            e0, e1 = _events(torch)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            sim.step(args.steps, stream=sh)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            sim.sync()
+            sprof = sim.profile(args.steps, stream=sh)
+            sim.sync()
+        sms = e0.elapsed_time(e1) / args.steps
+        staged = {"ms_per_step": sms, "value": n * 1e3 / sms, "vs_lists": (ms / args.steps) / sms,
+                  "kernel_ms_per_frame": {k: v[1] / args.steps for k, v in sprof.items()}}
+
     bps = algorithmic_bytes_per_particle_step(params.solver_iterations, 3,
                                               bool(params.active & (pbd.ACTIVE["computeOmegas"] | pbd.ACTIVE["computeViscosity"])))
     return {
@@ -730,6 +753,7 @@ def measure_workload(torch, pbd, scenes, name, args, stream, sh, world, dev, loc
                           "frac": bps * value / world / 1e9 / peak},
         "kernel_ms_per_frame": {k: v[1] / args.steps for k, v in prof.items()},
         "density_error": density,
+        **({"staged_passes": staged} if staged is not None else {}),
         **out_extra,
     }
 
@@ -766,7 +790,7 @@ def run_ours(args):
 
     dense = None
     if args.workload != DENSE:
-        dense = leg(measure_workload, torch, pbd, scenes, DENSE, args, stream, sh, world, dev, local)
+        dense = leg(measure_workload, torch, pbd, scenes, DENSE, args, stream, sh, world, dev, local, staged_compare=True)
     batched = leg(run_batched, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 60)))
     solids = leg(run_solids, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 100)))
     adjoint = leg(run_adjoint, torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check)
@@ -805,7 +829,26 @@ def run_leg(args):
     elif args.leg == "solids":
         out = run_solids(torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 100)))
     elif args.leg == "dense":
-        out = measure_workload(torch, pbd, scenes, DENSE, args, stream, sh, 1, torch.device("cuda", 0), 0)
+        out = measure_workload(torch, pbd, scenes, DENSE, args, stream, sh, 1, torch.device("cuda", 0), 0,
+                               staged_compare=True)
+    elif args.leg == "batched_frames":
+        # the 256-scene batch alone: W + K frames (a profiler target; no tuning, no single scenes)
+        sl = scenes.batched_scenes()
+        shared = scenes.workload_params(pbd, 64, 1000.0)
+        shared.lambda_epsilon = 0.1
+        descs = [pbd.scene_desc(sc["n"], sc["rest_density"], sc["gravity"], sc["box"]) for sc in sl]
+        with pbd.Batch(shared, descs) as b:
+            for k, sc in enumerate(sl):
+                b.add_particles(k, sc["pos"], sc["vel"])
+            b.step(args.warmup + args.steps, stream=sh)
+            b.sync()
+        out = {"scenes": len(sl), "frames": args.warmup + args.steps}
+    elif args.leg == "render":
+        params, pos, vel, _ = build_workload(pbd, scenes, "fluid_1m")
+        with pbd.Sim(params, len(pos)) as sim:
+            sim.add_particles(pos, vel)
+            sim.step(args.warmup + args.steps, stream=sh)
+            out = run_render(torch, pbd, sim, stream, sh, reps=3)
     else:
         out = run_adjoint(torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check)
     print(json.dumps({"leg": args.leg, **out}), flush=True)
@@ -821,7 +864,7 @@ def main():
     ap.add_argument("--workload", default="fluid_1m")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-fd-check", action="store_true", help="skip the FP64 finite-difference check of the adjoint")
-    ap.add_argument("--leg", choices=["contacts", "batched", "solids", "adjoint", "dense"],
+    ap.add_argument("--leg", choices=["contacts", "batched", "batched_frames", "solids", "adjoint", "dense", "render"],
                     help="measure only this secondary workload and print its result (not the bench line)")
     args = ap.parse_args()
     if args.warmup < 3:
