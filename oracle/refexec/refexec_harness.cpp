@@ -131,7 +131,8 @@ int refx_step_phase(int phase) {
     const pbd_params& p = H.prm;
     setup_frame();                                       // initializeFrame
     if (H.N == 0) return 0;                              // Fluid.cu:19
-    if (p.collision_type != 0) return 6;
+    if (p.collision_type > 1) return 6;
+    const bool batches = p.collision_type == 1;
     if (p.active & PBD_ACTIVE_APPLY_FORCES) cudaCallApplyForces();
     cudaCallInitializeCellIds();
     sortIds();
@@ -139,6 +140,7 @@ int refx_step_phase(int phase) {
     cudaCallResetCellInfo();
     cudaCallComputeCellInfo();
     if (phase == 1) return 0;
+    if (batches) cudaCallResetContacts();                // Fluid.cu:37-39
     if (p.active & PBD_ACTIVE_FIND_CONTACTS) cudaCallFindContacts();
     if (p.active & PBD_ACTIVE_FIND_NEIGHBOURS) cudaCallFindNeighbours();
     if (phase == 2) return 0;
@@ -146,9 +148,23 @@ int refx_step_phase(int phase) {
         if (p.active & PBD_ACTIVE_COMPUTE_LAMBDA) cudaCallComputeLambda();
         if (p.active & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS) cudaCallComputeDeltaPositions();
         for (unsigned k = 0; k < p.stabilization_iterations; ++k) {
-            defer_atomics = true;
-            cudaCallSolveCollisions();
-            defer_atomics = false;
+            if (!batches) {
+                defer_atomics = true;
+                cudaCallSolveCollisions();
+                defer_atomics = false;
+                continue;
+            }
+            // Fluid.cu:62-72.  Threads run one after another in grid order, so each batch is the
+            // greedy matching of the pending list entries in index order -- one legal schedule of
+            // setupCollisionConstraintBatches (whose blocks race and whose __syncthreads sits in
+            // divergent code, Collision.h:359-369); it agrees with every other schedule on scenes
+            // where each particle has at most one partner.
+            cudaCallResetContactConstraintSuccess();
+            for (unsigned b = 0; b < p.max_collision_batches; ++b) {
+                cudaCallResetContactConstraintParticleUsed();
+                cudaCallSetupCollisionConstraintBatches();
+                cudaCallSetupCollisionConstraintBatchesCheck();
+            }
         }
         if (p.active & PBD_ACTIVE_APPLY_DELTA_POSITIONS) cudaCallApplyDeltaPositions();
     }

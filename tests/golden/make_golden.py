@@ -16,6 +16,9 @@ Scenes:
   dense       the density-active workload's parameters (fluid_1m_dense: poly6 width 4.1, spiky
               3.5 diameters, two shells, rest density 1995, eps 1e-4, 4 iterations, dt 1/60,
               vorticity 5e-4, XSPH 1.5e-4) on a 10^3 unit lattice in a 24^3-cell box, seed 9
+  contact_pairs  collisionType 1 (16 batches) on 216 isolated overlapping pairs, the h = 1 workload
+              parameters with the density solve off: the reference's own claim and solve kernels
+              (Collision.h:344-459)
 For each: the front of a frame (keys, permutation, state), the neighbour lists, and the state,
 lambda, omega and f_ext after 1, 3 and 10 frames.
 """
@@ -59,7 +62,35 @@ def scene_dense():
     return p, pos, vel
 
 
-SCENES = {"config_txt": scene_config_txt, "h1_quirk": scene_h1_quirk, "dense": scene_dense}
+def scene_contact_pairs():
+    """collisionType 1 on 216 isolated overlapping pairs (separations 0.55-0.95 of a diameter,
+    seeded directions), 4 cells apart: every particle's list holds its partner alone, so each batch
+    of the reference's claim kernel pairs the same particles whatever its schedule."""
+    p = scenes.workload_params(pbd, 32, 1000.0)
+    p.collision_type = 1
+    p.max_collision_batches = 16
+    # the contact projection alone (no density solve): forces, the lists, the batches, the update
+    A = pbd.ACTIVE
+    p.active = A["applyForces"] | A["findContacts"] | A["findNeighbours"] | A["updatePositions"]
+    u = scenes.uniform01(11, 4 * 216).reshape(216, 4)
+    pos = np.zeros((432, 4), np.float32)
+    k = 0
+    for a in range(6):
+        for b in range(6):
+            for c in range(6):
+                centre = np.array([4.0 + 4 * a, 4.0 + 4 * b, 4.0 + 4 * c]) + 0.5
+                z = 2.0 * u[k, 0] - 1.0
+                phi = 2.0 * np.pi * u[k, 1]
+                d = np.array([np.sqrt(1.0 - z * z) * np.cos(phi), np.sqrt(1.0 - z * z) * np.sin(phi), z])
+                sep = 0.55 + 0.4 * u[k, 2]
+                pos[2 * k, :3] = centre - 0.5 * sep * d
+                pos[2 * k + 1, :3] = centre + 0.5 * sep * d
+                k += 1
+    return p, pos, np.zeros_like(pos)
+
+
+SCENES = {"config_txt": scene_config_txt, "h1_quirk": scene_h1_quirk, "dense": scene_dense,
+          "contact_pairs": scene_contact_pairs}
 FRAMES = (1, 3, 10)
 
 

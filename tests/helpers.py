@@ -48,7 +48,7 @@ def setup_pair(pbd, oracle_mod, params, pos, vel, precision="f32", capacity=None
 
 
 GOLDEN_DIR = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.abspath(__file__)), "golden")
-GOLDEN_SCENES = ("config_txt", "h1_quirk", "dense")
+GOLDEN_SCENES = ("config_txt", "h1_quirk", "dense", "contact_pairs")
 
 # Ten frames against the reference, particle by particle (ids carried by the frames' sort
 # permutations): the largest, 99th-percentile and median position / velocity difference per scene.
@@ -59,6 +59,7 @@ GOLDEN_TEN = {
     "config_txt": dict(x=(1e-3, 1e-3, 1e-4), v=(2e-2, 2e-2, 2e-3)),
     "dense": dict(x=(0.2, 2e-2, 2e-3), v=(5.0, 1.0, 5e-2)),
     "h1_quirk": dict(x=(2.0, 0.5, 2e-2), v=(100.0, 30.0, 2.0)),
+    "contact_pairs": dict(x=(1e-4, 1e-4, 1e-4), v=(1e-2, 1e-2, 1e-2)),
 }
 
 
