@@ -354,6 +354,11 @@ def run_batched(torch, pbd, scenes, stream, sh, frames):
     b.sync()
     ms_batch = e0.elapsed_time(e1) / frames
     launches = b.launches_per_step()
+    # the same frames' kernels one by one (direct launches, an event pair around each): what the
+    # graph's frame costs beyond its kernels is the room a persistent kernel could win back
+    prof = b.profile(frames, stream=sh)
+    b.sync()
+    kernel_sum = sum(v[1] for v in prof.values()) / frames
     b.close()
     sims = []
     for sc in sl:
@@ -383,7 +388,9 @@ def run_batched(torch, pbd, scenes, stream, sh, frames):
     return {"workload": "batched_256", "scenes": len(sl), "particles": total, "frames": frames,
             "ms_per_frame": ms_batch, "scenes_per_s": len(sl) * 1e3 / ms_batch,
             "particle_steps_per_s": total * 1e3 / ms_batch, "launches_per_frame": launches,
-            "neighbour_block": block, "one_by_one_ms_per_frame": ms_one,
+            "neighbour_block": block, "kernel_ms_per_frame": {k: v[1] / frames for k, v in prof.items()},
+            "kernel_sum_ms_per_frame": kernel_sum, "graph_minus_kernels_ms": ms_batch - kernel_sum,
+            "one_by_one_ms_per_frame": ms_one,
             "one_by_one_scenes_per_s": len(sl) * 1e3 / ms_one, "speedup_vs_one_by_one": ms_one / ms_batch}
 
 

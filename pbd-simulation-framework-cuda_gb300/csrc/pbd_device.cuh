@@ -20,6 +20,8 @@ struct SceneParams {
     float rho0;            // Density.restDensity of this scene
     float gravity;         // Forces.gravity of this scene
     float bmin[3], bmax[3];
+    uint32_t base;         // first entry of the scene's slice of the cell tables
+    uint32_t cells;        // the slice's size: the Morton cube (power-of-two side) that holds its walls
 };
 
 struct DevParams {
@@ -61,17 +63,28 @@ struct DevParams {
 
 // The scene a particle belongs to, as the walk and the per-scene constants see it.
 struct SceneCtx {
-    uint32_t base;   // first table entry of the scene's cells (scene * G)
+    uint32_t base;   // first table entry of the scene's cells
     uint32_t end;    // one past the scene's last particle in the sorted arrays
     uint32_t n;      // particles in the scene (the reference's numberOfParticles)
     float rho0;
+    uint32_t cells;  // cells of the scene's slice (Morton keys below it are in the tables)
 };
 
 __device__ __forceinline__ SceneCtx scene_ctx(const DevParams& P, uint32_t i) {
-    if (!P.batched) return SceneCtx{0u, P.N, P.N, P.rho0};
+    if (!P.batched) return SceneCtx{0u, P.N, P.N, P.rho0, P.G};
     const uint32_t sc = P.scene_of[i];
     const uint32_t s = P.scene_range[2 * sc], e = P.scene_range[2 * sc + 1];
-    return SceneCtx{sc * P.G, e, e - s, P.scenes[sc].rho0};
+    return SceneCtx{P.scenes[sc].base, e, e - s, P.scenes[sc].rho0, P.scenes[sc].cells};
+}
+
+// The scene whose slice holds table entry `key` (slices are in scene order): binary search.
+__device__ __forceinline__ uint32_t scene_of_key(const DevParams& P, uint32_t key) {
+    uint32_t lo = 0, hi = P.nscenes;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (P.scenes[mid].base <= key) lo = mid; else hi = mid;
+    }
+    return lo;
 }
 
 // ---------------------------------------------------------------- Morton (Hash.h) -----

@@ -98,9 +98,10 @@ predict_key_kernel(DevParams P, float4* __restrict__ x, float4* __restrict__ v, 
             pp = p[i];
         }
         uint32_t key = morton(pp.x, pp.y, pp.z);
-        if (P.batched) {                         // scene-major key: scenes sort apart
-            if (key >= P.G) { atomicOr(err, kErrKeyBits); key = P.G - 1u; }
-            key += sc * P.G;
+        if (P.batched) {                         // the scene's slice: scenes sort apart
+            const uint32_t cells = P.scenes[sc].cells;
+            if (key >= cells) { atomicOr(err, kErrKeyBits); key = cells - 1u; }
+            key += P.scenes[sc].base;
         }
         keys[i] = key;
         for (int ps = 0; ps < npasses; ++ps) atomicAdd(&sh[ps * kRadix + ((key >> (ps * kRadixBits)) & (kRadix - 1))], 1u);
@@ -157,10 +158,11 @@ reorder_cells_kernel(DevParams P, ReorderArgs A, SortScratch S, int npasses, uin
             if (i == N - 1 || A.skeys[i + 1] != k) A.cell_end[k] = i + 1;
         }
         if (P.batched) {                         // scene of each sorted slot and each scene's range
-            const uint32_t sc = k / P.G;
+            const uint32_t sc = scene_of_key(P, k);
+            const uint32_t lo = P.scenes[sc].base, hi = lo + P.scenes[sc].cells;
             P.scene_of[i] = sc;
-            if (i == 0 || A.skeys[i - 1] / P.G != sc) P.scene_range[2 * sc] = i;
-            if (i == N - 1 || A.skeys[i + 1] / P.G != sc) P.scene_range[2 * sc + 1] = i + 1;
+            if (i == 0 || A.skeys[i - 1] < lo) P.scene_range[2 * sc] = i;
+            if (i == N - 1 || A.skeys[i + 1] >= hi) P.scene_range[2 * sc + 1] = i + 1;
         }
     }
 }

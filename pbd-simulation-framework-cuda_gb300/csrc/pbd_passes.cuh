@@ -106,10 +106,10 @@ __device__ __forceinline__ void for_each_range(const DevParams& P, const SceneCt
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     h[c] = hxy + mz[c];
-                    cs3[c] = h[c] < P.G ? __ldg(cs + S.base + h[c]) : kEmptyCell;
+                    cs3[c] = h[c] < S.cells ? __ldg(cs + S.base + h[c]) : kEmptyCell;
                 }
 #pragma unroll
-                for (int c = 0; c < 3; ++c) ce3[c] = h[c] < P.G ? __ldg(ce + S.base + h[c]) : 0u;
+                for (int c = 0; c < 3; ++c) ce3[c] = h[c] < S.cells ? __ldg(ce + S.base + h[c]) : 0u;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     if (cs3[c] >= N) continue;
@@ -135,7 +135,7 @@ __device__ __forceinline__ void for_each_range(const DevParams& P, const SceneCt
 #pragma unroll 1
                     for (int c = -sh; c <= sh; c += cstep) {
                         const uint32_t h = hx + hy + morton_axis(__fmaf_rn((float)c, P.d, pi.z));
-                        if (h >= P.G) continue;
+                        if (h >= S.cells) continue;
                         const uint32_t s = __ldg(cs + S.base + h);
                         uint32_t e = __ldg(ce + S.base + h);
                         if (s >= N) continue;
@@ -414,10 +414,10 @@ __device__ __forceinline__ uint32_t store_full_list(const DevParams& P, const Sc
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             h[c] = hxy + mz[c];
-            s3[c] = h[c] < P.G ? __ldg(cs + S.base + h[c]) : kEmptyCell;
+            s3[c] = h[c] < S.cells ? __ldg(cs + S.base + h[c]) : kEmptyCell;
         }
 #pragma unroll
-        for (int c = 0; c < 3; ++c) e3[c] = h[c] < P.G ? __ldg(ce + S.base + h[c]) : 0u;
+        for (int c = 0; c < 3; ++c) e3[c] = h[c] < S.cells ? __ldg(ce + S.base + h[c]) : 0u;
         uint32_t len[3];
         uint32_t reach = n;   // entries stored before the cell: the walk reaches it while below the cap
 #pragma unroll

@@ -65,6 +65,7 @@ constexpr int kMaxGraphs = 8;
 // is longer goes to the warp-cooperative cell walk.
 constexpr uint32_t kListMax = 64;    // near list: entries within the cut
 constexpr uint32_t kFullMax = 255;   // full list: every entry of the frame's list (meta holds 8-bit counts)
+constexpr uint32_t kFullSlim = 128;  // the full list's slots when the list covers 27 cells (~32 entries)
 
 constexpr int kThreadsParticle = 256;
 constexpr int kThreadsNeighbourDefault = 128;
@@ -174,6 +175,8 @@ struct pbd_sim {
     uint32_t graph_n = 0xFFFFFFFFu;
     bool dirty = true;
     uint32_t launches = 0;
+    uint32_t batch_cells = 0;                // batched form: cells of all scenes' slices
+    uint32_t fl_slots = 0;                   // slots of the full list per particle
     uint32_t sort_spin_limit = kSpinLimit;   // pbd_debug_set_wait_limit
     uint32_t sort_hold = 0;
 };
@@ -194,15 +197,23 @@ int sort_passes(const pbd_sim* s) {
     // With applyForces on, every key comes from a position clamped inside the enclosure, whose
     // limits are at most 126.5 (Communication.h:573-598): keys < 2^21, three 8-bit digits.
     // The batched form prefixes the scene number: 21 + log2(scenes) bits.
-    if (s->batched) {
-        uint32_t bits = 21;
-        while ((1u << (bits - 21)) < s->nscenes) ++bits;
+    if (s->batched) {   // keys run up to the last scene's slice end
+        uint32_t bits = 1;
+        while (bits < 32 && (1ull << bits) < s->batch_cells) ++bits;
         return std::min(kMaxPasses, (int)((bits + kRadixBits - 1) / kRadixBits));
     }
     return (s->prm.active & PBD_ACTIVE_APPLY_FORCES) ? 3 : 4;
 }
 
-uint32_t table_size(const pbd_sim* s) { return s->prm.max_grid * (s->batched ? s->nscenes : 1u); }
+uint32_t host_expand_bits(uint32_t v) {   // Hash.h:10-16, for the scenes' table slices
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+uint32_t table_size(const pbd_sim* s) { return s->batched ? s->batch_cells : s->prm.max_grid; }
 
 float powi_host(float x, int n) {
     float r = 1.0f;
@@ -419,7 +430,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const NbList L0{nullptr, nullptr, 0u, 0u};
     // full lists: stored by the first lambda pass of the frame (its walk of the anchor cells)
     const bool use_full = !(prm.flags & PBD_FLAG_FULL_WALK) && (act & PBD_ACTIVE_COMPUTE_LAMBDA) && I > 0;
-    const NbList F = use_full ? NbList{s->fl_list, s->fl_meta, s->cap, kFullMax} : L0;
+    const NbList F = use_full ? NbList{s->fl_list, s->fl_meta, s->cap, s->fl_slots} : L0;
     // PBD_FLAG_STAGED_PASSES: the later lambda passes and the delta passes stage each block's
     // neighbourhood in shared memory (the full list stays the fallback); inverse masses are not
     // staged, so simulations with solids read the lists
@@ -781,6 +792,7 @@ int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<Scene
         s->batched = true;
         s->nscenes = (uint32_t)scenes->size();
         s->h_scenes = *scenes;
+        s->batch_cells = scenes->back().base + scenes->back().cells;
         s->scene_cap = *caps;
         s->scene_count.assign(s->nscenes, 0u);
     }
@@ -812,7 +824,10 @@ int create_sim(const pbd_params* prm, uint32_t capacity, const std::vector<Scene
     parts.push_back({(void**)&s->dfr_items, (size_t)s->defer_cap * 4}); parts.push_back({(void**)&s->dfr_count, 8});
     parts.push_back({(void**)&s->dnr_items, (size_t)s->defer_cap * 4}); parts.push_back({(void**)&s->dnr_count, 8});
     parts.push_back({(void**)&s->nb_list, (size_t)kListMax * C * 4}); parts.push_back({(void**)&s->nb_meta, C * 4});
-    parts.push_back({(void**)&s->fl_list, (size_t)kFullMax * C * 4}); parts.push_back({(void**)&s->fl_meta, C * 4});
+    // full-list slots: kFullMax when the parameters reach beyond the 27 cells (shells), else
+    // kFullSlim; longer lists are walked by a warp per particle instead (correct, slower)
+    s->fl_slots = ((prm->active & PBD_ACTIVE_FIND_NEIGHBOURS) && prm->kernel_width_neighbours >= 2) ? kFullMax : kFullSlim;
+    parts.push_back({(void**)&s->fl_list, (size_t)s->fl_slots * C * 4}); parts.push_back({(void**)&s->fl_meta, C * 4});
     if (s->batched) {
         parts.push_back({(void**)&s->d_scenes, (size_t)s->nscenes * sizeof(SceneParams)});
         parts.push_back({(void**)&s->scene_of, C * 4});
@@ -1413,10 +1428,9 @@ int pbd_batch_create(const pbd_params* shared, uint32_t nscenes, const pbd_scene
     if (!shared || !scenes || !out || nscenes == 0) { set_error("pbd_batch_create: bad argument"); return PBD_ERR_INVALID_ARG; }
     *out = nullptr;
     if (shared->max_grid != 128u * 128u * 128u) { set_error("pbd_batch_create: scenes use the 128^3 grid (max_grid)"); return PBD_ERR_UNSUPPORTED; }
-    if ((uint64_t)nscenes * shared->max_grid > (1ull << 32) - 1) { set_error("pbd_batch_create: at most 2047 scenes"); return PBD_ERR_RANGE; }
     std::vector<SceneParams> sp(nscenes);
     std::vector<uint32_t> caps(nscenes);
-    uint64_t total = 0;
+    uint64_t total = 0, cells = 0;
     for (uint32_t k = 0; k < nscenes; ++k) {
         pbd_params q = *shared;   // each scene's values are checked with the reference's ranges
         q.rest_density = scenes[k].rest_density;
@@ -1429,6 +1443,16 @@ int pbd_batch_create(const pbd_params* shared, uint32_t nscenes, const pbd_scene
         sp[k].rho0 = scenes[k].rest_density;
         sp[k].gravity = scenes[k].gravity;
         for (int a = 0; a < 3; ++a) { sp[k].bmin[a] = scenes[k].bounds_min[a]; sp[k].bmax[a] = scenes[k].bounds_max[a]; }
+        // the scene's slice of the cell tables: every Morton key of a cell its walls enclose (keys
+        // come from positions clamped to the walls; the key grows with each coordinate, so the
+        // far corner's key is the largest)
+        const uint32_t tx = (uint32_t)std::min(127.f, std::max(0.f, scenes[k].bounds_max[0]));
+        const uint32_t ty = (uint32_t)std::min(127.f, std::max(0.f, scenes[k].bounds_max[1]));
+        const uint32_t tz = (uint32_t)std::min(127.f, std::max(0.f, scenes[k].bounds_max[2]));
+        sp[k].base = (uint32_t)cells;
+        sp[k].cells = (host_expand_bits(tx) << 2) + (host_expand_bits(ty) << 1) + host_expand_bits(tz) + 1u;
+        cells += sp[k].cells;
+        if (cells > (1ull << 32) - 1) { set_error("pbd_batch_create: the scenes' cell tables exceed 2^32 cells"); return PBD_ERR_RANGE; }
         caps[k] = scenes[k].capacity;
         total += scenes[k].capacity;
     }
