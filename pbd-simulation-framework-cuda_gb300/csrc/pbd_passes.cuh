@@ -452,6 +452,103 @@ __device__ __forceinline__ uint32_t store_full_list(const DevParams& P, const Sc
     return n > F.kmax ? kListOff : (n | (n << 8));
 }
 
+// The cells of one group of particle i's list (the 3 cells of a findContacts column, or the cells
+// of a findNeighbours column: 2 sh + 1 on an edge column, 2 otherwise), stored into the full list:
+// all table loads in flight first, then the entries in list order, skipping self, with the cap M,
+// the list's room and the long-range hand-over of walk_seq.  Returns true when the walk ends here
+// (cap reached or handed over).
+template <int kMax>
+__device__ __forceinline__ bool store_cell_group(const DevParams& P, const SceneCtx& S, uint32_t i, const uint32_t* h,
+                                                 int ncell, const uint32_t* __restrict__ cs,
+                                                 const uint32_t* __restrict__ ce, const NbList& F, bool quirk,
+                                                 uint32_t& n, bool* deferred) {
+    const uint32_t N = P.N, M = P.M;
+    uint32_t s[kMax], e[kMax], len[kMax];
+#pragma unroll
+    for (int c = 0; c < kMax; ++c) s[c] = (c < ncell && h[c] < S.cells) ? __ldg(cs + S.base + h[c]) : kEmptyCell;
+#pragma unroll
+    for (int c = 0; c < kMax; ++c) e[c] = (c < ncell && h[c] < S.cells) ? __ldg(ce + S.base + h[c]) : 0u;
+    uint32_t reach = n;   // entries stored before the cell: the walk reaches it while below the cap
+#pragma unroll
+    for (int c = 0; c < kMax; ++c) {
+        const bool valid = c < ncell && s[c] < N;
+        const uint32_t ec = ((quirk && h[c] == S.n - 1) || e[c] > S.end) ? S.end : e[c];
+        len[c] = valid ? ec - s[c] : 0u;
+        if (valid && reach < M && len[c] > kLongRange) { *deferred = true; return true; }
+        reach += len[c] - ((valid && s[c] <= i && i < ec) ? 1u : 0u);
+    }
+    uint32_t* out = F.list + i;
+    if (reach < M && reach <= F.kmax) {   // the group fits below the cap and the list's room
+        uint32_t* o = out + (size_t)n * F.stride;
+#pragma unroll
+        for (int c = 0; c < kMax; ++c)
+#pragma unroll 1
+            for (uint32_t t = 0; t < len[c]; ++t) {
+                const uint32_t j = s[c] + t;
+                if (j == i) continue;
+                *o = j;
+                o += F.stride;
+            }
+        n = reach;
+        return false;
+    }
+#pragma unroll
+    for (int c = 0; c < kMax; ++c)
+#pragma unroll 1
+        for (uint32_t t = 0; t < len[c]; ++t) {
+            const uint32_t j = s[c] + t;
+            if (j == i) continue;
+            if (n < F.kmax) out[(size_t)n * F.stride] = j;
+            if (++n == M) return true;
+        }
+    return false;
+}
+
+// The frame's full list of particle i with findNeighbours' shells (kernelWidthNeighbours 2 or 3,
+// findContacts on): the 27 cells, then each shell, by cell groups (store_cell_group).  Returns the
+// list's meta (kListOff when it does not fit or the particle is handed over; *deferred tells which).
+__device__ __forceinline__ uint32_t store_full_list_shells(const DevParams& P, const SceneCtx& S, uint32_t i, float4 pa,
+                                                           const uint32_t* __restrict__ cs,
+                                                           const uint32_t* __restrict__ ce, const NbList& F,
+                                                           bool* deferred) {
+    const uint32_t M = P.M;
+    if (M == 0) return 0u;
+    const bool quirk = (P.flags & PBD_FLAG_CELL_END_QUIRK) && S.n >= 2;
+    const int K = (int)P.K;
+    uint32_t n = 0, nc = 0xFFFFFFFFu;
+    auto meta = [&]() -> uint32_t {
+        const uint32_t c = nc == 0xFFFFFFFFu ? n : nc;
+        return n > F.kmax ? kListOff : (n | (c << 8));
+    };
+    uint32_t h[7];
+    for (int a = -1; a <= 1; ++a) {
+        const uint32_t hx = morton_axis(__fmaf_rn((float)a, P.d, pa.x)) << 2;
+        for (int b = -1; b <= 1; ++b) {
+            const uint32_t hxy = hx + (morton_axis(__fmaf_rn((float)b, P.d, pa.y)) << 1);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) h[c] = hxy + morton_axis(__fmaf_rn((float)(c - 1), P.d, pa.z));
+            if (store_cell_group<3>(P, S, i, h, 3, cs, ce, F, quirk, n, deferred)) return *deferred ? kListOff : meta();
+        }
+    }
+    nc = n;
+    for (int sh = 2; sh <= K; ++sh)
+        for (int a = -sh; a <= sh; ++a) {
+            const uint32_t hx = morton_axis(__fmaf_rn((float)a, P.d, pa.x)) << 2;
+            for (int b = -sh; b <= sh; ++b) {
+                const uint32_t hxy = hx + (morton_axis(__fmaf_rn((float)b, P.d, pa.y)) << 1);
+                const bool edge = (a == sh || a == -sh || b == sh || b == -sh);
+                const int m = edge ? 2 * sh + 1 : 2;   // interior columns: only c = -sh and c = +sh
+#pragma unroll
+                for (int t = 0; t < 7; ++t) {
+                    const int c = edge ? t - sh : (t == 0 ? -sh : sh);
+                    h[t] = hxy + morton_axis(__fmaf_rn((float)c, P.d, pa.z));
+                }
+                if (store_cell_group<7>(P, S, i, h, m, cs, ce, F, quirk, n, deferred)) return *deferred ? kListOff : meta();
+            }
+        }
+    return meta();
+}
+
 // A visitor that sums nothing: a walk with Recorder<NullVisit> only stores the lists.
 struct NullVisit {
     struct Contrib {};
@@ -593,8 +690,11 @@ lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restric
         // the walk stores the full list (indices only), the filter the near list; the sums then
         // run over the shortest list that fits
         uint32_t fm;
-        if (P.K <= 1 && (P.active & PBD_ACTIVE_FIND_CONTACTS)) {
+        const bool shells = (P.active & PBD_ACTIVE_FIND_NEIGHBOURS) && P.K >= 2;
+        if (!shells && (P.active & PBD_ACTIVE_FIND_CONTACTS)) {
             fm = store_full_list(P, S, i, pa[i], cs, ce, F, &deferred);
+        } else if (shells && P.K <= 3 && (P.active & PBD_ACTIVE_FIND_CONTACTS)) {
+            fm = store_full_list_shells(P, S, i, pa[i], cs, ce, F, &deferred);
         } else {
             ListRecorder rec(F, i);
             walk_seq(P, S, i, pa[i], p, cs, ce, rec, true, &deferred);
