@@ -39,6 +39,7 @@ struct DevParams {
     float rho0;
     float hs, hp;          // spiky width (x diameter already applied), poly width
     float hp2;             // hp*hp
+    float hp_lim;          // hp - 0.001 (poly6's upper bound, Density.h:19)
     float k_scorr;
     float c_visc, e_vort;
     float stiffness, one_minus_stiffness;
@@ -116,7 +117,7 @@ __device__ __forceinline__ float dist2(float rx, float ry, float rz) {
 // ---------------------------------------------------------- pair kernels (Density.h) --
 // poly6Viscosity: W = 315 t^3 t^3 / den, t = hp^2 - d^2, for 0.001 < d < hp - 0.001.
 __device__ __forceinline__ float poly6(const DevParams& P, float dist) {
-    if (dist > 0.001f && dist < P.hp - 0.001f) {
+    if (dist > 0.001f && dist < P.hp_lim) {
         float t = __fsub_rn(P.hp2, __fmul_rn(dist, dist));
         float t3 = t * t * t;
         return (315.0f * t3 * t3) * P.poly_inv_den;
@@ -138,6 +139,7 @@ __device__ __forceinline__ float spiky_scale(const DevParams& P, float dist, flo
 // r *= x |n| times.  The usual exponents are spelled out with the same products in the same
 // order (1 * x = x exactly), without the loop.
 __device__ __forceinline__ float powi(float x, int n) {
+    if (n == 4) return ((x * x) * x) * x;   // config.txt's nSCorr: one test before the others
     switch (n) {
         case 0: return 1.0f;
         case 1: return x;

@@ -228,11 +228,12 @@ constexpr uint32_t kNearBatch = 1;   // near lists (~6 entries)
 template <bool kOwn = false, uint32_t B = kListBatch, class V>
 __device__ __forceinline__ void walk_list_part(const NbList& L, uint32_t i, uint32_t k0, uint32_t k1, bool contact,
                                                const float4* __restrict__ p, V& vis) {
-    const uint32_t* e = L.list + i;
+    const size_t st = L.stride;
+    const uint32_t* e = L.list + i + (size_t)k0 * st;   // entry k0; each batch moves it by B entries
     uint32_t jn[B];
 #pragma unroll
     for (uint32_t b = 0; b < B; ++b) {
-        const uint32_t* a = e + (size_t)(k0 + b) * L.stride;
+        const uint32_t* a = e + b * st;
         jn[b] = (k0 + b < k1) ? (kOwn ? *a : __ldcs(a)) : i;
     }
 #pragma unroll 1
@@ -247,9 +248,10 @@ __device__ __forceinline__ void walk_list_part(const NbList& L, uint32_t i, uint
             pj[b] = __ldg(p + j[b]);
             ex[b] = fetch_extra(vis, j[b]);
         }
+        e += B * st;
 #pragma unroll
         for (uint32_t b = 0; b < B; ++b) {
-            const uint32_t* a = e + (size_t)(kb + B + b) * L.stride;
+            const uint32_t* a = e + b * st;
             jn[b] = (kb + B + b < k1) ? (kOwn ? *a : __ldcs(a)) : i;
         }
 #pragma unroll

@@ -239,6 +239,7 @@ DevParams make_dev_params(const pbd_sim* s) {
     P.hs = P.d * p.kernel_width_spiky;                    // Initialize.h:45
     P.hp = p.kernel_width_poly;                           // Initialize.h:53
     P.hp2 = P.hp * P.hp;
+    P.hp_lim = P.hp - 0.001f;
     P.k_scorr = p.k_scorr;
     P.c_visc = p.c_viscosity;
     P.e_vort = p.e_vorticity;
