@@ -2,7 +2,7 @@
 
 Only tests/ and bench.py's checks import this module; the shipped library never does.  It
 restates, for the adjoint's supported configuration (applyForces, the density solve with
-stabilizationIterations = 1, solveCollisions, updatePositions; no vorticity or viscosity,
+stabilizationIterations = 1, solveCollisions, updatePositions, XSPH viscosity; no vorticity,
 enclosurePositionDamping = 0, unit cell width, the cell-end quirk off), the frame that
 Fluid::compute runs (src/app/simulation/Fluid.cu:14-97):
 
@@ -13,6 +13,7 @@ Fluid::compute runs (src/app/simulation/Fluid.cu:14-97):
   computeDelta    (kernel/Density.h:104-145), solveCollisions (kernel/Collision.h:171-242),
   applyDelta      p <- p + c - Delta, x <- x + c (Jacobi: all reads from the iteration's snapshot)
   updatePositions v = (p - x)/dt, x = p (kernel/Update.h:11-32)
+  viscosity       v <- v + c sum_j (v_j - v_i) W(|p_i - p_j|), Jacobi (kernel/Density.h:280-310)
 
 Particles stay in id order here (the re-order is a permutation: it changes summation order
 only).  `rollout` runs frames and can keep a tape; `backward` returns dL/dv0, dL/dx0,
@@ -50,6 +51,10 @@ class Consts:
         self.wq = self.poly6(np.array([q]))[0][0]
         c = max(self.hp, self.hs, d)
         self.cut2 = c * c * 1.0001
+        # XSPH viscosity (Density.h:280-310, Jacobi) after updatePositions, when active
+        self.cvisc = float(prm.c_viscosity) if (prm.active & (1 << 9)) else 0.0
+        if prm.active & (1 << 8):
+            raise ValueError("the restatement has no vorticity")
 
     def poly6(self, L):
         inside = (L > 0.001) & (L < self.hp - 0.001)
@@ -155,6 +160,12 @@ def frame(C, x, v, tape=None):
         p = p + c - delta
         x = x + c
     v = (p - x) / C.dt
+    if C.cvisc:   # v += c sum_j (v_j - v_i) W(|p_i - p_j|) over the frame's list, at the final positions
+        if tape is not None:
+            tape[-1]["pf"], tape[-1]["vu"] = p.copy(), v.copy()
+        I, J, r, L, rh = _pair_geometry(C, p, I0, J0)
+        W, _ = C.poly6(L)
+        v = v + C.cvisc * _sum(I, W[:, None] * (v[J] - v[I]), n)
     return p.copy(), v
 
 
@@ -172,9 +183,18 @@ def _hess_mul(g, dg, L, rh, a):
 def frame_backward(C, rec, gxo, gvo, acc):
     """Reverse of `frame` for the taped record `rec`: (dL/dx', dL/dv') -> (dL/dx, dL/dv)."""
     n = len(gxo)
+    I0, J0 = rec["I"], rec["J"]
+    if C.cvisc:   # reverse of the viscosity: dL/dv' -> dL/dv (before it) and dL/dp (final positions)
+        pf, vu = rec["pf"], rec["vu"]
+        I, J, r, L, rh = _pair_geometry(C, pf, I0, J0)
+        W, dW = C.poly6(L)
+        c = C.cvisc
+        gv_u = gvo * (1.0 - c * _sum(I, W, n))[:, None] + c * _sum(J, W[:, None] * gvo[I], n)
+        term = c * np.einsum("ij,ij->i", gvo[I], vu[J] - vu[I]) * dW
+        gxo = gxo + _sum(I, term[:, None] * rh, n) - _sum(J, term[:, None] * rh, n)
+        gvo = gv_u
     gp = gxo + gvo / C.dt
     gx = -gvo / C.dt
-    I0, J0 = rec["I"], rec["J"]
     for it in range(C.iters - 1, -1, -1):
         p = rec["p"][it]
         I, J, r, L, rh = _pair_geometry(C, p, I0, J0)

@@ -9,6 +9,7 @@
 //             c_i = sum_contacts 0.5 (1 - stiffness) (d - |r|) r_hat              (Collision.h:171-242)
 //             p <- p + c - Delta ;  x <- x + c
 //   update    v' = (p - x)/dt ; x' = p                                              (Update.h:11-32)
+//   viscosity v'' = v' + c sum_j (v'_j - v'_i) W(|p_i - p_j|), when active           (Density.h:280-310)
 // with r = p_i - p_j, G = spiky gradient g(|r|) r_hat, W = poly6.  The reverse passes scatter the
 // pair terms to the partner with atomic adds (so the neighbour relation need not be symmetric)
 // in 64-bit fixed point, which is associative, so the gradients do not depend on the order in
@@ -98,6 +99,88 @@ __device__ __forceinline__ void block_add2(double a, double b, unsigned long lon
         if (ta != 0.0) fix_add_scalar(acc, ta);
         if (tb != 0.0) fix_add_scalar(acc + 1, tb);
     }
+}
+
+__device__ __forceinline__ void scatter_add3(unsigned long long* sj, float3 v) {
+    fix_add(sj + 0, v.x);
+    fix_add(sj + 1, v.y);
+    fix_add(sj + 2, v.z);
+}
+
+// XSPH viscosity backward (Density.h:280-310, Jacobi), the frame's last pass:
+//   v'_i = v_i + c sum_j (v_j - v_i) W(|p_i - p_j|)   at the frame's final positions p
+// vbar_i = v'bar_i (1 - c sum_j W_ij) + sum over the lists holding i of c W v'bar (scattered);
+// pbar_i += sum_j c (v'bar_i . (v_j - v_i)) dW/dL rhat, pbar_j -= the same (scattered).
+struct AdjViscVisit {
+    struct Contrib { int dummy; };
+    using Extra = float4;   // v_j before the viscosity
+    const DevParams& P;
+    const float4* __restrict__ vu;
+    float4 pi, vi;
+    float3 gvo;        // dL/dv'_i
+    float c;
+    unsigned long long* scat_p;   // partners' dL/dp terms (fixed point)
+    unsigned long long* scat_v;   // partners' dL/dv terms (fixed point)
+    float sumw;
+    float3 gpi;
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ static Contrib zero() { return Contrib{0}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ float4 fetch(uint32_t j) const { return __ldg(vu + j); }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, const float4& vj, bool) {
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = dist2(rx, ry, rz);
+        if (r2 >= P.hp2 || r2 <= 0.0f) return zero();
+        const float L = sqrtf(r2);
+        float W, dW;
+        poly6_w(P, L, W, dW);
+        if (W == 0.0f && dW == 0.0f) return zero();
+        sumw += W;
+        const float cw = c * W;
+        scatter_add3(scat_v + 4 * (size_t)j, make_float3(cw * gvo.x, cw * gvo.y, cw * gvo.z));
+        const float term = c * (gvo.x * (vj.x - vi.x) + gvo.y * (vj.y - vi.y) + gvo.z * (vj.z - vi.z)) * dW / L;
+        const float3 t3 = make_float3(term * rx, term * ry, term * rz);
+        gpi.x += t3.x; gpi.y += t3.y; gpi.z += t3.z;
+        scatter_sub3(scat_p + 4 * (size_t)j, t3);
+        return zero();
+    }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
+};
+
+// gx_mod = dL/dx' + the viscosity's own dL/dp terms, gv_u = dL/dv before the viscosity (own
+// terms); the partners' terms go to scat_p / scat_v for adj_update_visc_kernel.
+__global__ void __launch_bounds__(128)
+adj_visc_kernel(DevParams P, const float4* __restrict__ pf, const float4* __restrict__ pa, const float4* __restrict__ vu,
+                const float4* __restrict__ gx_out, const float4* __restrict__ gv_out, float4* __restrict__ gx_mod,
+                float4* __restrict__ gv_u, unsigned long long* __restrict__ scat_p, unsigned long long* __restrict__ scat_v,
+                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const SceneCtx S = scene_ctx(P, i);
+    const float4 g = gv_out[i], gx = gx_out[i];
+    AdjViscVisit vis{P, vu, pf[i], vu[i], make_float3(g.x, g.y, g.z), P.c_visc, scat_p, scat_v, 0.f,
+                     make_float3(0.f, 0.f, 0.f)};
+    bool deferred = false;
+    walk_seq(P, S, i, pa[i], pf, cs, ce, vis, false, &deferred);
+    gx_mod[i] = make_float4(gx.x + vis.gpi.x, gx.y + vis.gpi.y, gx.z + vis.gpi.z, 0.f);
+    const float k = 1.0f - P.c_visc * vis.sumw;
+    gv_u[i] = make_float4(g.x * k, g.y * k, g.z * k, 0.f);
+}
+
+// update backward after the viscosity's: the partners' terms added to the own ones first
+__global__ void adj_update_visc_kernel(const DevParams P, float4* __restrict__ gx_mod, const float4* __restrict__ gv_u,
+                                       float4* __restrict__ gp, unsigned long long* __restrict__ scat_p,
+                                       unsigned long long* __restrict__ scat_v) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const float4 tp = take_scattered(scat_p, i), tv = take_scattered(scat_v, i);
+    const float4 a0 = gx_mod[i], b0 = gv_u[i];
+    const float4 a = make_float4(a0.x + tp.x, a0.y + tp.y, a0.z + tp.z, 0.f);
+    const float4 b = make_float4(b0.x + tv.x, b0.y + tv.y, b0.z + tv.z, 0.f);
+    const float r = P.inv_dt;
+    gp[i] = make_float4(a.x + b.x * r, a.y + b.y * r, a.z + b.z * r, 0.f);
+    gx_mod[i] = make_float4(-b.x * r, -b.y * r, -b.z * r, 0.f);   // becomes dL/dx
 }
 
 // update backward: pbar = xbar + vbar/dt, xbar = -vbar/dt   (sorted order of the frame)

@@ -88,6 +88,8 @@ struct Tape {
     float4* aux[kMaxTapeIters];    // the lambda pass's sums (2N float4: rho, B, S)
     uint32_t* near[kMaxTapeIters];       // each iteration's near lists (kListMax x N, slot-major)
     uint32_t* near_meta[kMaxTapeIters];  // and their counts
+    float4* p_fin;                 // with viscosity: the frame's final positions and the
+    float4* v_u;                   // velocities before the viscosity pass (sorted order)
 };
 
 struct pbd_sim {
@@ -587,6 +589,10 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         ++nl;
     }
     const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
+    if (tape && visc && tape->p_fin) {   // what the viscosity's reverse pass reads
+        cudaMemcpyAsync(tape->p_fin, s->x[cur.x], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(tape->v_u, s->v[cur.v], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
+    }
     bool v_read = false;   // the frame's final velocities are on their way to s->rb_host
     if (readback) {   // x (and v, unless viscosity follows) is final: copy it while the last passes run
         cudaEventRecord(s->rb_fork, st);
@@ -1544,7 +1550,7 @@ static int adjoint_supported(const pbd_sim* s) {
     const uint32_t need = PBD_ACTIVE_APPLY_FORCES | PBD_ACTIVE_FIND_CONTACTS | PBD_ACTIVE_COMPUTE_LAMBDA |
                           PBD_ACTIVE_COMPUTE_DELTA_POSITIONS | PBD_ACTIVE_APPLY_DELTA_POSITIONS | PBD_ACTIVE_UPDATE_POSITIONS;
     if ((p.active & need) != need) { set_error("adjoint: applyForces, findContacts, computeLambda, computeDeltaPositions, applyDeltaPositions and updatePositions must be active"); return PBD_ERR_UNSUPPORTED; }
-    if (p.active & (PBD_ACTIVE_COMPUTE_VORTICITY | PBD_ACTIVE_COMPUTE_VISCOSITY)) { set_error("adjoint: vorticity and viscosity have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
+    if (p.active & PBD_ACTIVE_COMPUTE_VORTICITY) { set_error("adjoint: vorticity has no reverse pass"); return PBD_ERR_UNSUPPORTED; }
     if (p.stabilization_iterations != 1 || p.solver_iterations == 0 || p.solver_iterations > (uint32_t)kMaxTapeIters) { set_error("adjoint: stabilizationIterations must be 1 and solverIterations 1..16"); return PBD_ERR_UNSUPPORTED; }
     if (p.enclosure_position_damping != 0.0f) { set_error("adjoint: enclosurePositionDamping must be 0"); return PBD_ERR_UNSUPPORTED; }
     if (s->mass_used || s->batched) { set_error("adjoint: solids and batches have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
@@ -1567,7 +1573,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     const int nck = (nsteps + k - 1) / k;
     const uint32_t I = s->prm.solver_iterations;
     // workspace: checkpoints, the final state, k frames of tape, gradient buffers
-    const size_t per_tape = N * (16 + 16 + 4 + 4) + (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4);
+    const bool visc = (s->prm.active & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
+    const size_t per_tape = N * (16 + 16 + 4 + 4 + (visc ? 32 : 0)) + (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 512;
     const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + 64 +
                         N * 64 + (size_t)(18 + (4 + 5 * I) * k) * 256;
     if (need > s->adj_bytes) {
@@ -1602,6 +1609,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
             T.near[it] = (uint32_t*)take(N * 4 * kListMax);
             T.near_meta[it] = (uint32_t*)take(N * 4);
         }
+        T.p_fin = visc ? (float4*)take(N * 16) : nullptr;
+        T.v_u = visc ? (float4*)take(N * 16) : nullptr;
     }
     for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
     s->adj_glam = (float*)take(N * 4);
@@ -1674,7 +1683,13 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
         if (T.keys != held) { retable(s, st, held, T.keys, N); held = T.keys; }
         // adj_update writes all of gp: each frame starts from the same pair of buffers
         float4 *gp = s->adj_g[3], *gp2 = s->adj_g[4];
-        adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
+        if (T.p_fin) {   // the viscosity's reverse first (the frame's last pass), into gx and gp2
+            adj_visc_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, gx_out, gv_out, gx, gp2, s->adj_scat,
+                                                s->adj_scat2, s->cell_start, s->cell_end);
+            adj_update_visc_kernel<<<ge, 256, 0, st>>>(P, gx, gp2, gp, s->adj_scat, s->adj_scat2);
+        } else {
+            adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
+        }
         for (int it = (int)I - 1; it >= 0; --it) {
             const float4* p = T.p_it[it];
             const float4* pa = T.p_it[0];

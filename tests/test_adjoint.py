@@ -1,7 +1,7 @@
 """Adjoint of the frame: dL/dv0, dL/dx0, dL/drest_density and dL/deps of L = sum(c . x_final).
 
 CPU: the FP64 restatement (oracle/adjoint.py) is pinned to the C oracle's FP64 trajectory and
-its reverse pass to central differences of its own forward.
+its reverse pass to central differences of its own forward, with and without XSPH viscosity.
 GPU: pbd_adjoint_forward/backward through the C ABI against that FP64 reverse pass on the same
 seeded scene, with several checkpoint spacings, and the state the forward left restored.
 Tolerance of the GPU gradients against the FP64 reverse pass (FP32 forward and reverse): 2% of
@@ -17,8 +17,9 @@ from helpers import maxdiff
 FRAMES = 8
 
 
-def adjoint_scene(pbd, scenes, shape=(7, 7, 7), box=14, spacing=0.75, iterations=3, seed=5, vel_sigma=1.0):
-    prm = scenes.workload_params(pbd, box, 1000.0, iterations=iterations)
+def adjoint_scene(pbd, scenes, shape=(7, 7, 7), box=14, spacing=0.75, iterations=3, seed=5, vel_sigma=1.0,
+                  viscosity=0.0):
+    prm = scenes.workload_params(pbd, box, 1000.0, iterations=iterations, viscosity=viscosity)
     prm.lambda_epsilon = 0.1
     prm.flags &= ~pbd.FLAG_CELL_END_QUIRK
     prm.flags |= pbd.FLAG_TRACK_IDS
@@ -35,8 +36,9 @@ def adj():
     return m
 
 
-def test_restatement_follows_oracle(pbd, scenes, oracle_mod, adj):
-    prm, pos, vel, _ = adjoint_scene(pbd, scenes)
+@pytest.mark.parametrize("viscosity", [0.0, 0.01])
+def test_restatement_follows_oracle(pbd, scenes, oracle_mod, adj, viscosity):
+    prm, pos, vel, _ = adjoint_scene(pbd, scenes, viscosity=viscosity)
     C = adj.Consts(prm)
     o = oracle_mod.Oracle(prm, len(pos), "f64")
     o.add_particles(pos, vel)
@@ -55,8 +57,9 @@ def _loss(adj, C, x0, v0, w):
     return float(np.sum(w * x))
 
 
-def test_reverse_pass_matches_central_differences(pbd, scenes, adj):
-    prm, pos, vel, w = adjoint_scene(pbd, scenes)
+@pytest.mark.parametrize("viscosity", [0.0, 0.01])
+def test_reverse_pass_matches_central_differences(pbd, scenes, adj, viscosity):
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, viscosity=viscosity)
     C = adj.Consts(prm)
     x0, v0 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
     gv, gx, gr, ge = adj.backward(C, x0, v0, FRAMES, w)
@@ -110,9 +113,9 @@ def _close_l2(a, b, rel=0.02):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("every", [FRAMES, 3, 1])
-def test_gpu_adjoint_matches_fp64(need_gpu, pbd, scenes, adj, every):
-    prm, pos, vel, w = adjoint_scene(pbd, scenes)
+@pytest.mark.parametrize("every,viscosity", [(FRAMES, 0.0), (3, 0.0), (1, 0.0), (3, 0.01)])
+def test_gpu_adjoint_matches_fp64(need_gpu, pbd, scenes, adj, every, viscosity):
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, viscosity=viscosity)
     C = adj.Consts(prm)
     rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), FRAMES, w)
     sim, fin, after, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, FRAMES, every)
@@ -124,10 +127,11 @@ def test_gpu_adjoint_matches_fp64(need_gpu, pbd, scenes, adj, every):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("iterations", [1, 4])
-def test_gpu_adjoint_one_frame_exact(need_gpu, pbd, scenes, adj, iterations):
+@pytest.mark.parametrize("iterations,viscosity", [(1, 0.0), (4, 0.0), (4, 0.01)])
+def test_gpu_adjoint_one_frame_exact(need_gpu, pbd, scenes, adj, iterations, viscosity):
     """one frame: the FP32 reverse pass equals the FP64 one up to FP32 rounding"""
-    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(12, 10, 12), box=20, iterations=iterations, seed=7)
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(12, 10, 12), box=20, iterations=iterations, seed=7,
+                                     viscosity=viscosity)
     C = adj.Consts(prm)
     rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), 1, w)
     _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, 1, 1)
