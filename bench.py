@@ -1,7 +1,7 @@
 """Benchmark of the GB300 PBD step: particle-steps/s on the 1M-particle fluid workloads.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
-                    [--leg contacts|batched|batched_frames|solids|adjoint|dense|render]
+                    [--leg headline|contacts|batched|batched_frames|solids|adjoint|dense|render]
 
 Our arm (default): the headline workload fluid_1m -- 100^3 = 1,000,000 fluid particles in a
 128^3-cell domain (seed 2), kernel radius 1, 4 solver iterations, vorticity 5e-4, XSPH 0.01,
@@ -842,6 +842,8 @@ def run_leg(args):
         out = run_batched(torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 60)))
     elif args.leg == "solids":
         out = run_solids(torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 100)))
+    elif args.leg == "headline":
+        out = measure_workload(torch, pbd, scenes, args.workload, args, stream, sh, 1, torch.device("cuda", 0), 0)
     elif args.leg == "dense":
         out = measure_workload(torch, pbd, scenes, DENSE, args, stream, sh, 1, torch.device("cuda", 0), 0,
                                staged_compare=True)
@@ -878,7 +880,8 @@ def main():
     ap.add_argument("--workload", default="fluid_1m")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-fd-check", action="store_true", help="skip the FP64 finite-difference check of the adjoint")
-    ap.add_argument("--leg", choices=["contacts", "batched", "batched_frames", "solids", "adjoint", "dense", "render"],
+    ap.add_argument("--leg", choices=["headline", "contacts", "batched", "batched_frames", "solids", "adjoint", "dense",
+                                      "render"],
                     help="measure only this secondary workload and print its result (not the bench line)")
     args = ap.parse_args()
     if args.warmup < 3:
