@@ -528,6 +528,9 @@ def run_adjoint(torch, pbd, scenes, stream, sh, frames=60, every=10, fd_check=Tr
         out["gradient_check"] = checks
         met = [h for h in (frames, *short) if all(checks[f"{h}_frames"]["within_1e-3"].values())]
         out["largest_horizon_within_1e-3"] = max(met) if met else 0
+        out["largest_horizon_within_1e-3_by_gradient"] = {
+            name: max([h for h in (frames, *short) if checks[f"{h}_frames"]["within_1e-3"][name]] or [0])
+            for name in ("rest_density", "eps", "v0_direction")}
         out["gradient_check_s"] = time.perf_counter() - t0
     return out
 

@@ -13,9 +13,11 @@
 // with r = p_i - p_j, G = spiky gradient g(|r|) r_hat, W = poly6.  The reverse passes scatter the
 // pair terms to the partner with atomic adds (so the neighbour relation need not be symmetric)
 // in 64-bit fixed point, which is associative, so the gradients do not depend on the order in
-// which the atomics land: a reverse pass gives the same bits every time.  A particle's own terms
-// are summed in its list's order; dL/drest_density and dL/deps are summed per block in double
-// and across blocks in fixed point.
+// which the atomics land: a reverse pass gives the same bits every time.  The fixed point's scale
+// is set per frame from the largest gradient entering the frame's reverse pass.  A particle's own
+// terms are summed in its list's order; dL/drest_density and dL/deps are summed per block in
+// double into the block's own slot (one block per slot per launch, launches in stream order) and
+// the slots are added in index order at the end.
 #pragma once
 #include "pbd_passes.cuh"
 
@@ -55,36 +57,41 @@ __device__ __forceinline__ float3 spiky_hess_mul(float g, float dg, float L, flo
                        dg * rv * rh.z + gl * (v.z - rv * rh.z));
 }
 
-// Fixed point of the scattered terms: 2^32, which holds every float in (2^-33, 2^31) exactly
-// (the scaling is a power of two and the conversion saturates); of the two scalar gradients:
-// 2^36 (resolution 1.5e-11, range +-1.3e8).  A pass's scattered terms are taken up (and the
-// slots cleared) by the next kernel, which reads its own particle's slot first.
-constexpr float kFixScatter = 4294967296.0f;
-constexpr float kUnfixScatter = 2.3283064365386963e-10f;   // 2^-32
-constexpr double kFixScalar = 68719476736.0;
-__device__ __forceinline__ void fix_add(unsigned long long* a, float v) {
-    atomicAdd(a, (unsigned long long)__float2ll_rn(v * kFixScatter));
+// Fixed point of the scattered terms, scaled per frame: the frame's reverse pass starts with
+// adj_gmax_kernel, which takes the largest |dL/dx'| + |dL/dv'|/dt over the particles (m < 2^e);
+// every scatter and take of that frame then uses the scale 2^(40 - e).  A term of magnitude a
+// keeps a - 2^(e-41) of its value (relative 2^-41 of the frame's largest gradient), and the
+// sums stay below 2^62 while no particle's scattered terms exceed 2^22 times that gradient.
+// A fixed scale cannot serve both a loss averaged over a million particles (terms ~1e-7) and
+// a summed one that has grown over many frames.
+struct FixScale { float sc, inv; };
+__device__ __forceinline__ FixScale fix_scale(const uint32_t* __restrict__ gmax) {
+    const uint32_t be = (*gmax >> 23) & 0xFFu;                 // biased exponent of the largest gradient
+    int s = (be == 0xFFu) ? 0 : 40 - ((int)be - 126);           // m < 2^(be - 126); inf/NaN: scale 1
+    s = max(-120, min(120, s));
+    return FixScale{__int_as_float((s + 127) << 23), __int_as_float((127 - s) << 23)};
 }
-__device__ __forceinline__ void fix_add_scalar(unsigned long long* a, double v) {
-    const double q = fmin(fmax(v * kFixScalar, -9.0e18), 9.0e18);
-    atomicAdd(a, (unsigned long long)__double2ll_rn(q));
+__device__ __forceinline__ void fix_add(unsigned long long* a, float v, float sc) {
+    atomicAdd(a, (unsigned long long)__float2ll_rn(v * sc));
 }
-__device__ __forceinline__ void scatter_sub3(unsigned long long* sj, float3 v) {
-    fix_add(sj + 0, -v.x);
-    fix_add(sj + 1, -v.y);
-    fix_add(sj + 2, -v.z);
+__device__ __forceinline__ void scatter_sub3(unsigned long long* sj, float3 v, float sc) {
+    fix_add(sj + 0, -v.x, sc);
+    fix_add(sj + 1, -v.y, sc);
+    fix_add(sj + 2, -v.z, sc);
 }
 // Particle i's scattered terms as floats; the slot is cleared for the next pass.
-__device__ __forceinline__ float4 take_scattered(unsigned long long* scat, uint32_t i) {
+__device__ __forceinline__ float4 take_scattered(unsigned long long* scat, uint32_t i, float inv) {
     unsigned long long* s = scat + 4 * (size_t)i;
-    const float4 r = make_float4(__ll2float_rn((long long)s[0]) * kUnfixScatter, __ll2float_rn((long long)s[1]) * kUnfixScatter,
-                                 __ll2float_rn((long long)s[2]) * kUnfixScatter, __ll2float_rn((long long)s[3]) * kUnfixScatter);
+    const float4 r = make_float4(__ll2float_rn((long long)s[0]) * inv, __ll2float_rn((long long)s[1]) * inv,
+                                 __ll2float_rn((long long)s[2]) * inv, __ll2float_rn((long long)s[3]) * inv);
     s[0] = s[1] = s[2] = s[3] = 0ull;
     return r;
 }
 
-// Block-reduce two doubles (in a fixed order) and add them to the fixed-point accumulators.
-__device__ __forceinline__ void block_add2(double a, double b, unsigned long long* acc) {
+// Block-reduce two doubles (in a fixed order) and add them to this block's slots acc[2b], acc[2b+1]:
+// a launch has one block per slot and the launches run in stream order, so no atomics are needed
+// and the sums do not depend on scheduling.
+__device__ __forceinline__ void block_add2(double a, double b, double* acc) {
     __shared__ double sa[32], sb[32];
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_down_sync(0xffffffffu, a, o);
@@ -96,15 +103,30 @@ __device__ __forceinline__ void block_add2(double a, double b, unsigned long lon
     if (threadIdx.x == 0) {
         double ta = 0.0, tb = 0.0;
         for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) { ta += sa[w]; tb += sb[w]; }
-        if (ta != 0.0) fix_add_scalar(acc, ta);
-        if (tb != 0.0) fix_add_scalar(acc + 1, tb);
+        acc[2 * (size_t)blockIdx.x] += ta;
+        acc[2 * (size_t)blockIdx.x + 1] += tb;
     }
 }
 
-__device__ __forceinline__ void scatter_add3(unsigned long long* sj, float3 v) {
-    fix_add(sj + 0, v.x);
-    fix_add(sj + 1, v.y);
-    fix_add(sj + 2, v.z);
+__device__ __forceinline__ void scatter_add3(unsigned long long* sj, float3 v, float sc) {
+    fix_add(sj + 0, v.x, sc);
+    fix_add(sj + 1, v.y, sc);
+    fix_add(sj + 2, v.z, sc);
+}
+
+// The largest |dL/dx'| + |dL/dv'|/dt entering a frame's reverse pass (non-negative floats order
+// as their bit patterns), for fix_scale.  *gmax is zeroed before the launch.
+__global__ void adj_gmax_kernel(const DevParams P, const float4* __restrict__ gx_out, const float4* __restrict__ gv_out,
+                                uint32_t* __restrict__ gmax) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float m = 0.0f;
+    if (i < P.N) {
+        const float4 a = gx_out[i], b = gv_out[i];
+        const float r = P.inv_dt;
+        m = fmaxf(fmaxf(fabsf(a.x) + fabsf(b.x) * r, fabsf(a.y) + fabsf(b.y) * r), fabsf(a.z) + fabsf(b.z) * r);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(gmax, __float_as_uint(m));
 }
 
 // XSPH viscosity backward (Density.h:280-310, Jacobi), the frame's last pass:
@@ -121,6 +143,7 @@ struct AdjViscVisit {
     float c;
     unsigned long long* scat_p;   // partners' dL/dp terms (fixed point)
     unsigned long long* scat_v;   // partners' dL/dv terms (fixed point)
+    float fix;                    // the frame's fixed-point scale
     float sumw;
     float3 gpi;
     __device__ __forceinline__ void end_contacts(uint32_t) {}
@@ -138,11 +161,11 @@ struct AdjViscVisit {
         if (W == 0.0f && dW == 0.0f) return zero();
         sumw += W;
         const float cw = c * W;
-        scatter_add3(scat_v + 4 * (size_t)j, make_float3(cw * gvo.x, cw * gvo.y, cw * gvo.z));
+        scatter_add3(scat_v + 4 * (size_t)j, make_float3(cw * gvo.x, cw * gvo.y, cw * gvo.z), fix);
         const float term = c * (gvo.x * (vj.x - vi.x) + gvo.y * (vj.y - vi.y) + gvo.z * (vj.z - vi.z)) * dW / L;
         const float3 t3 = make_float3(term * rx, term * ry, term * rz);
         gpi.x += t3.x; gpi.y += t3.y; gpi.z += t3.z;
-        scatter_sub3(scat_p + 4 * (size_t)j, t3);
+        scatter_sub3(scat_p + 4 * (size_t)j, t3, fix);
         return zero();
     }
     __device__ __forceinline__ void add(const Contrib&, bool) {}
@@ -154,12 +177,12 @@ __global__ void __launch_bounds__(128)
 adj_visc_kernel(DevParams P, const float4* __restrict__ pf, const float4* __restrict__ pa, const float4* __restrict__ vu,
                 const float4* __restrict__ gx_out, const float4* __restrict__ gv_out, float4* __restrict__ gx_mod,
                 float4* __restrict__ gv_u, unsigned long long* __restrict__ scat_p, unsigned long long* __restrict__ scat_v,
-                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce) {
+                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
     const float4 g = gv_out[i], gx = gx_out[i];
-    AdjViscVisit vis{P, vu, pf[i], vu[i], make_float3(g.x, g.y, g.z), P.c_visc, scat_p, scat_v, 0.f,
+    AdjViscVisit vis{P, vu, pf[i], vu[i], make_float3(g.x, g.y, g.z), P.c_visc, scat_p, scat_v, fix_scale(gmax).sc, 0.f,
                      make_float3(0.f, 0.f, 0.f)};
     bool deferred = false;
     walk_seq(P, S, i, pa[i], pf, cs, ce, vis, false, &deferred);
@@ -171,10 +194,11 @@ adj_visc_kernel(DevParams P, const float4* __restrict__ pf, const float4* __rest
 // update backward after the viscosity's: the partners' terms added to the own ones first
 __global__ void adj_update_visc_kernel(const DevParams P, float4* __restrict__ gx_mod, const float4* __restrict__ gv_u,
                                        float4* __restrict__ gp, unsigned long long* __restrict__ scat_p,
-                                       unsigned long long* __restrict__ scat_v) {
+                                       unsigned long long* __restrict__ scat_v, const uint32_t* __restrict__ gmax) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
-    const float4 tp = take_scattered(scat_p, i), tv = take_scattered(scat_v, i);
+    const float inv = fix_scale(gmax).inv;
+    const float4 tp = take_scattered(scat_p, i, inv), tv = take_scattered(scat_v, i, inv);
     const float4 a0 = gx_mod[i], b0 = gv_u[i];
     const float4 a = make_float4(a0.x + tp.x, a0.y + tp.y, a0.z + tp.z, 0.f);
     const float4 b = make_float4(b0.x + tv.x, b0.y + tv.y, b0.z + tv.z, 0.f);
@@ -205,6 +229,7 @@ struct AdjDeltaVisit {
     float3 a;          // Delta-bar / rho0
     float3 cbar;       // dL/dc_i = gp_in + gx
     unsigned long long* scat;   // per particle: x, y, z of dL/dp, dL/dlambda (fixed point)
+    float fix;         // the frame's fixed-point scale
     float3 gpi;        // this particle's own accumulated term
     float3 sdelta;     // sum coef * G (for the rho0 term)
     float glami;
@@ -233,7 +258,7 @@ struct AdjDeltaVisit {
             const float3 G = make_float3(g * rh.x, g * rh.y, g * rh.z);
             const float gd = G.x * a.x + G.y * a.y + G.z * a.z;
             glami += gd;
-            fix_add(scat + 4 * (size_t)j + 3, gd);
+            fix_add(scat + 4 * (size_t)j + 3, gd, fix);
             const float3 Ha = spiky_hess_mul(g, dg, L, rh, a);
             rbar.x += coef * Ha.x + gd * dsc * rh.x;
             rbar.y += coef * Ha.y + gd * dsc * rh.y;
@@ -253,7 +278,7 @@ struct AdjDeltaVisit {
             }
         }
         gpi.x += rbar.x; gpi.y += rbar.y; gpi.z += rbar.z;
-        scatter_sub3(scat + 4 * (size_t)j, rbar);
+        scatter_sub3(scat + 4 * (size_t)j, rbar, fix);
         return zero();
     }
     __device__ __forceinline__ void add(const Contrib&, bool) {}
@@ -263,18 +288,19 @@ __global__ void __launch_bounds__(128)
 adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float* __restrict__ lambda,
                  const float4* __restrict__ gp_in, const float4* __restrict__ gx, float4* __restrict__ gp_out,
                  float* __restrict__ glam, unsigned long long* __restrict__ scat, unsigned long long* __restrict__ scat_in,
-                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, unsigned long long* acc, bool collide,
-                 NbList Lt) {
+                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, double* acc, bool collide,
+                 NbList Lt, const uint32_t* __restrict__ gmax) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double drho = 0.0;
     if (i < P.N) {
         const SceneCtx S = scene_ctx(P, i);
-        const float4 g0 = gp_in[i], t = take_scattered(scat_in, i), gxi = gx[i];   // + the pass after's partners
+        const FixScale fs = fix_scale(gmax);
+        const float4 g0 = gp_in[i], t = take_scattered(scat_in, i, fs.inv), gxi = gx[i];   // + the pass after's partners
         const float4 gpin = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
         const float inv = 1.0f / S.rho0;
         AdjDeltaVisit vis{P, lambda, p[i], lambda[i],
                           make_float3(-gpin.x * inv, -gpin.y * inv, -gpin.z * inv),
-                          make_float3(gpin.x + gxi.x, gpin.y + gxi.y, gpin.z + gxi.z), scat,
+                          make_float3(gpin.x + gxi.x, gpin.y + gxi.y, gpin.z + gxi.z), scat, fs.sc,
                           make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), 0.f, collide};
         // the forward's near list of this iteration (the pairs within the cut), else the cells
         const uint32_t meta = Lt.list ? Lt.meta[i] : kListOff;
@@ -301,6 +327,7 @@ struct AdjLambdaBwd {
     float dbar2;       // 2 Dbar / rho0
     float3 Sg;
     unsigned long long* scat;
+    float fix;         // the frame's fixed-point scale
     float3 gpi;
     __device__ __forceinline__ void end_contacts(uint32_t) {}
     __device__ static Contrib zero() { return Contrib{0}; }
@@ -322,7 +349,7 @@ struct AdjLambdaBwd {
             rbar.x += dbar2 * Hv.x; rbar.y += dbar2 * Hv.y; rbar.z += dbar2 * Hv.z;
         }
         gpi.x += rbar.x; gpi.y += rbar.y; gpi.z += rbar.z;
-        scatter_sub3(scat + 4 * (size_t)j, rbar);
+        scatter_sub3(scat + 4 * (size_t)j, rbar, fix);
         return zero();
     }
     __device__ __forceinline__ void add(const Contrib&, bool) {}
@@ -332,12 +359,13 @@ __global__ void __launch_bounds__(128)
 adj_lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ aux,
                   const float* __restrict__ glam, float4* __restrict__ gp_out, unsigned long long* __restrict__ scat,
                   unsigned long long* __restrict__ scat_in, const uint32_t* __restrict__ cs,
-                  const uint32_t* __restrict__ ce, unsigned long long* acc, NbList Lt) {
+                  const uint32_t* __restrict__ ce, double* acc, NbList Lt, const uint32_t* __restrict__ gmax) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double drho = 0.0, deps = 0.0;
     if (i < P.N) {
         const SceneCtx S = scene_ctx(P, i);
-        const float4 t = take_scattered(scat_in, i);   // the delta pass's partners' terms
+        const FixScale fs = fix_scale(gmax);
+        const float4 t = take_scattered(scat_in, i, fs.inv);   // the delta pass's partners' terms
         const float4 g0 = gp_out[i];
         const float4 g = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
         const float lb = glam[i] + t.w;
@@ -352,7 +380,7 @@ adj_lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __res
         drho = (double)Cbar * (-(double)s0.x / r02) + (double)Dbar * (-(double)BS / r02);
         deps = (double)Dbar;
         if (lb != 0.0f) {
-            AdjLambdaBwd b{P, p[i], Cbar / rho0, 2.0f * Dbar / rho0, make_float3(s0.z, s0.w, s1.x), scat,
+            AdjLambdaBwd b{P, p[i], Cbar / rho0, 2.0f * Dbar / rho0, make_float3(s0.z, s0.w, s1.x), scat, fs.sc,
                            make_float3(0.f, 0.f, 0.f)};
             const uint32_t meta = Lt.list ? Lt.meta[i] : kListOff;
             bool deferred = false;
@@ -372,7 +400,7 @@ __global__ void adj_predict_kernel(DevParams P, const uint32_t* __restrict__ per
                                    const float4* __restrict__ v_in, const float4* __restrict__ fext,
                                    const float4* __restrict__ gp, const float4* __restrict__ gxp,
                                    float4* __restrict__ gx_out, float4* __restrict__ gv_out,
-                                   unsigned long long* __restrict__ scat_in) {
+                                   unsigned long long* __restrict__ scat_in, const uint32_t* __restrict__ gmax) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const uint32_t o = perm[i];
@@ -387,7 +415,7 @@ __global__ void adj_predict_kernel(DevParams P, const uint32_t* __restrict__ per
     const float mx = (px < P.bmin[0] || px > P.bmax[0]) ? 0.f : 1.f;
     const float my = (py < P.bmin[1] || py > P.bmax[1]) ? 0.f : 1.f;
     const float mz = (pz < P.bmin[2] || pz > P.bmax[2]) ? 0.f : 1.f;
-    const float4 g0 = gp[i], t = take_scattered(scat_in, i), gx = gxp[i];   // + the last lambda pass's partners
+    const float4 g0 = gp[i], t = take_scattered(scat_in, i, fix_scale(gmax).inv), gx = gxp[i];   // + the last lambda pass's partners
     const float4 g = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
     gx_out[o] = make_float4(gx.x + mx * g.x, gx.y + my * g.y, gx.z + mz * g.z, 0.f);
     gv_out[o] = make_float4(mx * g.x * dt, my * g.y * dt, mz * g.z * dt, 0.f);

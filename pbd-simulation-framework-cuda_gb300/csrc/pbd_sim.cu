@@ -136,7 +136,8 @@ struct pbd_sim {
     std::vector<AdjGraph> adj_graphs;   // recorded segments of the adjoint
     uint64_t adj_graphs_pgen = ~0ull;
     void* adj_graphs_arena = nullptr;
-    unsigned long long* adj_acc = nullptr;   // dL/drest_density, dL/deps in fixed point
+    double* adj_acc = nullptr;               // per reverse block: dL/drest_density, dL/deps
+    uint32_t* adj_gmax = nullptr;            // the frame's largest entering gradient (fixed-point scale)
     unsigned long long* adj_scat = nullptr;  // partners' terms of a delta reverse pass, fixed point (4 per particle)
     unsigned long long* adj_scat2 = nullptr; // the same for the lambda reverse passes
     std::vector<uint32_t> scene_cap, scene_count;
@@ -1575,8 +1576,9 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     // workspace: checkpoints, the final state, k frames of tape, gradient buffers
     const bool visc = (s->prm.active & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     const size_t per_tape = N * (16 + 16 + 4 + 4 + (visc ? 32 : 0)) + (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 512;
-    const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + 64 +
-                        N * 64 + (size_t)(18 + (4 + 5 * I) * k) * 256;
+    const size_t acc_bytes = 16 * (size_t)div_up((uint32_t)N, 128);   // two doubles per reverse block
+    const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + acc_bytes +
+                        N * 64 + (size_t)(19 + (4 + 5 * I) * k) * 256;
     if (need > s->adj_bytes) {
         if (s->adj_arena) CK(cudaStreamSynchronize(st));
         if (s->adj_arena) cudaFree(s->adj_arena);
@@ -1614,7 +1616,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     }
     for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
     s->adj_glam = (float*)take(N * 4);
-    s->adj_acc = (unsigned long long*)take(64);
+    s->adj_acc = (double*)take(acc_bytes);
+    s->adj_gmax = (uint32_t*)take(4);
     s->adj_scat = (unsigned long long*)take((size_t)N * 32);
     s->adj_scat2 = (unsigned long long*)take((size_t)N * 32);
     s->adj_steps = nsteps;
@@ -1683,10 +1686,13 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
         if (T.keys != held) { retable(s, st, held, T.keys, N); held = T.keys; }
         // adj_update writes all of gp: each frame starts from the same pair of buffers
         float4 *gp = s->adj_g[3], *gp2 = s->adj_g[4];
+        // the frame's fixed-point scale, from the gradient entering it
+        cudaMemsetAsync(s->adj_gmax, 0, 4, st);
+        adj_gmax_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, s->adj_gmax);
         if (T.p_fin) {   // the viscosity's reverse first (the frame's last pass), into gx and gp2
             adj_visc_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, gx_out, gv_out, gx, gp2, s->adj_scat,
-                                                s->adj_scat2, s->cell_start, s->cell_end);
-            adj_update_visc_kernel<<<ge, 256, 0, st>>>(P, gx, gp2, gp, s->adj_scat, s->adj_scat2);
+                                                s->adj_scat2, s->cell_start, s->cell_end, s->adj_gmax);
+            adj_update_visc_kernel<<<ge, 256, 0, st>>>(P, gx, gp2, gp, s->adj_scat, s->adj_scat2, s->adj_gmax);
         } else {
             adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
         }
@@ -1698,12 +1704,14 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
             // the next kernel adds a particle's scattered terms in one place: the same bits
             // whatever order the atomics landed in
             adj_delta_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.lam[it], gp, gx, gp2, s->adj_glam, s->adj_scat,
-                                                 s->adj_scat2, s->cell_start, s->cell_end, s->adj_acc, collide, Lt);
+                                                 s->adj_scat2, s->cell_start, s->cell_end, s->adj_acc, collide, Lt,
+                                                 s->adj_gmax);
             adj_lambda_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.aux[it], s->adj_glam, gp2, s->adj_scat2, s->adj_scat,
-                                                  s->cell_start, s->cell_end, s->adj_acc, Lt);
+                                                  s->cell_start, s->cell_end, s->adj_acc, Lt, s->adj_gmax);
             std::swap(gp, gp2);
         }
-        adj_predict_kernel<<<ge, 256, 0, st>>>(P, T.perm, T.x_in, T.v_in, s->fext, gp, gx, gx_out, gv_out, s->adj_scat2);
+        adj_predict_kernel<<<ge, 256, 0, st>>>(P, T.perm, T.x_in, T.v_in, s->fext, gp, gx, gx_out, gv_out, s->adj_scat2,
+                                               s->adj_gmax);
     }
     // back to the tables the next recompute's predict expects: the cells of keys[fin]
     retable(s, st, held, s->keys[fin], N);
@@ -1768,7 +1776,8 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
     float4 *gx_out = s->adj_g[0], *gv_out = s->adj_g[1];
     CK(cudaMemcpyAsync(gx_out, dL_dx_final, (size_t)N * 16, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(gv_out, 0, (size_t)N * 16, st));
-    CK(cudaMemsetAsync(s->adj_acc, 0, 64, st));
+    const uint32_t nblk = div_up(N, 128);   // the reverse kernels' blocks: two accumulators each
+    CK(cudaMemsetAsync(s->adj_acc, 0, (size_t)nblk * 16, st));
     CK(cudaMemsetAsync(s->adj_scat, 0, (size_t)N * 32, st));
     CK(cudaMemsetAsync(s->adj_scat2, 0, (size_t)N * 32, st));
     for (int ck = s->adj_nck - 1; ck >= 0; --ck) {
@@ -1791,13 +1800,15 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
     CK(cudaMemcpyAsync(s->ids[s->cur.x], s->adj_fin_ids, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
     s->adj_last_taped = s->adj_nck == 1;       // else the tape now holds the first segment
     s->anchor = -1;
-    unsigned long long acc_fix[2] = {0ull, 0ull};
-    CK(cudaMemcpyAsync(acc_fix, s->adj_acc, 16, cudaMemcpyDeviceToHost, st));
+    std::vector<double> acc((size_t)nblk * 2);
+    CK(cudaMemcpyAsync(acc.data(), s->adj_acc, (size_t)nblk * 16, cudaMemcpyDeviceToHost, st));
     if (dL_dv0) CK(cudaMemcpyAsync(dL_dv0, gv_out, (size_t)N * 16, cudaMemcpyDeviceToHost, st));
     if (dL_dx0) CK(cudaMemcpyAsync(dL_dx0, gx_out, (size_t)N * 16, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (dL_drho0) *dL_drho0 = (double)(long long)acc_fix[0] / kFixScalar;
-    if (dL_deps) *dL_deps = (double)(long long)acc_fix[1] / kFixScalar;
+    double drho = 0.0, deps = 0.0;   // the blocks' slots in index order
+    for (uint32_t b = 0; b < nblk; ++b) { drho += acc[2 * (size_t)b]; deps += acc[2 * (size_t)b + 1]; }
+    if (dL_drho0) *dL_drho0 = drho;
+    if (dL_deps) *dL_deps = deps;
     s->last_stream = st;
     return PBD_OK;
 }

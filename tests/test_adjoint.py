@@ -235,34 +235,69 @@ def test_gpu_adjoint_is_reproducible(need_gpu, pbd, scenes):
     assert gr1 == gr2 and ge1 == ge2
 
 
-@pytest.mark.gpu
-def test_gpu_adjoint_at_the_workload_size(need_gpu, pbd, scenes, adj):
+def _workload_grads(pbd, scenes, adj, frames, every):
     """The differentiable dam break at its stated size (65,536 particles, 4 iterations, the loss
-    mean |x_F - target|^2, checkpoints every 5 frames) over 10 frames, against the FP64 reverse
-    pass on the FP64 trajectory: the rest-density and eps gradients within 1%, dL/dv0 along a
-    seeded direction and as a whole within 2% (the GPU differentiates its own FP32 trajectory,
-    which has left the FP64 one by up to ~1e-3 cells by frame 10)."""
+    mean |x_F - target|^2): the GPU gradients for the FP64 trajectory's dL/dx_F, and the FP64
+    reverse pass's, with dL/dv0 along a seeded direction."""
     pos, vel, target = scenes.adjoint_dam_break()
     prm = scenes.workload_params(pbd, 72, 1000.0)
     prm.lambda_epsilon = 0.1
     prm.flags &= ~pbd.FLAG_CELL_END_QUIRK
     prm.flags |= pbd.FLAG_TRACK_IDS
-    n, frames = len(pos), 10
+    n = len(pos)
     C = adj.Consts(prm)
     x0, v0 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
     xF, _ = adj.rollout(C, x0, v0, frames)
     w = 2.0 * (xF - target) / n
     rv, rx, rr, re = adj.backward(C, x0, v0, frames, w)
-    sim = pbd.Sim(prm, n)
-    sim.add_particles(pos, vel)
-    sim.adjoint_forward(frames, 5)
-    fin = sim.state()
-    dl = np.zeros((n, 4), np.float32)
-    dl[:, :3] = 2.0 * (fin["x"][:, :3] - target[fin["ids"]]) / n
-    gv, gx, gr, ge = sim.adjoint_backward(dl)
-    sim.close()
+    _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, frames, every)
     dirn = np.random.default_rng(5).normal(size=(n, 3))
-    a, b = float(np.sum(gv[:, :3] * dirn)), float(np.sum(rv * dirn))
-    assert abs(a - b) <= 0.02 * abs(b), (a, b)
-    assert _close_l2(gv[:, :3], rv, 0.02)
-    assert abs(gr - rr) <= 0.01 * abs(rr) and abs(ge - re) <= 0.01 * abs(re), (gr, rr, ge, re)
+    return (gv, gx, gr, ge, float(np.sum(gv * dirn))), (rv, rx, rr, re, float(np.sum(rv * dirn)))
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_at_the_workload_size_one_frame(need_gpu, pbd, scenes, adj):
+    """One frame of the workload: dL/drest_density and dL/deps within 1e-4 of the FP64 reverse
+    pass (measured 1.4e-5).  The loss is averaged over 65,536 particles, so the partners' terms
+    are ~1e-7..1e-5: with a fixed 2^-32 fixed-point resolution for the scattered terms dL/deps
+    was 3.2e-3 off here.  dL/dv0 within 1% (measured 1.6e-3): on this unit lattice many pairs sit
+    at the contact distance, and the FP64 reverse pass's own dL/dv0 moves by 3.6e-3 when its
+    positions are rounded to FP32 after every iteration."""
+    (gv, gx, gr, ge, gd), (rv, rx, rr, re, rd) = _workload_grads(pbd, scenes, adj, 1, 1)
+    assert abs(gr - rr) <= 1e-4 * abs(rr) and abs(ge - re) <= 1e-4 * abs(re), (gr, rr, ge, re)
+    assert abs(gd - rd) <= 1e-2 * abs(rd), (gd, rd)
+    assert _close_l2(gv, rv, 2e-3) and _close_l2(gx, rx, 2e-3)
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_at_the_workload_size(need_gpu, pbd, scenes, adj):
+    """The workload over 10 frames (checkpoints every 5), against the FP64 reverse pass on the
+    FP64 trajectory: the rest-density and eps gradients within 1e-3 (measured 3.7e-4), dL/dv0
+    along a seeded direction and as a whole within 2% (the GPU differentiates its own FP32
+    trajectory, which has left the FP64 one by up to ~4e-4 cells by frame 10)."""
+    (gv, gx, gr, ge, gd), (rv, rx, rr, re, rd) = _workload_grads(pbd, scenes, adj, 10, 5)
+    assert abs(gd - rd) <= 0.02 * abs(rd), (gd, rd)
+    assert _close_l2(gv, rv, 0.02)
+    assert abs(gr - rr) <= 1e-3 * abs(rr) and abs(ge - re) <= 1e-3 * abs(re), (gr, rr, ge, re)
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_scales_with_the_loss(need_gpu, pbd, scenes):
+    """The scattered terms' fixed point is scaled per frame by the entering gradient's binary
+    exponent, so a loss gradient scaled by 2^-40 or 2^+20 gives gradients scaled by exactly that
+    power of two (the same integers in the fixed point), and nothing underflows or saturates."""
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(12, 10, 12), box=20, iterations=4, seed=7)
+    sim = pbd.Sim(prm, len(pos))
+    sim.add_particles(pos, vel)
+    sim.adjoint_forward(6, 3)
+    fin = sim.state()
+    dl = np.zeros((len(pos), 4), np.float32)
+    dl[:, :3] = w[fin["ids"]]
+    gv, gx, gr, ge = sim.adjoint_backward(dl)
+    assert np.any(gv[:, :3] != 0) and gr != 0 and ge != 0
+    for k in (-40, 20):
+        f = np.float32(2.0 ** k)
+        gv2, gx2, gr2, ge2 = sim.adjoint_backward(dl * f)
+        assert np.array_equal(gv2, gv * f) and np.array_equal(gx2, gx * f), k
+        assert gr2 == gr * 2.0 ** k and ge2 == ge * 2.0 ** k, k
+    sim.close()
