@@ -270,3 +270,28 @@ def test_full_size_workload_vs_oracle(need_gpu, pbd, scenes, oracle_mod):
         dv = np.abs(g["v"][:, :3] - o["v"][:, :3]).max(axis=1)
         assert dx.max() < tx and dv.max() < tv, (frames, dx.max(), dv.max())
         sim.close()
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 33, 4095, 4097, 8193])
+def test_ragged_particle_counts(need_gpu, pbd, scenes, oracle_mod, n):
+    """Particle counts around a warp and a sort tile (4096 keys): one particle alone, pairs,
+    partial warps and partial last tiles; uniform random positions in a 24^3-cell box (several
+    particles share cells, some start outside the walls and are clamped) and random velocities.
+    The front is bit-exact, then three frames within the one-frame tolerance x 10."""
+    params = scenes.workload_params(pbd, 24, 1000.0)
+    params.lambda_epsilon = 0.1
+    params.flags |= pbd.FLAG_TRACK_IDS
+    rng = np.random.default_rng(1000 + n)
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    pos[:, :3] = rng.uniform(0.5, 23.5, size=(n, 3))
+    vel[:, :3] = rng.normal(0.0, 2.0, size=(n, 3))
+    sim, orc, g, o, gs, os_ = _front_compare(pbd, oracle_mod, params, pos, vel)
+    assert np.array_equal(g["keys"], o["keys"]) and np.array_equal(g["perm"], o["perm"])
+    assert np.array_equal(gs["p"], os_["p"].astype(np.float32))
+    sim.close(); orc.close()
+    g, o, sim, orc = _run_both(pbd, oracle_mod, params, pos, vel, 3)
+    assert sim.n == n
+    assert np.array_equal(g["ids"], o["ids"])
+    assert maxdiff(g["x"][:, :3], o["x"][:, :3]) < 10 * TOL_X1
+    assert maxdiff(g["v"][:, :3], o["v"][:, :3]) < 10 * TOL_V1
