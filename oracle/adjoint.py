@@ -15,6 +15,11 @@ Fluid::compute runs (src/app/simulation/Fluid.cu:14-97):
   updatePositions v = (p - x)/dt, x = p (kernel/Update.h:11-32)
   viscosity       v <- v + c sum_j (v_j - v_i) W(|p_i - p_j|), Jacobi (kernel/Density.h:280-310)
 
+Unified solids (per-particle inverse mass w, the library's extension of the reference's
+inverseMass terms, kernel/Collision.h:223-225): a particle with w = 0 takes no gravity, its
+density correction is scaled by w_i, the contact overlap is split w_i / (w_i + w_j) (1/2 each
+with unit masses) and the viscosity coefficient is c w_i.
+
 Particles stay in id order here (the re-order is a permutation: it changes summation order
 only).  `rollout` runs frames and can keep a tape; `backward` returns dL/dv0, dL/dx0,
 dL/drest_density and dL/deps for L = sum(c . x_final) and is checked against central
@@ -26,7 +31,7 @@ PI = 3.14159265359    # Globals.h:122
 
 
 class Consts:
-    def __init__(self, prm):
+    def __init__(self, prm, inv_mass=None):
         d = 2.0 * prm.particle_radius
         if abs(d - 1.0) > 1e-12:
             raise ValueError("the restatement assumes a unit cell width (particle radius 0.5)")
@@ -55,6 +60,16 @@ class Consts:
         self.cvisc = float(prm.c_viscosity) if (prm.active & (1 << 9)) else 0.0
         if prm.active & (1 << 8):
             raise ValueError("the restatement has no vorticity")
+        # inverse masses in id order (None: every particle 1, the reference's)
+        self.w = None if inv_mass is None else np.asarray(inv_mass, np.float64)
+
+    def share(self, I, J):
+        """Contact share of particle I in pair (I, J) times (1 - stiffness) (Collision.h:223-225)."""
+        if self.w is None:
+            return np.full(len(I), self.ac)
+        wi, wj = self.w[I], self.w[J]
+        tot = wi + wj
+        return np.where(tot > 0.0, wi / np.where(tot > 0.0, tot, 1.0), 0.0) * (2.0 * self.ac)
 
     def poly6(self, L):
         inside = (L > 0.001) & (L < self.hp - 0.001)
@@ -129,7 +144,7 @@ def _lambda(C, n, I, L, rh):
 
 def _predict(C, x, v):
     vv = v.copy()
-    vv[:, 1] += C.g * C.dt
+    vv[:, 1] += C.g * C.dt * (1.0 if C.w is None else (C.w != 0.0))   # solids take no gravity
     p = x + vv * C.dt
     lo, hi = p < C.bmin, p > C.bmax
     p = np.where(lo, C.bmin + 0.001, np.where(hi, C.bmax - 0.001, p))
@@ -152,11 +167,13 @@ def frame(C, x, v, tape=None):
         sc = -C.k * (q["W"] / C.wq) ** C.n
         coef = lam[I] + lam[J] + sc
         delta = _sum(I, (coef * q["g"])[:, None] * rh, n) / C.rho0
+        if C.w is not None:
+            delta = C.w[:, None] * delta
         c = np.zeros_like(p)
         if C.collide:
             ov = C.d - L
             cm = (ov > 0.0) & (L > 0.00001)
-            c = _sum(I[cm], (C.ac * ov[cm])[:, None] * rh[cm], n)
+            c = _sum(I[cm], (C.share(I[cm], J[cm]) * ov[cm])[:, None] * rh[cm], n)
         p = p + c - delta
         x = x + c
     v = (p - x) / C.dt
@@ -165,7 +182,8 @@ def frame(C, x, v, tape=None):
             tape[-1]["pf"], tape[-1]["vu"] = p.copy(), v.copy()
         I, J, r, L, rh = _pair_geometry(C, p, I0, J0)
         W, _ = C.poly6(L)
-        v = v + C.cvisc * _sum(I, W[:, None] * (v[J] - v[I]), n)
+        ci = C.cvisc if C.w is None else (C.cvisc * C.w)[:, None]
+        v = v + ci * _sum(I, W[:, None] * (v[J] - v[I]), n)
     return p.copy(), v
 
 
@@ -188,9 +206,9 @@ def frame_backward(C, rec, gxo, gvo, acc):
         pf, vu = rec["pf"], rec["vu"]
         I, J, r, L, rh = _pair_geometry(C, pf, I0, J0)
         W, dW = C.poly6(L)
-        c = C.cvisc
-        gv_u = gvo * (1.0 - c * _sum(I, W, n))[:, None] + c * _sum(J, W[:, None] * gvo[I], n)
-        term = c * np.einsum("ij,ij->i", gvo[I], vu[J] - vu[I]) * dW
+        c = np.full(n, C.cvisc) if C.w is None else C.cvisc * C.w
+        gv_u = gvo * (1.0 - c * _sum(I, W, n))[:, None] + _sum(J, (c[I] * W)[:, None] * gvo[I], n)
+        term = c[I] * np.einsum("ij,ij->i", gvo[I], vu[J] - vu[I]) * dW
         gxo = gxo + _sum(I, term[:, None] * rh, n) - _sum(J, term[:, None] * rh, n)
         gvo = gv_u
     gp = gxo + gvo / C.dt
@@ -205,8 +223,8 @@ def frame_backward(C, rec, gxo, gvo, acc):
         dsc = -C.k * C.n * qq ** (C.n - 1) * dW / C.wq if C.n != 0 else np.zeros_like(W)
         coef = lam[I] + lam[J] + sc
         G = g[:, None] * rh
-        # Delta and contacts
-        a = -gp / C.rho0
+        # Delta (scaled by the inverse mass) and contacts
+        a = -gp / C.rho0 if C.w is None else -(C.w[:, None] * gp) / C.rho0
         gd = np.einsum("ij,ij->i", G, a[I])
         glam = _sum(I, gd, n) + _sum(J, gd, n)
         rbar = coef[:, None] * _hess_mul(g, dg, L, rh, a[I]) + (gd * dsc)[:, None] * rh
@@ -216,9 +234,10 @@ def frame_backward(C, rec, gxo, gvo, acc):
             cm = ((ov > 0.0) & (L > 0.00001)).astype(np.float64)
             rc = np.einsum("ij,ij->i", rh, cbar)
             ol = ov / L
-            rbar += (C.ac * cm)[:, None] * (-rc[:, None] * rh + ol[:, None] * (cbar - rc[:, None] * rh))
+            rbar += (C.share(I, J) * cm)[:, None] * (-rc[:, None] * rh + ol[:, None] * (cbar - rc[:, None] * rh))
         sdelta = _sum(I, coef[:, None] * G, n)
-        acc[0] += float(np.sum(gp * sdelta)) / (C.rho0 * C.rho0)
+        wgp = gp if C.w is None else C.w[:, None] * gp
+        acc[0] += float(np.sum(wgp * sdelta)) / (C.rho0 * C.rho0)
         gnew = gp + _sum(I, rbar, n) - _sum(J, rbar, n)
         # lambda
         Cbar = -glam / q["D"]

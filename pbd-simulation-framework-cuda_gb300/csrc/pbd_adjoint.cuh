@@ -6,11 +6,13 @@
 //   reorder   gather by the permutation                                           (SortReorder.h:86-115)
 //   I times   lambda_i = -(rho_i/rho0 - 1) / (B_i + |S_i|^2/rho0 + eps)             (Density.h:48-93)
 //             Delta_i = (1/rho0) sum_j (lambda_i + lambda_j + s_corr_ij) G_ij        (Density.h:104-145)
-//             c_i = sum_contacts 0.5 (1 - stiffness) (d - |r|) r_hat              (Collision.h:171-242)
-//             p <- p + c - Delta ;  x <- x + c
+//             c_i = sum_contacts s_ij (1 - stiffness) (d - |r|) r_hat             (Collision.h:171-242)
+//             p <- p + c - w_i Delta ;  x <- x + c
 //   update    v' = (p - x)/dt ; x' = p                                              (Update.h:11-32)
-//   viscosity v'' = v' + c sum_j (v'_j - v'_i) W(|p_i - p_j|), when active           (Density.h:280-310)
-// with r = p_i - p_j, G = spiky gradient g(|r|) r_hat, W = poly6.  The reverse passes scatter the
+//   viscosity v'' = v' + c w_i sum_j (v'_j - v'_i) W(|p_i - p_j|), when active       (Density.h:280-310)
+// with r = p_i - p_j, G = spiky gradient g(|r|) r_hat, W = poly6, w_i the inverse mass (1 without
+// solids; a solid's 0 holds it still) and s_ij = w_i / (w_i + w_j) its share of a contact's
+// overlap (1/2 with unit masses, Collision.h:223-225).  The reverse passes scatter the
 // pair terms to the partner with atomic adds (so the neighbour relation need not be symmetric)
 // in 64-bit fixed point, which is associative, so the gradients do not depend on the order in
 // which the atomics land: a reverse pass gives the same bits every time.  The fixed point's scale
@@ -177,17 +179,19 @@ __global__ void __launch_bounds__(128)
 adj_visc_kernel(DevParams P, const float4* __restrict__ pf, const float4* __restrict__ pa, const float4* __restrict__ vu,
                 const float4* __restrict__ gx_out, const float4* __restrict__ gv_out, float4* __restrict__ gx_mod,
                 float4* __restrict__ gv_u, unsigned long long* __restrict__ scat_p, unsigned long long* __restrict__ scat_v,
-                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax) {
+                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax,
+                const float* __restrict__ w) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
     const float4 g = gv_out[i], gx = gx_out[i];
-    AdjViscVisit vis{P, vu, pf[i], vu[i], make_float3(g.x, g.y, g.z), P.c_visc, scat_p, scat_v, fix_scale(gmax).sc, 0.f,
+    const float ci = w ? w[i] * P.c_visc : P.c_visc;   // a solid's coefficient is 0
+    AdjViscVisit vis{P, vu, pf[i], vu[i], make_float3(g.x, g.y, g.z), ci, scat_p, scat_v, fix_scale(gmax).sc, 0.f,
                      make_float3(0.f, 0.f, 0.f)};
     bool deferred = false;
     walk_seq(P, S, i, pa[i], pf, cs, ce, vis, false, &deferred);
     gx_mod[i] = make_float4(gx.x + vis.gpi.x, gx.y + vis.gpi.y, gx.z + vis.gpi.z, 0.f);
-    const float k = 1.0f - P.c_visc * vis.sumw;
+    const float k = 1.0f - ci * vis.sumw;
     gv_u[i] = make_float4(g.x * k, g.y * k, g.z * k, 0.f);
 }
 
@@ -224,9 +228,11 @@ struct AdjDeltaVisit {
     struct Contrib { int dummy; };
     const DevParams& P;
     const float* __restrict__ lambda;
+    const float* __restrict__ w;   // inverse masses (solids), or null
+    float wi;
     float4 pi;
     float li;
-    float3 a;          // Delta-bar / rho0
+    float3 a;          // Delta-bar / rho0 (w_i scales the density correction)
     float3 cbar;       // dL/dc_i = gp_in + gx
     unsigned long long* scat;   // per particle: x, y, z of dL/dp, dL/dlambda (fixed point)
     float fix;         // the frame's fixed-point scale
@@ -267,9 +273,15 @@ struct AdjDeltaVisit {
         }
         if (contact && collide) {
             const float overlap = P.d - L;
-            if (overlap > 0.0f && L > 0.00001f) {
+            // this particle's share of the overlap: w_i / (w_i + w_j), 1/2 with unit masses
+            float share = 0.5f;
+            if (w) {
+                const float wj = __ldg(w + j);
+                share = (wi + wj) > 0.0f ? wi / (wi + wj) : 0.0f;
+            }
+            if (overlap > 0.0f && L > 0.00001f && share != 0.0f) {
                 // f = ac (d - L) rhat, df/dr = ac [ -rhat rhat^T + (d - L)/L (I - rhat rhat^T) ]
-                const float ac = 0.5f * P.one_minus_stiffness;
+                const float ac = share * P.one_minus_stiffness;
                 const float rc = rh.x * cbar.x + rh.y * cbar.y + rh.z * cbar.z;
                 const float ol = overlap / L;
                 rbar.x += ac * (-rc * rh.x + ol * (cbar.x - rc * rh.x));
@@ -289,7 +301,7 @@ adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
                  const float4* __restrict__ gp_in, const float4* __restrict__ gx, float4* __restrict__ gp_out,
                  float* __restrict__ glam, unsigned long long* __restrict__ scat, unsigned long long* __restrict__ scat_in,
                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, double* acc, bool collide,
-                 NbList Lt, const uint32_t* __restrict__ gmax) {
+                 NbList Lt, const uint32_t* __restrict__ gmax, const float* __restrict__ w) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double drho = 0.0;
     if (i < P.N) {
@@ -297,9 +309,10 @@ adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
         const FixScale fs = fix_scale(gmax);
         const float4 g0 = gp_in[i], t = take_scattered(scat_in, i, fs.inv), gxi = gx[i];   // + the pass after's partners
         const float4 gpin = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
-        const float inv = 1.0f / S.rho0;
-        AdjDeltaVisit vis{P, lambda, p[i], lambda[i],
-                          make_float3(-gpin.x * inv, -gpin.y * inv, -gpin.z * inv),
+        const float wi = w ? w[i] : 1.0f;
+        const float inv = 1.0f / S.rho0, winv = wi * inv;
+        AdjDeltaVisit vis{P, lambda, w, wi, p[i], lambda[i],
+                          make_float3(-gpin.x * winv, -gpin.y * winv, -gpin.z * winv),
                           make_float3(gpin.x + gxi.x, gpin.y + gxi.y, gpin.z + gxi.z), scat, fs.sc,
                           make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), 0.f, collide};
         // the forward's near list of this iteration (the pairs within the cut), else the cells
@@ -310,8 +323,9 @@ adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
         // own terms: this thread alone writes slot i (the partners' terms are in scat)
         gp_out[i] = make_float4(gpin.x + vis.gpi.x, gpin.y + vis.gpi.y, gpin.z + vis.gpi.z, 0.f);
         glam[i] = vis.glami;
-        // Delta_i = sdelta / rho0: d/drho0 = -sdelta / rho0^2, Delta-bar = -gp_in
-        drho = (double)(gpin.x * vis.sdelta.x + gpin.y * vis.sdelta.y + gpin.z * vis.sdelta.z) * (double)(inv * inv);
+        // Delta_i = sdelta / rho0 (applied as w_i Delta_i): d/drho0 = -w_i sdelta / rho0^2, Delta-bar = -w_i gp_in
+        drho = (double)(gpin.x * vis.sdelta.x + gpin.y * vis.sdelta.y + gpin.z * vis.sdelta.z) * (double)(inv * inv) *
+               (double)wi;
     }
     block_add2(drho, 0.0, acc);
 }

@@ -90,6 +90,7 @@ struct Tape {
     uint32_t* near_meta[kMaxTapeIters];  // and their counts
     float4* p_fin;                 // with viscosity: the frame's final positions and the
     float4* v_u;                   // velocities before the viscosity pass (sorted order)
+    float* w;                      // with solids: the inverse masses (sorted order)
 };
 
 struct pbd_sim {
@@ -117,6 +118,7 @@ struct pbd_sim {
     uint32_t* adj_fin_keys = nullptr;
     float4 *adj_fin_p = nullptr, *adj_fin_col = nullptr;
     uint32_t* adj_fin_ids = nullptr;
+    float *adj_ck_w = nullptr, *adj_fin_w = nullptr;   // with solids: the inverse masses (permuted with the state)
     std::vector<Tape> adj_tape;
     float4 *adj_g[5]{};            // gradient buffers
     float* adj_glam = nullptr;
@@ -412,6 +414,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     if (front_only) return cudaGetLastError();
     const float4* pa = s->p[anchor];
     const float* wf = s->mass_used ? s->w[cur.x] : nullptr;   // after the re-order
+    if (tape && tape->w && wf) cudaMemcpyAsync(tape->w, wf, (size_t)N * 4, cudaMemcpyDeviceToDevice, st);
     auto next_p = [&](int c) { return c == anchor ? (anchor + 1) % 3 : 3 - c - anchor; };
 
     const uint32_t gn = div_up(N, tn);
@@ -1554,7 +1557,7 @@ static int adjoint_supported(const pbd_sim* s) {
     if (p.active & PBD_ACTIVE_COMPUTE_VORTICITY) { set_error("adjoint: vorticity has no reverse pass"); return PBD_ERR_UNSUPPORTED; }
     if (p.stabilization_iterations != 1 || p.solver_iterations == 0 || p.solver_iterations > (uint32_t)kMaxTapeIters) { set_error("adjoint: stabilizationIterations must be 1 and solverIterations 1..16"); return PBD_ERR_UNSUPPORTED; }
     if (p.enclosure_position_damping != 0.0f) { set_error("adjoint: enclosurePositionDamping must be 0"); return PBD_ERR_UNSUPPORTED; }
-    if (s->mass_used || s->batched) { set_error("adjoint: solids and batches have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
+    if (s->batched) { set_error("adjoint: batches have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
     if (p.collision_type != 0) { set_error("adjoint: collisionType 1 has no reverse pass"); return PBD_ERR_UNSUPPORTED; }
     return PBD_OK;
 }
@@ -1575,9 +1578,12 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     const uint32_t I = s->prm.solver_iterations;
     // workspace: checkpoints, the final state, k frames of tape, gradient buffers
     const bool visc = (s->prm.active & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
-    const size_t per_tape = N * (16 + 16 + 4 + 4 + (visc ? 32 : 0)) + (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 512;
+    const bool solids = s->mass_used != 0;
+    const size_t per_tape = N * (16 + 16 + 4 + 4 + (visc ? 32 : 0) + (solids ? 4 : 0)) +
+                            (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 768;
     const size_t acc_bytes = 16 * (size_t)div_up((uint32_t)N, 128);   // two doubles per reverse block
-    const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + acc_bytes +
+    const size_t w_bytes = solids ? ((size_t)nck + 1) * N * 4 + 512 : 0;   // checkpoints + final
+    const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + acc_bytes + w_bytes +
                         N * 64 + (size_t)(19 + (4 + 5 * I) * k) * 256;
     if (need > s->adj_bytes) {
         if (s->adj_arena) CK(cudaStreamSynchronize(st));
@@ -1597,6 +1603,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     s->adj_fin_col = (float4*)take(N * 16);
     s->adj_fin_keys = (uint32_t*)take(N * 4);
     s->adj_fin_ids = (uint32_t*)take(N * 4);
+    s->adj_ck_w = solids ? (float*)take((size_t)nck * N * 4) : nullptr;
+    s->adj_fin_w = solids ? (float*)take(N * 4) : nullptr;
     s->adj_tape.assign(k, Tape{});
     for (int t = 0; t < k; ++t) {
         Tape& T = s->adj_tape[t];
@@ -1613,6 +1621,7 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
         }
         T.p_fin = visc ? (float4*)take(N * 16) : nullptr;
         T.v_u = visc ? (float4*)take(N * 16) : nullptr;
+        T.w = solids ? (float*)take(N * 4) : nullptr;
     }
     for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
     s->adj_glam = (float*)take(N * 4);
@@ -1629,6 +1638,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
         const int nf = std::min(k, nsteps - ck * k);
         CK(cudaMemcpyAsync(s->adj_ck_x + (size_t)ck * N, s->x[s->cur.x], N * 16, cudaMemcpyDeviceToDevice, st));
         CK(cudaMemcpyAsync(s->adj_ck_v + (size_t)ck * N, s->v[s->cur.v], N * 16, cudaMemcpyDeviceToDevice, st));
+        if (solids)   // the re-order permutes the inverse masses with the state
+            CK(cudaMemcpyAsync(s->adj_ck_w + (size_t)ck * N, s->w[s->cur.x], N * 4, cudaMemcpyDeviceToDevice, st));
         if (ck + 1 < nck) {
             if (int rc = pbd_step(s, nf, stream)) return rc;
         } else {
@@ -1650,6 +1661,7 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     CK(cudaMemcpyAsync(s->adj_fin_p, s->p[s->cur.p], N * 16, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->adj_fin_col, s->col[s->cur.x], N * 16, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->adj_fin_ids, s->ids[s->cur.x], N * 4, cudaMemcpyDeviceToDevice, st));
+    if (solids) CK(cudaMemcpyAsync(s->adj_fin_w, s->w[s->cur.x], N * 4, cudaMemcpyDeviceToDevice, st));
     s->last_stream = st;
     return PBD_OK;
 }
@@ -1691,7 +1703,7 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
         adj_gmax_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, s->adj_gmax);
         if (T.p_fin) {   // the viscosity's reverse first (the frame's last pass), into gx and gp2
             adj_visc_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, gx_out, gv_out, gx, gp2, s->adj_scat,
-                                                s->adj_scat2, s->cell_start, s->cell_end, s->adj_gmax);
+                                                s->adj_scat2, s->cell_start, s->cell_end, s->adj_gmax, T.w);
             adj_update_visc_kernel<<<ge, 256, 0, st>>>(P, gx, gp2, gp, s->adj_scat, s->adj_scat2, s->adj_gmax);
         } else {
             adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
@@ -1705,7 +1717,7 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
             // whatever order the atomics landed in
             adj_delta_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.lam[it], gp, gx, gp2, s->adj_glam, s->adj_scat,
                                                  s->adj_scat2, s->cell_start, s->cell_end, s->adj_acc, collide, Lt,
-                                                 s->adj_gmax);
+                                                 s->adj_gmax, T.w);
             adj_lambda_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.aux[it], s->adj_glam, gp2, s->adj_scat2, s->adj_scat,
                                                   s->cell_start, s->cell_end, s->adj_acc, Lt, s->adj_gmax);
             std::swap(gp, gp2);
@@ -1787,6 +1799,8 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
         if (recompute) {   // the segment's checkpoint into the state buffers
             CK(cudaMemcpyAsync(s->x[s->cur.x], s->adj_ck_x + (size_t)ck * N, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
             CK(cudaMemcpyAsync(s->v[s->cur.v], s->adj_ck_v + (size_t)ck * N, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
+            if (s->adj_ck_w)
+                CK(cudaMemcpyAsync(s->w[s->cur.x], s->adj_ck_w + (size_t)ck * N, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
         }
         if (int rc = adj_segment(s, st, nf, recompute ? 1 : 2)) return rc;
     }
@@ -1798,6 +1812,7 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
     CK(cudaMemcpyAsync(s->p[s->cur.p], s->adj_fin_p, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->col[s->cur.x], s->adj_fin_col, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->ids[s->cur.x], s->adj_fin_ids, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
+    if (s->adj_fin_w) CK(cudaMemcpyAsync(s->w[s->cur.x], s->adj_fin_w, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
     s->adj_last_taped = s->adj_nck == 1;       // else the tape now holds the first segment
     s->anchor = -1;
     std::vector<double> acc((size_t)nblk * 2);

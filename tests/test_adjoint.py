@@ -1,7 +1,8 @@
 """Adjoint of the frame: dL/dv0, dL/dx0, dL/drest_density and dL/deps of L = sum(c . x_final).
 
 CPU: the FP64 restatement (oracle/adjoint.py) is pinned to the C oracle's FP64 trajectory and
-its reverse pass to central differences of its own forward, with and without XSPH viscosity.
+its reverse pass to central differences of its own forward, with and without XSPH viscosity and
+unified solids (inverse mass 0).
 GPU: pbd_adjoint_forward/backward through the C ABI against that FP64 reverse pass on the same
 seeded scene, with several checkpoint spacings, and the state the forward left restored.
 Tolerance of the GPU gradients against the FP64 reverse pass (FP32 forward and reverse): 2% of
@@ -30,18 +31,36 @@ def adjoint_scene(pbd, scenes, shape=(7, 7, 7), box=14, spacing=0.75, iterations
     return prm, pos, vel, weights
 
 
+def with_solids(pos, vel, seed=5):
+    """Unified solids in an adjoint scene: the lowest layer and a seeded tenth of the other
+    particles get inverse mass 0 and no velocity.  Returns (vel, inverse masses)."""
+    rng = np.random.default_rng(seed + 100)
+    m = np.ones(len(pos), np.float32)
+    m[pos[:, 1] < pos[:, 1].min() + 0.5] = 0.0
+    m[rng.random(len(pos)) < 0.1] = 0.0
+    vel = vel.copy()
+    vel[m == 0.0, :3] = 0.0
+    return vel, m
+
+
 @pytest.fixture(scope="module")
 def adj():
     from oracle import adjoint as m
     return m
 
 
-@pytest.mark.parametrize("viscosity", [0.0, 0.01])
-def test_restatement_follows_oracle(pbd, scenes, oracle_mod, adj, viscosity):
+@pytest.mark.parametrize("viscosity,solids", [(0.0, False), (0.01, False), (0.0, True), (0.01, True)])
+def test_restatement_follows_oracle(pbd, scenes, oracle_mod, adj, viscosity, solids):
     prm, pos, vel, _ = adjoint_scene(pbd, scenes, viscosity=viscosity)
-    C = adj.Consts(prm)
+    m = None
+    if solids:
+        vel, m = with_solids(pos, vel)
+    C = adj.Consts(prm, m)
     o = oracle_mod.Oracle(prm, len(pos), "f64")
-    o.add_particles(pos, vel)
+    if solids:
+        o.add_particles_mass(pos, vel, m)
+    else:
+        o.add_particles(pos, vel)
     x, v = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
     for _ in range(FRAMES):
         o.step(1)
@@ -50,6 +69,8 @@ def test_restatement_follows_oracle(pbd, scenes, oracle_mod, adj, viscosity):
     order = np.argsort(s["ids"])
     assert maxdiff(s["x"][order, :3], x) < 1e-8
     assert maxdiff(s["v"][order, :3], v) < 1e-6
+    if solids:   # the solids never moved
+        assert np.array_equal(x[m == 0], pos[m == 0, :3].astype(np.float64))
 
 
 def _loss(adj, C, x0, v0, w):
@@ -57,22 +78,27 @@ def _loss(adj, C, x0, v0, w):
     return float(np.sum(w * x))
 
 
-@pytest.mark.parametrize("viscosity", [0.0, 0.01])
-def test_reverse_pass_matches_central_differences(pbd, scenes, adj, viscosity):
+@pytest.mark.parametrize("viscosity,solids", [(0.0, False), (0.01, False), (0.01, True)])
+def test_reverse_pass_matches_central_differences(pbd, scenes, adj, viscosity, solids):
     prm, pos, vel, w = adjoint_scene(pbd, scenes, viscosity=viscosity)
-    C = adj.Consts(prm)
+    m = None
+    if solids:
+        vel, m = with_solids(pos, vel)
+    C = adj.Consts(prm, m)
     x0, v0 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
     gv, gx, gr, ge = adj.backward(C, x0, v0, FRAMES, w)
     rng = np.random.default_rng(11)
     dirn = rng.normal(size=x0.shape)
-    h = 1e-6
+    # with solids a step of 1e-6 straddles a contact threshold within the 8 frames (the
+    # differences at 1e-7 agree with the reverse pass to 1e-9)
+    h = 1e-7 if solids else 1e-6
     fd_v = (_loss(adj, C, x0, v0 + h * dirn, w) - _loss(adj, C, x0, v0 - h * dirn, w)) / (2 * h)
     assert abs(fd_v - np.sum(gv * dirn)) <= 1e-4 * abs(fd_v)
     fd_x = (_loss(adj, C, x0 + h * dirn, v0, w) - _loss(adj, C, x0 - h * dirn, v0, w)) / (2 * h)
     assert abs(fd_x - np.sum(gx * dirn)) <= 1e-3 * abs(fd_x)
     for attr, g in (("rho0", gr), ("eps", ge)):
         base = getattr(C, attr)
-        hh = 1e-4 * base
+        hh = (1e-5 if solids else 1e-4) * base   # 1e-4 straddles the same threshold with solids
         cp, cm = copy.copy(C), copy.copy(C)
         setattr(cp, attr, base + hh)
         setattr(cm, attr, base - hh)
@@ -89,9 +115,12 @@ def test_adjoint_symbols_and_argument_checks_declared(pbd):
 # GPU
 # ---------------------------------------------------------------------------------------
 
-def _gpu_grads(pbd, prm, pos, vel, weights, frames, every):
+def _gpu_grads(pbd, prm, pos, vel, weights, frames, every, inv_mass=None):
     sim = pbd.Sim(prm, len(pos))
-    sim.add_particles(pos, vel)
+    if inv_mass is not None:
+        sim.add_particles_mass(pos, vel, inv_mass)
+    else:
+        sim.add_particles(pos, vel)
     sim.adjoint_forward(frames, every)
     fin = sim.state()
     dl = np.zeros((len(pos), 4), np.float32)
@@ -113,12 +142,16 @@ def _close_l2(a, b, rel=0.02):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("every,viscosity", [(FRAMES, 0.0), (3, 0.0), (1, 0.0), (3, 0.01)])
-def test_gpu_adjoint_matches_fp64(need_gpu, pbd, scenes, adj, every, viscosity):
+@pytest.mark.parametrize("every,viscosity,solids", [(FRAMES, 0.0, False), (3, 0.0, False), (1, 0.0, False),
+                                                    (3, 0.01, False), (3, 0.01, True)])
+def test_gpu_adjoint_matches_fp64(need_gpu, pbd, scenes, adj, every, viscosity, solids):
     prm, pos, vel, w = adjoint_scene(pbd, scenes, viscosity=viscosity)
-    C = adj.Consts(prm)
+    m = None
+    if solids:
+        vel, m = with_solids(pos, vel)
+    C = adj.Consts(prm, m)
     rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), FRAMES, w)
-    sim, fin, after, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, FRAMES, every)
+    sim, fin, after, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, FRAMES, every, m)
     assert _close(gv, rv) and _close(gx, rx)
     assert abs(gr - rr) <= 0.02 * abs(rr) and abs(ge - re) <= 0.02 * abs(re)
     # the backward leaves the simulation as the forward left it
@@ -127,14 +160,18 @@ def test_gpu_adjoint_matches_fp64(need_gpu, pbd, scenes, adj, every, viscosity):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("iterations,viscosity", [(1, 0.0), (4, 0.0), (4, 0.01)])
-def test_gpu_adjoint_one_frame_exact(need_gpu, pbd, scenes, adj, iterations, viscosity):
+@pytest.mark.parametrize("iterations,viscosity,solids", [(1, 0.0, False), (4, 0.0, False), (4, 0.01, False),
+                                                         (4, 0.01, True)])
+def test_gpu_adjoint_one_frame_exact(need_gpu, pbd, scenes, adj, iterations, viscosity, solids):
     """one frame: the FP32 reverse pass equals the FP64 one up to FP32 rounding"""
     prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(12, 10, 12), box=20, iterations=iterations, seed=7,
                                      viscosity=viscosity)
-    C = adj.Consts(prm)
+    m = None
+    if solids:
+        vel, m = with_solids(pos, vel, seed=7)
+    C = adj.Consts(prm, m)
     rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), 1, w)
-    _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, 1, 1)
+    _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, 1, 1, m)
     assert _close_l2(gv, rv, 2e-5) and _close_l2(gx, rx, 2e-5)
     assert abs(gr - rr) <= 1e-4 * abs(rr) and abs(ge - re) <= 1e-4 * abs(re)
 
@@ -161,10 +198,18 @@ def test_gpu_adjoint_larger_scene(need_gpu, pbd, scenes, adj):
 
 
 @pytest.mark.gpu
-def test_gpu_step_after_backward_is_unchanged(need_gpu, pbd, scenes):
+@pytest.mark.parametrize("solids", [False, True])
+def test_gpu_step_after_backward_is_unchanged(need_gpu, pbd, scenes, solids):
+    """the reverse pass recomputes earlier segments (re-ordering the state and, with solids, the
+    inverse masses) and puts everything back: later frames are bit-identical to a plain run"""
     prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(10, 10, 10), box=18)
-    a = pbd.Sim(prm, len(pos)); a.add_particles(pos, vel)
-    b = pbd.Sim(prm, len(pos)); b.add_particles(pos, vel)
+    if solids:
+        vel, m = with_solids(pos, vel)
+        a = pbd.Sim(prm, len(pos)); a.add_particles_mass(pos, vel, m)
+        b = pbd.Sim(prm, len(pos)); b.add_particles_mass(pos, vel, m)
+    else:
+        a = pbd.Sim(prm, len(pos)); a.add_particles(pos, vel)
+        b = pbd.Sim(prm, len(pos)); b.add_particles(pos, vel)
     a.adjoint_forward(6, 4)
     b.step(6)
     dl = np.ones((len(pos), 4), np.float32)
