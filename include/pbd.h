@@ -314,8 +314,9 @@ int pbd_render_sprites(pbd_sim* sim, const pbd_camera* camera, uint8_t* rgba, fl
  * segment from its checkpoint (the last one is taped by the forward itself) with the neighbour
  * lists, permutations and wall contacts of the forward held fixed (they are piecewise constant),
  * and leaves the simulation as the forward left it; it may be called again for another loss on
- * the same forward.  Supported: the density solve, contacts, walls, integration, XSPH
- * viscosity and unified solids (pbd_add_particles_mass); vorticity, batches,
+ * the same forward.  Supported: the density solve, contacts, walls, integration, omega +
+ * vorticity confinement (its force reaches the next frame), XSPH viscosity and unified solids
+ * (pbd_add_particles_mass); batches, vorticity without computeOmegas,
  * stabilizationIterations != 1 and enclosurePositionDamping != 0 return PBD_ERR_UNSUPPORTED. */
 int pbd_adjoint_forward(pbd_sim* sim, int nsteps, int ckpt_every, void* stream);
 int pbd_adjoint_backward(pbd_sim* sim, const float* dL_dx_final, float* dL_dv0, float* dL_dx0,

@@ -13,6 +13,10 @@ Fluid::compute runs (src/app/simulation/Fluid.cu:14-97):
   computeDelta    (kernel/Density.h:104-145), solveCollisions (kernel/Collision.h:171-242),
   applyDelta      p <- p + c - Delta, x <- x + c (Jacobi: all reads from the iteration's snapshot)
   updatePositions v = (p - x)/dt, x = p (kernel/Update.h:11-32)
+  computeOmega    omega_i = sum_j (v_j - v_i) x grad W_spiky(p_i - p_j)          (kernel/Density.h:232-269)
+  vorticity       eta_i = sum_j |omega_j - omega_i| / (p_j - p_i + 1e-8), componentwise, over
+                  every list entry; n = (eta + 1e-8) / (|eta| + 1e-8); f_i = e (n x omega_i),
+                  the external force of the next frame's applyForces       (kernel/Density.h:179-221)
   viscosity       v <- v + c sum_j (v_j - v_i) W(|p_i - p_j|), Jacobi (kernel/Density.h:280-310)
 
 Unified solids (per-particle inverse mass w, the library's extension of the reference's
@@ -20,6 +24,7 @@ inverseMass terms, kernel/Collision.h:223-225): a particle with w = 0 takes no g
 density correction is scaled by w_i, the contact overlap is split w_i / (w_i + w_j) (1/2 each
 with unit masses) and the viscosity coefficient is c w_i.
 
+Omega, vorticity and viscosity read the positions and velocities right after updatePositions.
 Particles stay in id order here (the re-order is a permutation: it changes summation order
 only).  `rollout` runs frames and can keep a tape; `backward` returns dL/dv0, dL/dx0,
 dL/drest_density and dL/deps for L = sum(c . x_final) and is checked against central
@@ -58,8 +63,12 @@ class Consts:
         self.cut2 = c * c * 1.0001
         # XSPH viscosity (Density.h:280-310, Jacobi) after updatePositions, when active
         self.cvisc = float(prm.c_viscosity) if (prm.active & (1 << 9)) else 0.0
+        # vorticity confinement (needs computeOmegas): its force enters the next frame's predict
+        self.evort = 0.0
         if prm.active & (1 << 8):
-            raise ValueError("the restatement has no vorticity")
+            if not prm.active & (1 << 7):
+                raise ValueError("vorticity without computeOmegas reads a stale omega")
+            self.evort = float(prm.e_vorticity)
         # inverse masses in id order (None: every particle 1, the reference's)
         self.w = None if inv_mass is None else np.asarray(inv_mass, np.float64)
 
@@ -142,22 +151,51 @@ def _lambda(C, n, I, L, rh):
     return -Cc / D, dict(W=W, dW=dW, g=g, dg=dg, rho=rho, B=B, S=S, s2=s2, C=Cc, D=D)
 
 
-def _predict(C, x, v):
+def _predict(C, x, v, f=None):
     vv = v.copy()
-    vv[:, 1] += C.g * C.dt * (1.0 if C.w is None else (C.w != 0.0))   # solids take no gravity
+    moves = np.ones(len(v)) if C.w is None else (C.w != 0.0).astype(np.float64)   # solids: no gravity, no force
+    vv[:, 1] += C.g * C.dt * moves
+    if f is not None:
+        vv += C.dt * f * moves[:, None]
     p = x + vv * C.dt
     lo, hi = p < C.bmin, p > C.bmax
     p = np.where(lo, C.bmin + 0.001, np.where(hi, C.bmax - 0.001, p))
     return p, ~(lo | hi)
 
 
-def frame(C, x, v, tape=None):
-    """One frame on (n, 3) float64 positions and velocities; returns (x', v')."""
+def _omega(C, pf, vu, I0, J0):
+    """omega_i = sum_j (v_j - v_i) x G_ij over the pairs within the cut (spiky is 0 beyond)."""
+    n = len(pf)
+    I, J, r, L, rh = _pair_geometry(C, pf, I0, J0)
+    g, dg = C.spiky(L)
+    G = g[:, None] * rh
+    return _sum(I, np.cross(vu[J] - vu[I], G), n), (I, J, L, rh, g, dg, G)
+
+
+def _eta(C, pf, om, I0, J0):
+    """eta_i = sum_j |omega_j - omega_i| / (p_j - p_i + 1e-8) over every list entry."""
+    n = len(pf)
+    D = pf[J0] - pf[I0] + 1e-8
+    u = om[J0] - om[I0]
+    ol = np.sqrt(np.einsum("ij,ij->i", u, u))
+    return _sum(I0, ol[:, None] / D, n), (D, u, ol)
+
+
+def _vort_force(C, eta, om):
+    gl = np.sqrt(np.einsum("ij,ij->i", eta, eta))
+    nv = (eta + 1e-8) / (gl + 1e-8)[:, None]
+    return C.evort * np.cross(nv, om), nv, gl
+
+
+def frame(C, x, v, f=None, tape=None):
+    """One frame on (n, 3) float64 positions and velocities with the external force f of the
+    frame before (None: none); returns (x', v', f') with f' the vorticity force for the next
+    frame (zeros without vorticity)."""
     n = len(x)
-    p, _ = _predict(C, x, v)
+    p, _ = _predict(C, x, v, f)
     I0, J0 = candidate_pairs(p, C.M)
     if tape is not None:
-        tape.append(dict(x=x.copy(), v=v.copy(), I=I0, J=J0, p=[]))
+        tape.append(dict(x=x.copy(), v=v.copy(), f=None if f is None else f.copy(), I=I0, J=J0, p=[]))
     x = x.copy()
     for _ in range(C.iters):
         if tape is not None:
@@ -177,19 +215,27 @@ def frame(C, x, v, tape=None):
         p = p + c - delta
         x = x + c
     v = (p - x) / C.dt
-    if C.cvisc:   # v += c sum_j (v_j - v_i) W(|p_i - p_j|) over the frame's list, at the final positions
+    if tape is not None and (C.cvisc or C.evort):
+        tape[-1]["pf"], tape[-1]["vu"] = p.copy(), v.copy()
+    fn = np.zeros_like(p)
+    if C.evort:   # omega and the vorticity force at the final positions, from v before viscosity
+        om, _ = _omega(C, p, v, I0, J0)
+        eta, _ = _eta(C, p, om, I0, J0)
+        fn, _, _ = _vort_force(C, eta, om)
         if tape is not None:
-            tape[-1]["pf"], tape[-1]["vu"] = p.copy(), v.copy()
+            tape[-1]["om"], tape[-1]["eta"] = om, eta
+    if C.cvisc:   # v += c sum_j (v_j - v_i) W(|p_i - p_j|) over the frame's list, at the final positions
         I, J, r, L, rh = _pair_geometry(C, p, I0, J0)
         W, _ = C.poly6(L)
         ci = C.cvisc if C.w is None else (C.cvisc * C.w)[:, None]
         v = v + ci * _sum(I, W[:, None] * (v[J] - v[I]), n)
-    return p.copy(), v
+    return p.copy(), v, fn
 
 
 def rollout(C, x, v, frames, tape=None):
+    f = None
     for _ in range(frames):
-        x, v = frame(C, x, v, tape)
+        x, v, f = frame(C, x, v, f, tape)
     return x, v
 
 
@@ -198,10 +244,41 @@ def _hess_mul(g, dg, L, rh, a):
     return dg[:, None] * ra[:, None] * rh + (g / L)[:, None] * (a - ra[:, None] * rh)
 
 
-def frame_backward(C, rec, gxo, gvo, acc):
-    """Reverse of `frame` for the taped record `rec`: (dL/dx', dL/dv') -> (dL/dx, dL/dv)."""
+def _vort_backward(C, rec, gf):
+    """Reverse of omega + the vorticity force for dL/df' = gf: (dL/dp, dL/dv) at the final
+    positions and the velocities before viscosity."""
+    pf, vu, om, eta = rec["pf"], rec["vu"], rec["om"], rec["eta"]
+    I0, J0 = rec["I"], rec["J"]
+    n = len(pf)
+    _, nv, gl = _vort_force(C, eta, om)
+    nbar = C.evort * np.cross(om, gf)                 # f = e (n x omega)
+    obar = C.evort * np.cross(gf, nv)
+    ge = gl + 1e-8
+    safe = np.where(gl > 0.0, gl, 1.0)
+    etabar = nbar / ge[:, None] - eta * (np.einsum("ij,ij->i", eta + 1e-8, nbar) / (ge * ge * safe) * (gl > 0.0))[:, None]
+    _, (D, u, ol) = _eta(C, pf, om, I0, J0)
+    sq = np.einsum("ij,ij->i", etabar[I0], 1.0 / D)
+    du = np.where(ol[:, None] > 0.0, (sq / np.where(ol > 0.0, ol, 1.0))[:, None] * u, 0.0)
+    obar = obar + _sum(J0, du, n) - _sum(I0, du, n)
+    tp = -etabar[I0] * ol[:, None] / (D * D)          # d eta_i / d p_j (componentwise)
+    pbar = _sum(J0, tp, n) - _sum(I0, tp, n)
+    _, (I, J, L, rh, g, dg, G) = _omega(C, pf, vu, I0, J0)
+    gG = np.cross(G, obar[I])                         # (u x G) . obar = u . (G x obar)
+    vbar = _sum(J, gG, n) - _sum(I, gG, n)
+    rb = _hess_mul(g, dg, L, rh, np.cross(obar[I], vu[J] - vu[I]))   # dG = H dr, r = p_i - p_j
+    pbar = pbar + _sum(I, rb, n) - _sum(J, rb, n)
+    return pbar, vbar
+
+
+def frame_backward(C, rec, gxo, gvo, acc, gf=None):
+    """Reverse of `frame` for the taped record `rec`: (dL/dx', dL/dv', dL/df') ->
+    (dL/dx, dL/dv, dL/df) with f the external force the frame's applyForces took."""
     n = len(gxo)
     I0, J0 = rec["I"], rec["J"]
+    vbar = None
+    if C.evort and gf is not None and np.any(gf):
+        pbar, vbar = _vort_backward(C, rec, gf)
+        gxo = gxo + pbar
     if C.cvisc:   # reverse of the viscosity: dL/dv' -> dL/dv (before it) and dL/dp (final positions)
         pf, vu = rec["pf"], rec["vu"]
         I, J, r, L, rh = _pair_geometry(C, pf, I0, J0)
@@ -211,6 +288,8 @@ def frame_backward(C, rec, gxo, gvo, acc):
         term = c[I] * np.einsum("ij,ij->i", gvo[I], vu[J] - vu[I]) * dW
         gxo = gxo + _sum(I, term[:, None] * rh, n) - _sum(J, term[:, None] * rh, n)
         gvo = gv_u
+    if vbar is not None:   # omega read the velocities before the viscosity
+        gvo = gvo + vbar
     gp = gxo + gvo / C.dt
     gx = -gvo / C.dt
     for it in range(C.iters - 1, -1, -1):
@@ -248,10 +327,11 @@ def frame_backward(C, rec, gxo, gvo, acc):
         rbar2 = (Cbar[I] / C.rho0 * dW)[:, None] * rh + (2.0 * Dbar[I] / C.rho0)[:, None] * _hess_mul(g, dg, L, rh, G + S[I])
         gnew += _sum(I, rbar2, n) - _sum(J, rbar2, n)
         gp = gnew
-    _, mask = _predict(C, rec["x"], rec["v"])
+    _, mask = _predict(C, rec["x"], rec["v"], rec["f"])
     gx_in = gx + mask * gp
     gv_in = mask * gp * C.dt
-    return gx_in, gv_in
+    moves = np.ones(n) if C.w is None else (C.w != 0.0).astype(np.float64)
+    return gx_in, gv_in, gv_in * (C.dt * moves)[:, None]     # v* = v + dt (g + f): dL/df = dt dL/dv*
 
 
 def backward(C, x0, v0, frames, weights):
@@ -260,7 +340,8 @@ def backward(C, x0, v0, frames, weights):
     rollout(C, np.asarray(x0, np.float64), np.asarray(v0, np.float64), frames, tape)
     gx = np.asarray(weights, np.float64).copy()
     gv = np.zeros_like(gx)
+    gf = np.zeros_like(gx)      # the last frame's vorticity force acts on no frame
     acc = [0.0, 0.0]
     for rec in reversed(tape):
-        gx, gv = frame_backward(C, rec, gx, gv, acc)
+        gx, gv, gf = frame_backward(C, rec, gx, gv, acc, gf)
     return gv, gx, acc[0], acc[1]

@@ -195,6 +195,167 @@ adj_visc_kernel(DevParams P, const float4* __restrict__ pf, const float4* __rest
     gv_u[i] = make_float4(g.x * k, g.y * k, g.z * k, 0.f);
 }
 
+// Vorticity confinement backward (Density.h:179-221), before the viscosity's own terms are
+// taken up.  The frame's force f_i = e (n_i x omega_i) acts in the next frame's applyForces
+// (v* = v + dt (g + f), not on solids), so dL/df_i = dt dL/dv_i of the next frame's input, which
+// the next frame's reverse pass left in gv_out.  With eta_i = sum_j |omega_j - omega_i| /
+// (p_j - p_i + 1e-8) (componentwise, every list entry) and n = (eta + 1e-8) / (|eta| + 1e-8):
+//   nbar = e omega_i x fbar,  omegabar_i = e fbar x n,
+//   etabar = nbar / (|eta| + 1e-8) - eta ((eta + 1e-8) . nbar) / ((|eta| + 1e-8)^2 |eta|),
+// and per entry, with D = p_j - p_i + 1e-8, u = omega_j - omega_i, l = |u|:
+//   omegabar_j += (sum_a etabar_a / D_a) u / l (omegabar_i the opposite),
+//   pbar_j,a -= etabar_a l / D_a^2 (pbar_i,a the opposite).
+// Two walks of the frame's list (the anchors' cells at the final positions): eta, then the
+// terms.  Own terms: pbar into gx, omegabar into gom; partners' terms to scat_om and scat_p.
+struct AdjEtaVisit {   // eta_i, as the forward sums it
+    struct Contrib { int dummy; };
+    using Extra = float4;   // omega_j
+    const float4* __restrict__ om;
+    float4 pi, oi;
+    float ex = 0.f, ey = 0.f, ez = 0.f;
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ static Contrib zero() { return Contrib{0}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ float4 fetch(uint32_t j) const { return __ldg(om + j); }
+    __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, const float4& oj, bool) {
+        const float dx = oj.x - oi.x, dy = oj.y - oi.y, dz = oj.z - oi.z;
+        const float ol = sqrtf(dist2(dx, dy, dz));
+        ex += __fdividef(ol, (pj.x - pi.x) + 0.00000001f);
+        ey += __fdividef(ol, (pj.y - pi.y) + 0.00000001f);
+        ez += __fdividef(ol, (pj.z - pi.z) + 0.00000001f);
+        return zero();
+    }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
+};
+struct AdjVortVisit {   // the entries' terms for etabar
+    struct Contrib { int dummy; };
+    using Extra = float4;   // omega_j
+    const float4* __restrict__ om;
+    float4 pi, oi;
+    float3 eb;          // etabar_i
+    unsigned long long* scat_om;
+    unsigned long long* scat_p;
+    float fix;
+    float3 obi = make_float3(0.f, 0.f, 0.f), pbi = make_float3(0.f, 0.f, 0.f);
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ static Contrib zero() { return Contrib{0}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ float4 fetch(uint32_t j) const { return __ldg(om + j); }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, const float4& oj, bool) {
+        const float ux = oj.x - oi.x, uy = oj.y - oi.y, uz = oj.z - oi.z;
+        const float ol = sqrtf(dist2(ux, uy, uz));
+        const float Dx = (pj.x - pi.x) + 0.00000001f, Dy = (pj.y - pi.y) + 0.00000001f, Dz = (pj.z - pi.z) + 0.00000001f;
+        const float ix = 1.0f / Dx, iy = 1.0f / Dy, iz = 1.0f / Dz;
+        if (ol > 0.0f) {
+            const float sq = (eb.x * ix + eb.y * iy + eb.z * iz) / ol;
+            const float3 du = make_float3(sq * ux, sq * uy, sq * uz);
+            scatter_add3(scat_om + 4 * (size_t)j, du, fix);
+            obi.x -= du.x; obi.y -= du.y; obi.z -= du.z;
+        }
+        const float3 tp = make_float3(-eb.x * ol * ix * ix, -eb.y * ol * iy * iy, -eb.z * ol * iz * iz);
+        scatter_add3(scat_p + 4 * (size_t)j, tp, fix);
+        pbi.x -= tp.x; pbi.y -= tp.y; pbi.z -= tp.z;
+        return zero();
+    }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
+};
+
+__global__ void __launch_bounds__(128)
+adj_vort_kernel(DevParams P, const float4* __restrict__ pf, const float4* __restrict__ pa, const float4* __restrict__ om,
+                const float4* __restrict__ gv_out, const float* __restrict__ w, float4* __restrict__ gx,
+                float4* __restrict__ gom, unsigned long long* __restrict__ scat_om, unsigned long long* __restrict__ scat_p,
+                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const float4 g = gv_out[i];
+    const float k = (w && w[i] == 0.0f) ? 0.0f : P.dt;   // solids take no force
+    const float3 fb = make_float3(g.x * k, g.y * k, g.z * k);
+    if (fb.x == 0.0f && fb.y == 0.0f && fb.z == 0.0f) { gom[i] = make_float4(0.f, 0.f, 0.f, 0.f); return; }
+    const SceneCtx S = scene_ctx(P, i);
+    const float4 oi = om[i], pi = pf[i], ai = pa[i];
+    bool deferred = false;
+    AdjEtaVisit ev{om, pi, oi};
+    walk_seq(P, S, i, ai, pf, cs, ce, ev, false, &deferred);
+    const float e = P.e_vort, EPS = 0.00000001f;
+    const float gl = sqrtf(ev.ex * ev.ex + ev.ey * ev.ey + ev.ez * ev.ez), ge = gl + EPS;
+    const float3 nv = make_float3((ev.ex + EPS) / ge, (ev.ey + EPS) / ge, (ev.ez + EPS) / ge);
+    const float3 nb = make_float3(e * (oi.y * fb.z - oi.z * fb.y), e * (oi.z * fb.x - oi.x * fb.z), e * (oi.x * fb.y - oi.y * fb.x));
+    const float3 ob = make_float3(e * (fb.y * nv.z - fb.z * nv.y), e * (fb.z * nv.x - fb.x * nv.z), e * (fb.x * nv.y - fb.y * nv.x));
+    const float c2 = gl > 0.0f ? ((ev.ex + EPS) * nb.x + (ev.ey + EPS) * nb.y + (ev.ez + EPS) * nb.z) / (ge * ge * gl) : 0.0f;
+    const float3 eb = make_float3(nb.x / ge - ev.ex * c2, nb.y / ge - ev.ey * c2, nb.z / ge - ev.ez * c2);
+    AdjVortVisit vv{om, pi, oi, eb, scat_om, scat_p, fix_scale(gmax).sc};
+    walk_seq(P, S, i, ai, pf, cs, ce, vv, false, &deferred);
+    gom[i] = make_float4(ob.x + vv.obi.x, ob.y + vv.obi.y, ob.z + vv.obi.z, 0.f);
+    const float4 x0 = gx[i];
+    gx[i] = make_float4(x0.x + vv.pbi.x, x0.y + vv.pbi.y, x0.z + vv.pbi.z, 0.f);
+}
+
+// computeOmega backward (Density.h:232-269): omega_i = sum_j (v_j - v_i) x G_ij, G = g(|r|) rhat,
+// r = p_i - p_j (the pairs within the spiky support), at the final positions and the velocities
+// before the viscosity.  With obar_i (own + partners'): vbar_j += G x obar_i (vbar_i the
+// opposite), pbar_i += H (obar_i x (v_j - v_i)) (pbar_j the opposite), H = dG/dr.  Own terms go
+// into gv_u and gx, partners' terms to scat_v and scat_p.
+struct AdjOmegaVisit {
+    struct Contrib { int dummy; };
+    using Extra = float4;   // v_j
+    const DevParams& P;
+    const float4* __restrict__ vu;
+    float4 pi, vi;
+    float3 ob;
+    unsigned long long* scat_v;
+    unsigned long long* scat_p;
+    float fix;
+    float3 vbi = make_float3(0.f, 0.f, 0.f), pbi = make_float3(0.f, 0.f, 0.f);
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ static Contrib zero() { return Contrib{0}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ float4 fetch(uint32_t j) const { return __ldg(vu + j); }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, const float4& vj, bool) {
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = dist2(rx, ry, rz);
+        if (r2 >= P.cut2 || r2 <= 0.0f) return zero();
+        const float L = sqrtf(r2);
+        float g, dg;
+        spiky_g(P, L, g, dg);
+        if (g == 0.0f && dg == 0.0f) return zero();
+        const float3 rh = make_float3(rx / L, ry / L, rz / L);
+        const float3 G = make_float3(g * rh.x, g * rh.y, g * rh.z);
+        const float3 gG = make_float3(G.y * ob.z - G.z * ob.y, G.z * ob.x - G.x * ob.z, G.x * ob.y - G.y * ob.x);
+        scatter_add3(scat_v + 4 * (size_t)j, gG, fix);
+        vbi.x -= gG.x; vbi.y -= gG.y; vbi.z -= gG.z;
+        const float ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
+        const float3 ou = make_float3(ob.y * uz - ob.z * uy, ob.z * ux - ob.x * uz, ob.x * uy - ob.y * ux);
+        const float3 rb = spiky_hess_mul(g, dg, L, rh, ou);
+        pbi.x += rb.x; pbi.y += rb.y; pbi.z += rb.z;
+        scatter_sub3(scat_p + 4 * (size_t)j, rb, fix);
+        return zero();
+    }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
+};
+
+__global__ void __launch_bounds__(128)
+adj_omega_kernel(DevParams P, const float4* __restrict__ pf, const float4* __restrict__ pa, const float4* __restrict__ vu,
+                 const float4* __restrict__ gom, unsigned long long* __restrict__ scat_om, float4* __restrict__ gx,
+                 float4* __restrict__ gv_u, unsigned long long* __restrict__ scat_v, unsigned long long* __restrict__ scat_p,
+                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const FixScale fs = fix_scale(gmax);
+    const float4 t = take_scattered(scat_om, i, fs.inv), o0 = gom[i];
+    const float3 ob = make_float3(o0.x + t.x, o0.y + t.y, o0.z + t.z);
+    if (ob.x == 0.0f && ob.y == 0.0f && ob.z == 0.0f) return;
+    const SceneCtx S = scene_ctx(P, i);
+    AdjOmegaVisit vis{P, vu, pf[i], vu[i], ob, scat_v, scat_p, fs.sc};
+    bool deferred = false;
+    walk_seq(P, S, i, pa[i], pf, cs, ce, vis, false, &deferred);
+    const float4 a = gx[i], b = gv_u[i];
+    gx[i] = make_float4(a.x + vis.pbi.x, a.y + vis.pbi.y, a.z + vis.pbi.z, 0.f);
+    gv_u[i] = make_float4(b.x + vis.vbi.x, b.y + vis.vbi.y, b.z + vis.vbi.z, 0.f);
+}
+
 // update backward after the viscosity's: the partners' terms added to the own ones first
 __global__ void adj_update_visc_kernel(const DevParams P, float4* __restrict__ gx_mod, const float4* __restrict__ gv_u,
                                        float4* __restrict__ gp, unsigned long long* __restrict__ scat_p,

@@ -91,6 +91,8 @@ struct Tape {
     float4* p_fin;                 // with viscosity: the frame's final positions and the
     float4* v_u;                   // velocities before the viscosity pass (sorted order)
     float* w;                      // with solids: the inverse masses (sorted order)
+    float4* omega;                 // with vorticity: the frame's omega (sorted order) and the
+    float4* fext;                  // external force its applyForces took (pre-sort order)
 };
 
 struct pbd_sim {
@@ -122,6 +124,8 @@ struct pbd_sim {
     std::vector<Tape> adj_tape;
     float4 *adj_g[5]{};            // gradient buffers
     float* adj_glam = nullptr;
+    unsigned long long* adj_scat3 = nullptr;  // with vorticity: partners' dL/domega terms, fixed point
+    float4* adj_gom = nullptr;                // with vorticity: each particle's own dL/domega
     bool adj_last_taped = false;   // the tape holds the forward's last segment
     uint64_t gen = 0, adj_gen = 0; // bumped by every call that changes the state or parameters
     uint64_t pgen = 0;             // bumped by every call that changes the parameters, N or the block size
@@ -373,6 +377,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     if (tape) {
         cudaMemcpyAsync(tape->x_in, s->x[cur.x], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(tape->v_in, s->v[cur.v], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
+        if (tape->fext) cudaMemcpyAsync(tape->fext, s->fext, (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
     }
     PROF_BEGIN("predict_key");
     const float* wcur = s->mass_used ? s->w[cur.x] : nullptr;
@@ -593,7 +598,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         ++nl;
     }
     const int vort = (act & PBD_ACTIVE_COMPUTE_VORTICITY) != 0, visc = (act & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
-    if (tape && visc && tape->p_fin) {   // what the viscosity's reverse pass reads
+    if (tape && (visc || vort) && tape->p_fin) {   // what the viscosity's and vorticity's reverse passes read
         cudaMemcpyAsync(tape->p_fin, s->x[cur.x], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(tape->v_u, s->v[cur.v], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
     }
@@ -625,6 +630,7 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             nl += 2;
         }
         PROF_END();
+        if (tape && tape->omega) cudaMemcpyAsync(tape->omega, s->omega, (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
     }
     if (vort || visc) {
         // vorticity sums every list entry: the full list; viscosity alone: the omega pass's near list
@@ -1554,7 +1560,10 @@ static int adjoint_supported(const pbd_sim* s) {
     const uint32_t need = PBD_ACTIVE_APPLY_FORCES | PBD_ACTIVE_FIND_CONTACTS | PBD_ACTIVE_COMPUTE_LAMBDA |
                           PBD_ACTIVE_COMPUTE_DELTA_POSITIONS | PBD_ACTIVE_APPLY_DELTA_POSITIONS | PBD_ACTIVE_UPDATE_POSITIONS;
     if ((p.active & need) != need) { set_error("adjoint: applyForces, findContacts, computeLambda, computeDeltaPositions, applyDeltaPositions and updatePositions must be active"); return PBD_ERR_UNSUPPORTED; }
-    if (p.active & PBD_ACTIVE_COMPUTE_VORTICITY) { set_error("adjoint: vorticity has no reverse pass"); return PBD_ERR_UNSUPPORTED; }
+    if ((p.active & PBD_ACTIVE_COMPUTE_VORTICITY) && !(p.active & PBD_ACTIVE_COMPUTE_OMEGAS)) {
+        set_error("adjoint: vorticity needs computeOmegas (it would read a stale omega)");
+        return PBD_ERR_UNSUPPORTED;
+    }
     if (p.stabilization_iterations != 1 || p.solver_iterations == 0 || p.solver_iterations > (uint32_t)kMaxTapeIters) { set_error("adjoint: stabilizationIterations must be 1 and solverIterations 1..16"); return PBD_ERR_UNSUPPORTED; }
     if (p.enclosure_position_damping != 0.0f) { set_error("adjoint: enclosurePositionDamping must be 0"); return PBD_ERR_UNSUPPORTED; }
     if (s->batched) { set_error("adjoint: batches have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
@@ -1579,11 +1588,13 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     // workspace: checkpoints, the final state, k frames of tape, gradient buffers
     const bool visc = (s->prm.active & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     const bool solids = s->mass_used != 0;
-    const size_t per_tape = N * (16 + 16 + 4 + 4 + (visc ? 32 : 0) + (solids ? 4 : 0)) +
-                            (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 768;
+    const bool vort = (s->prm.active & PBD_ACTIVE_COMPUTE_VORTICITY) != 0;
+    const size_t per_tape = N * (16 + 16 + 4 + 4 + ((visc || vort) ? 32 : 0) + (solids ? 4 : 0) + (vort ? 32 : 0)) +
+                            (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 1280;
     const size_t acc_bytes = 16 * (size_t)div_up((uint32_t)N, 128);   // two doubles per reverse block
     const size_t w_bytes = solids ? ((size_t)nck + 1) * N * 4 + 512 : 0;   // checkpoints + final
-    const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + acc_bytes + w_bytes +
+    const size_t vort_bytes = vort ? N * 48 + 512 : 0;                     // scat3 + gom
+    const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + acc_bytes + w_bytes + vort_bytes +
                         N * 64 + (size_t)(19 + (4 + 5 * I) * k) * 256;
     if (need > s->adj_bytes) {
         if (s->adj_arena) CK(cudaStreamSynchronize(st));
@@ -1619,9 +1630,11 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
             T.near[it] = (uint32_t*)take(N * 4 * kListMax);
             T.near_meta[it] = (uint32_t*)take(N * 4);
         }
-        T.p_fin = visc ? (float4*)take(N * 16) : nullptr;
-        T.v_u = visc ? (float4*)take(N * 16) : nullptr;
+        T.p_fin = (visc || vort) ? (float4*)take(N * 16) : nullptr;
+        T.v_u = (visc || vort) ? (float4*)take(N * 16) : nullptr;
         T.w = solids ? (float*)take(N * 4) : nullptr;
+        T.omega = vort ? (float4*)take(N * 16) : nullptr;
+        T.fext = vort ? (float4*)take(N * 16) : nullptr;
     }
     for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
     s->adj_glam = (float*)take(N * 4);
@@ -1629,6 +1642,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     s->adj_gmax = (uint32_t*)take(4);
     s->adj_scat = (unsigned long long*)take((size_t)N * 32);
     s->adj_scat2 = (unsigned long long*)take((size_t)N * 32);
+    s->adj_scat3 = vort ? (unsigned long long*)take((size_t)N * 32) : nullptr;
+    s->adj_gom = vort ? (float4*)take((size_t)N * 16) : nullptr;
     s->adj_steps = nsteps;
     s->adj_every = k;
     s->adj_nck = nck;
@@ -1684,6 +1699,7 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
     const bool lists = near_lists_on(s, P);
     const bool collide = s->prm.collision_type == 0;
     const uint32_t gn = div_up(N, 128), ge = div_up(N, 256);
+    const bool visc_on = (s->prm.active & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     float4 *gx_out = s->adj_g[0], *gv_out = s->adj_g[1], *gx = s->adj_g[2];
     if (recompute) {
         for (int t = 0; t < nf; ++t) {
@@ -1701,9 +1717,22 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
         // the frame's fixed-point scale, from the gradient entering it
         cudaMemsetAsync(s->adj_gmax, 0, 4, st);
         adj_gmax_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, s->adj_gmax);
-        if (T.p_fin) {   // the viscosity's reverse first (the frame's last pass), into gx and gp2
-            adj_visc_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, gx_out, gv_out, gx, gp2, s->adj_scat,
-                                                s->adj_scat2, s->cell_start, s->cell_end, s->adj_gmax, T.w);
+        if (T.p_fin) {
+            // the passes after updatePositions, last first, into gx (dL/dp final) and gp2 (dL/dv
+            // before the viscosity): the viscosity's own terms, then vorticity's and omega's
+            if (visc_on) {
+                adj_visc_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, gx_out, gv_out, gx, gp2, s->adj_scat,
+                                                    s->adj_scat2, s->cell_start, s->cell_end, s->adj_gmax, T.w);
+            } else {
+                cudaMemcpyAsync(gx, gx_out, (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
+                cudaMemcpyAsync(gp2, gv_out, (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
+            }
+            if (T.omega) {   // dL/df of this frame's force is in gv_out (the next frame's dL/dv)
+                adj_vort_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.omega, gv_out, T.w, gx, s->adj_gom,
+                                                    s->adj_scat3, s->adj_scat, s->cell_start, s->cell_end, s->adj_gmax);
+                adj_omega_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, s->adj_gom, s->adj_scat3, gx, gp2,
+                                                     s->adj_scat2, s->adj_scat, s->cell_start, s->cell_end, s->adj_gmax);
+            }
             adj_update_visc_kernel<<<ge, 256, 0, st>>>(P, gx, gp2, gp, s->adj_scat, s->adj_scat2, s->adj_gmax);
         } else {
             adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
@@ -1722,8 +1751,8 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
                                                   s->cell_start, s->cell_end, s->adj_acc, Lt, s->adj_gmax);
             std::swap(gp, gp2);
         }
-        adj_predict_kernel<<<ge, 256, 0, st>>>(P, T.perm, T.x_in, T.v_in, s->fext, gp, gx, gx_out, gv_out, s->adj_scat2,
-                                               s->adj_gmax);
+        adj_predict_kernel<<<ge, 256, 0, st>>>(P, T.perm, T.x_in, T.v_in, T.fext ? T.fext : s->fext, gp, gx, gx_out, gv_out,
+                                               s->adj_scat2, s->adj_gmax);
     }
     // back to the tables the next recompute's predict expects: the cells of keys[fin]
     retable(s, st, held, s->keys[fin], N);

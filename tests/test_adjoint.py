@@ -1,8 +1,8 @@
 """Adjoint of the frame: dL/dv0, dL/dx0, dL/drest_density and dL/deps of L = sum(c . x_final).
 
 CPU: the FP64 restatement (oracle/adjoint.py) is pinned to the C oracle's FP64 trajectory and
-its reverse pass to central differences of its own forward, with and without XSPH viscosity and
-unified solids (inverse mass 0).
+its reverse pass to central differences of its own forward, with and without XSPH viscosity,
+unified solids (inverse mass 0) and vorticity confinement (whose force enters the next frame).
 GPU: pbd_adjoint_forward/backward through the C ABI against that FP64 reverse pass on the same
 seeded scene, with several checkpoint spacings, and the state the forward left restored.
 Tolerance of the GPU gradients against the FP64 reverse pass (FP32 forward and reverse): 2% of
@@ -19,8 +19,8 @@ FRAMES = 8
 
 
 def adjoint_scene(pbd, scenes, shape=(7, 7, 7), box=14, spacing=0.75, iterations=3, seed=5, vel_sigma=1.0,
-                  viscosity=0.0):
-    prm = scenes.workload_params(pbd, box, 1000.0, iterations=iterations, viscosity=viscosity)
+                  viscosity=0.0, vorticity=0.0):
+    prm = scenes.workload_params(pbd, box, 1000.0, iterations=iterations, viscosity=viscosity, vorticity=vorticity)
     prm.lambda_epsilon = 0.1
     prm.flags &= ~pbd.FLAG_CELL_END_QUIRK
     prm.flags |= pbd.FLAG_TRACK_IDS
@@ -49,9 +49,10 @@ def adj():
     return m
 
 
-@pytest.mark.parametrize("viscosity,solids", [(0.0, False), (0.01, False), (0.0, True), (0.01, True)])
-def test_restatement_follows_oracle(pbd, scenes, oracle_mod, adj, viscosity, solids):
-    prm, pos, vel, _ = adjoint_scene(pbd, scenes, viscosity=viscosity)
+@pytest.mark.parametrize("viscosity,solids,vorticity", [(0.0, False, 0.0), (0.01, False, 0.0), (0.0, True, 0.0),
+                                                        (0.01, True, 0.0), (0.0, False, 0.01), (0.01, True, 0.01)])
+def test_restatement_follows_oracle(pbd, scenes, oracle_mod, adj, viscosity, solids, vorticity):
+    prm, pos, vel, _ = adjoint_scene(pbd, scenes, viscosity=viscosity, vorticity=vorticity)
     m = None
     if solids:
         vel, m = with_solids(pos, vel)
@@ -62,9 +63,10 @@ def test_restatement_follows_oracle(pbd, scenes, oracle_mod, adj, viscosity, sol
     else:
         o.add_particles(pos, vel)
     x, v = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+    f = None
     for _ in range(FRAMES):
         o.step(1)
-        x, v = adj.frame(C, x, v)
+        x, v, f = adj.frame(C, x, v, f)
     s = o.state()
     order = np.argsort(s["ids"])
     assert maxdiff(s["x"][order, :3], x) < 1e-8
@@ -78,9 +80,10 @@ def _loss(adj, C, x0, v0, w):
     return float(np.sum(w * x))
 
 
-@pytest.mark.parametrize("viscosity,solids", [(0.0, False), (0.01, False), (0.01, True)])
-def test_reverse_pass_matches_central_differences(pbd, scenes, adj, viscosity, solids):
-    prm, pos, vel, w = adjoint_scene(pbd, scenes, viscosity=viscosity)
+@pytest.mark.parametrize("viscosity,solids,vorticity", [(0.0, False, 0.0), (0.01, False, 0.0), (0.01, True, 0.0),
+                                                        (0.0, False, 0.01), (0.01, True, 0.01)])
+def test_reverse_pass_matches_central_differences(pbd, scenes, adj, viscosity, solids, vorticity):
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, viscosity=viscosity, vorticity=vorticity)
     m = None
     if solids:
         vel, m = with_solids(pos, vel)
@@ -89,16 +92,16 @@ def test_reverse_pass_matches_central_differences(pbd, scenes, adj, viscosity, s
     gv, gx, gr, ge = adj.backward(C, x0, v0, FRAMES, w)
     rng = np.random.default_rng(11)
     dirn = rng.normal(size=x0.shape)
-    # with solids a step of 1e-6 straddles a contact threshold within the 8 frames (the
-    # differences at 1e-7 agree with the reverse pass to 1e-9)
-    h = 1e-7 if solids else 1e-6
+    # with solids or vorticity a step of 1e-6 straddles a contact threshold within the 8 frames
+    # (the differences at 1e-7 agree with the reverse pass to 1e-8)
+    h = 1e-7 if (solids or vorticity) else 1e-6
     fd_v = (_loss(adj, C, x0, v0 + h * dirn, w) - _loss(adj, C, x0, v0 - h * dirn, w)) / (2 * h)
-    assert abs(fd_v - np.sum(gv * dirn)) <= 1e-4 * abs(fd_v)
+    assert abs(fd_v - np.sum(gv * dirn)) <= 1e-4 * abs(fd_v), (fd_v, np.sum(gv * dirn))
     fd_x = (_loss(adj, C, x0 + h * dirn, v0, w) - _loss(adj, C, x0 - h * dirn, v0, w)) / (2 * h)
     assert abs(fd_x - np.sum(gx * dirn)) <= 1e-3 * abs(fd_x)
     for attr, g in (("rho0", gr), ("eps", ge)):
         base = getattr(C, attr)
-        hh = (1e-5 if solids else 1e-4) * base   # 1e-4 straddles the same threshold with solids
+        hh = (1e-5 if (solids or vorticity) else 1e-4) * base   # 1e-4 straddles the same threshold there
         cp, cm = copy.copy(C), copy.copy(C)
         setattr(cp, attr, base + hh)
         setattr(cm, attr, base - hh)
@@ -142,10 +145,12 @@ def _close_l2(a, b, rel=0.02):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("every,viscosity,solids", [(FRAMES, 0.0, False), (3, 0.0, False), (1, 0.0, False),
-                                                    (3, 0.01, False), (3, 0.01, True)])
-def test_gpu_adjoint_matches_fp64(need_gpu, pbd, scenes, adj, every, viscosity, solids):
-    prm, pos, vel, w = adjoint_scene(pbd, scenes, viscosity=viscosity)
+@pytest.mark.parametrize("every,viscosity,solids,vorticity", [(FRAMES, 0.0, False, 0.0), (3, 0.0, False, 0.0),
+                                                              (1, 0.0, False, 0.0), (3, 0.01, False, 0.0),
+                                                              (3, 0.01, True, 0.0), (3, 0.0, False, 0.01),
+                                                              (3, 0.01, True, 0.01)])
+def test_gpu_adjoint_matches_fp64(need_gpu, pbd, scenes, adj, every, viscosity, solids, vorticity):
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, viscosity=viscosity, vorticity=vorticity)
     m = None
     if solids:
         vel, m = with_solids(pos, vel)
@@ -237,7 +242,8 @@ def test_gpu_adjoint_rejects_unsupported(need_gpu, pbd, scenes):
     assert e.value.code == pbd.ERR_INVALID_ARG
     p2 = pbd.Params.from_buffer_copy(prm)
     p2.e_vorticity = 0.01
-    p2.active |= pbd.ACTIVE["computeOmegas"] | pbd.ACTIVE["computeVorticity"]
+    p2.active |= pbd.ACTIVE["computeVorticity"]          # without computeOmegas: a stale omega
+    p2.active &= ~pbd.ACTIVE["computeOmegas"]
     sim.set_params(p2)
     with pytest.raises(pbd.PBDError) as e:
         sim.adjoint_forward(2, 1)
@@ -346,3 +352,30 @@ def test_gpu_adjoint_scales_with_the_loss(need_gpu, pbd, scenes):
         assert np.array_equal(gv2, gv * f) and np.array_equal(gx2, gx * f), k
         assert gr2 == gr * 2.0 ** k and ge2 == ge * 2.0 ** k, k
     sim.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("viscosity,solids", [(0.0, False), (0.01, True)])
+def test_gpu_adjoint_vorticity_two_frames(need_gpu, pbd, scenes, adj, viscosity, solids):
+    """Vorticity confinement's force acts in the next frame, so two frames are the shortest
+    rollout it changes.  With e = 0.01 (20x the fluid workload's) it moves dL/dv0 by 4.3e-4
+    (8e-4 with solids and viscosity); the FP32 reverse pass is within 2e-5 (9e-5) of the FP64
+    one.  Stronger vorticity makes the gradient stiff (its force's direction sums
+    1/(p_j - p_i + 1e-8)): at e = 0.3 the FP32 and FP64 trajectories' forces differ by 9e-4 after
+    one frame and the GPU gradient departs from the FP64 one by ~1%."""
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(12, 10, 12), box=20, iterations=4, seed=7,
+                                     viscosity=viscosity, vorticity=0.01)
+    m = None
+    if solids:
+        vel, m = with_solids(pos, vel, seed=7)
+    C = adj.Consts(prm, m)
+    x0, v0 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+    rv, rx, rr, re = adj.backward(C, x0, v0, 2, w)
+    # the vorticity force matters: the gradients differ from those of the same rollout without it
+    C0 = adj.Consts(prm, m)
+    C0.evort = 0.0
+    rv0 = adj.backward(C0, x0, v0, 2, w)[0]
+    assert not _close_l2(rv0, rv, 3e-4)
+    _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, 2, 1, m)
+    assert _close_l2(gv, rv, 2.5e-4) and _close_l2(gx, rx, 2.5e-4)
+    assert abs(gr - rr) <= 5e-4 * abs(rr) and abs(ge - re) <= 5e-4 * abs(re)
