@@ -121,6 +121,7 @@ struct pbd_sim {
     float4 *adj_fin_p = nullptr, *adj_fin_col = nullptr;
     uint32_t* adj_fin_ids = nullptr;
     float *adj_ck_w = nullptr, *adj_fin_w = nullptr;   // with solids: the inverse masses (permuted with the state)
+    float4 *adj_ck_f = nullptr, *adj_fin_f = nullptr;  // with vorticity: the force the next frame applies
     std::vector<Tape> adj_tape;
     float4 *adj_g[5]{};            // gradient buffers
     float* adj_glam = nullptr;
@@ -1593,7 +1594,7 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
                             (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 1280;
     const size_t acc_bytes = 16 * (size_t)div_up((uint32_t)N, 128);   // two doubles per reverse block
     const size_t w_bytes = solids ? ((size_t)nck + 1) * N * 4 + 512 : 0;   // checkpoints + final
-    const size_t vort_bytes = vort ? N * 48 + 512 : 0;                     // scat3 + gom
+    const size_t vort_bytes = vort ? N * 48 + ((size_t)nck + 1) * N * 16 + 1024 : 0;   // scat3, gom, force checkpoints
     const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + acc_bytes + w_bytes + vort_bytes +
                         N * 64 + (size_t)(19 + (4 + 5 * I) * k) * 256;
     if (need > s->adj_bytes) {
@@ -1616,6 +1617,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     s->adj_fin_ids = (uint32_t*)take(N * 4);
     s->adj_ck_w = solids ? (float*)take((size_t)nck * N * 4) : nullptr;
     s->adj_fin_w = solids ? (float*)take(N * 4) : nullptr;
+    s->adj_ck_f = vort ? (float4*)take((size_t)nck * N * 16) : nullptr;
+    s->adj_fin_f = vort ? (float4*)take(N * 16) : nullptr;
     s->adj_tape.assign(k, Tape{});
     for (int t = 0; t < k; ++t) {
         Tape& T = s->adj_tape[t];
@@ -1655,6 +1658,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
         CK(cudaMemcpyAsync(s->adj_ck_v + (size_t)ck * N, s->v[s->cur.v], N * 16, cudaMemcpyDeviceToDevice, st));
         if (solids)   // the re-order permutes the inverse masses with the state
             CK(cudaMemcpyAsync(s->adj_ck_w + (size_t)ck * N, s->w[s->cur.x], N * 4, cudaMemcpyDeviceToDevice, st));
+        if (vort)     // the vorticity force the segment's first frame applies
+            CK(cudaMemcpyAsync(s->adj_ck_f + (size_t)ck * N, s->fext, N * 16, cudaMemcpyDeviceToDevice, st));
         if (ck + 1 < nck) {
             if (int rc = pbd_step(s, nf, stream)) return rc;
         } else {
@@ -1677,6 +1682,7 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     CK(cudaMemcpyAsync(s->adj_fin_col, s->col[s->cur.x], N * 16, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->adj_fin_ids, s->ids[s->cur.x], N * 4, cudaMemcpyDeviceToDevice, st));
     if (solids) CK(cudaMemcpyAsync(s->adj_fin_w, s->w[s->cur.x], N * 4, cudaMemcpyDeviceToDevice, st));
+    if (vort) CK(cudaMemcpyAsync(s->adj_fin_f, s->fext, N * 16, cudaMemcpyDeviceToDevice, st));
     s->last_stream = st;
     return PBD_OK;
 }
@@ -1830,6 +1836,8 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
             CK(cudaMemcpyAsync(s->v[s->cur.v], s->adj_ck_v + (size_t)ck * N, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
             if (s->adj_ck_w)
                 CK(cudaMemcpyAsync(s->w[s->cur.x], s->adj_ck_w + (size_t)ck * N, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
+            if (s->adj_ck_f)
+                CK(cudaMemcpyAsync(s->fext, s->adj_ck_f + (size_t)ck * N, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
         }
         if (int rc = adj_segment(s, st, nf, recompute ? 1 : 2)) return rc;
     }
@@ -1842,6 +1850,7 @@ int pbd_adjoint_backward(pbd_sim* s, const float* dL_dx_final, float* dL_dv0, fl
     CK(cudaMemcpyAsync(s->col[s->cur.x], s->adj_fin_col, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(s->ids[s->cur.x], s->adj_fin_ids, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
     if (s->adj_fin_w) CK(cudaMemcpyAsync(s->w[s->cur.x], s->adj_fin_w, (size_t)N * 4, cudaMemcpyDeviceToDevice, st));
+    if (s->adj_fin_f) CK(cudaMemcpyAsync(s->fext, s->adj_fin_f, (size_t)N * 16, cudaMemcpyDeviceToDevice, st));
     s->adj_last_taped = s->adj_nck == 1;       // else the tape now holds the first segment
     s->anchor = -1;
     std::vector<double> acc((size_t)nblk * 2);

@@ -203,11 +203,12 @@ def test_gpu_adjoint_larger_scene(need_gpu, pbd, scenes, adj):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("solids", [False, True])
-def test_gpu_step_after_backward_is_unchanged(need_gpu, pbd, scenes, solids):
+@pytest.mark.parametrize("solids,vorticity", [(False, 0.0), (True, 0.0), (False, 0.01)])
+def test_gpu_step_after_backward_is_unchanged(need_gpu, pbd, scenes, solids, vorticity):
     """the reverse pass recomputes earlier segments (re-ordering the state and, with solids, the
-    inverse masses) and puts everything back: later frames are bit-identical to a plain run"""
-    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(10, 10, 10), box=18)
+    inverse masses; with vorticity, from each segment's force) and puts everything back: later
+    frames are bit-identical to a plain run"""
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(10, 10, 10), box=18, vorticity=vorticity)
     if solids:
         vel, m = with_solids(pos, vel)
         a = pbd.Sim(prm, len(pos)); a.add_particles_mass(pos, vel, m)
@@ -379,3 +380,20 @@ def test_gpu_adjoint_vorticity_two_frames(need_gpu, pbd, scenes, adj, viscosity,
     _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, 2, 1, m)
     assert _close_l2(gv, rv, 2.5e-4) and _close_l2(gx, rx, 2.5e-4)
     assert abs(gr - rr) <= 5e-4 * abs(rr) and abs(ge - re) <= 5e-4 * abs(re)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solids", [False, True])
+def test_gpu_adjoint_segments_agree(need_gpu, pbd, scenes, solids):
+    """Recomputing a segment from its checkpoint (x, v, the inverse masses and the force the next
+    frame applies) gives the forward's own tape, bit for bit: gradients through 6 frames of
+    vorticity and viscosity are the same with one segment and with segments of 1 and 2 frames."""
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, shape=(10, 10, 10), box=18, viscosity=0.01, vorticity=0.01)
+    m = None
+    if solids:
+        vel, m = with_solids(pos, vel)
+    runs = [_gpu_grads(pbd, prm, pos, vel, w, 6, every, m)[3:] for every in (6, 2, 1)]
+    gv0, gx0, gr0, ge0 = runs[0]
+    for gv, gx, gr, ge in runs[1:]:
+        assert np.array_equal(gv, gv0) and np.array_equal(gx, gx0)
+        assert gr == gr0 and ge == ge0
