@@ -1,7 +1,7 @@
 """Benchmark of the GB300 PBD step: particle-steps/s on the 1M-particle fluid workloads.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
-                    [--leg headline|contacts|batched|batched_frames|solids|adjoint|dense|render]
+                    [--leg headline|contacts|batched|batched_frames|solids|adjoint|adjoint_physics|dense|render]
 
 Our arm (default): the headline workload fluid_1m -- 100^3 = 1,000,000 fluid particles in a
 128^3-cell domain (seed 2), kernel radius 1, 4 solver iterations, vorticity 5e-4, XSPH 0.01,
@@ -417,15 +417,18 @@ def run_solids(torch, pbd, scenes, stream, sh, frames):
             "ms_per_frame": ms, "particle_steps_per_s": len(pos) * 1e3 / ms}
 
 
-def run_adjoint(torch, pbd, scenes, stream, sh, frames=60, every=10, fd_check=True, short=(10, 5, 2)):
+def run_adjoint(torch, pbd, scenes, stream, sh, frames=60, every=10, fd_check=True, short=(10, 5, 2),
+                physics=False):
     """Differentiable dam break (65,536 particles, 60 frames x 4 iterations, checkpoints every
     10): device time of forward+adjoint against the forward alone, and the gradient of
     L = mean |x_final - target|^2 along a seeded direction of v0 and for rest density and eps,
     against central differences of the FP64 oracle (the step 1e-3, and a step near the FP32
-    resolution of the parameter), at the full horizon and at a short one."""
+    resolution of the parameter), at the full horizon and at a short one.  physics: the same
+    scene with the fluid workload's vorticity confinement (5e-4) and XSPH viscosity (0.01), both
+    differentiated (timing only)."""
     pos, vel, target = scenes.adjoint_dam_break()
     n = len(pos)
-    p = scenes.workload_params(pbd, 72, 1000.0)
+    p = scenes.workload_params(pbd, 72, 1000.0, vorticity=0.0005 if physics else 0.0, viscosity=0.01 if physics else 0.0)
     p.lambda_epsilon = 0.1
     p.flags &= ~pbd.FLAG_CELL_END_QUIRK
     p.flags |= pbd.FLAG_TRACK_IDS
@@ -466,7 +469,8 @@ def run_adjoint(torch, pbd, scenes, stream, sh, frames=60, every=10, fd_check=Tr
         ms_adj_fwd = e0.elapsed_time(e2)
         short_grads = [gradients(sim, h) for h in short] if fd_check else []
         sim.sync()
-    out = {"workload": "adjoint_64k", "particles": n, "frames": frames, "iterations": p.solver_iterations,
+    out = {"workload": "adjoint_64k" + ("_vorticity_xsph" if physics else ""), "particles": n, "frames": frames,
+           "iterations": p.solver_iterations,
            "checkpoint_every": every, "loss": loss, "forward_ms": ms_fwd, "forward_plus_adjoint_ms": ms_adj,
            "adjoint_forward_ms": ms_adj_fwd, "adjoint_backward_ms": ms_adj - ms_adj_fwd,
            "cost_ratio": ms_adj / ms_fwd, "dL_drest_density": gr, "dL_deps": ge,
@@ -811,6 +815,7 @@ def run_ours(args):
     batched = leg(run_batched, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 60)))
     solids = leg(run_solids, torch, pbd, scenes, stream, sh, frames=max(10, min(args.steps, 100)))
     adjoint = leg(run_adjoint, torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check)
+    adjoint_physics = leg(run_adjoint, torch, pbd, scenes, stream, sh, fd_check=False, physics=True)
     contacts = leg(run_contacts, torch, pbd, scenes, stream, sh, frames=20)
 
     line = {
@@ -820,7 +825,8 @@ def run_ours(args):
         "config": head["config"], "clocks": head["clocks"], "e2e": head["e2e"], "gpu_launches": head["gpu_launches"],
         "roofline": head["roofline"], "step_roofline": head["step_roofline"],
         "kernel_ms_per_frame": head["kernel_ms_per_frame"], "density_error": head["density_error"],
-        "dense": dense, "batched": batched, "solids": solids, "adjoint": adjoint, "contacts": contacts,
+        "dense": dense, "batched": batched, "solids": solids, "adjoint": adjoint, "adjoint_physics": adjoint_physics,
+        "contacts": contacts,
         "render": head.get("render"),
     }
     if rank == 0:
@@ -869,7 +875,8 @@ def run_leg(args):
             sim.step(args.warmup + args.steps, stream=sh)
             out = run_render(torch, pbd, sim, stream, sh, reps=3)
     else:
-        out = run_adjoint(torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check)
+        out = run_adjoint(torch, pbd, scenes, stream, sh, fd_check=not args.no_fd_check and args.leg == "adjoint",
+                          physics=args.leg == "adjoint_physics")
     print(json.dumps({"leg": args.leg, **out}), flush=True)
     return 0
 
@@ -883,8 +890,8 @@ def main():
     ap.add_argument("--workload", default="fluid_1m")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-fd-check", action="store_true", help="skip the FP64 finite-difference check of the adjoint")
-    ap.add_argument("--leg", choices=["headline", "contacts", "batched", "batched_frames", "solids", "adjoint", "dense",
-                                      "render"],
+    ap.add_argument("--leg", choices=["headline", "contacts", "batched", "batched_frames", "solids", "adjoint",
+                                      "adjoint_physics", "dense", "render"],
                     help="measure only this secondary workload and print its result (not the bench line)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -173,61 +173,16 @@ struct AdjViscVisit {
     __device__ __forceinline__ void add(const Contrib&, bool) {}
 };
 
-// gx_mod = dL/dx' + the viscosity's own dL/dp terms, gv_u = dL/dv before the viscosity (own
-// terms); the partners' terms go to scat_p / scat_v for adj_update_visc_kernel.
-__global__ void __launch_bounds__(128)
-adj_visc_kernel(DevParams P, const float4* __restrict__ pf, const float4* __restrict__ pa, const float4* __restrict__ vu,
-                const float4* __restrict__ gx_out, const float4* __restrict__ gv_out, float4* __restrict__ gx_mod,
-                float4* __restrict__ gv_u, unsigned long long* __restrict__ scat_p, unsigned long long* __restrict__ scat_v,
-                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax,
-                const float* __restrict__ w) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P.N) return;
-    const SceneCtx S = scene_ctx(P, i);
-    const float4 g = gv_out[i], gx = gx_out[i];
-    const float ci = w ? w[i] * P.c_visc : P.c_visc;   // a solid's coefficient is 0
-    AdjViscVisit vis{P, vu, pf[i], vu[i], make_float3(g.x, g.y, g.z), ci, scat_p, scat_v, fix_scale(gmax).sc, 0.f,
-                     make_float3(0.f, 0.f, 0.f)};
-    bool deferred = false;
-    walk_seq(P, S, i, pa[i], pf, cs, ce, vis, false, &deferred);
-    gx_mod[i] = make_float4(gx.x + vis.gpi.x, gx.y + vis.gpi.y, gx.z + vis.gpi.z, 0.f);
-    const float k = 1.0f - ci * vis.sumw;
-    gv_u[i] = make_float4(g.x * k, g.y * k, g.z * k, 0.f);
-}
-
-// Vorticity confinement backward (Density.h:179-221), before the viscosity's own terms are
-// taken up.  The frame's force f_i = e (n_i x omega_i) acts in the next frame's applyForces
-// (v* = v + dt (g + f), not on solids), so dL/df_i = dt dL/dv_i of the next frame's input, which
-// the next frame's reverse pass left in gv_out.  With eta_i = sum_j |omega_j - omega_i| /
-// (p_j - p_i + 1e-8) (componentwise, every list entry) and n = (eta + 1e-8) / (|eta| + 1e-8):
+// Vorticity confinement backward (Density.h:179-221).  The frame's force f_i = e (n_i x omega_i)
+// acts in the next frame's applyForces (v* = v + dt (g + f), not on solids), so dL/df_i = dt
+// dL/dv_i of the next frame's input, which the next frame's reverse pass left in gv_out.  With
+// eta_i = sum_j |omega_j - omega_i| / (p_j - p_i + 1e-8) (componentwise, every list entry; the
+// taped frame kept it) and n = (eta + 1e-8) / (|eta| + 1e-8):
 //   nbar = e omega_i x fbar,  omegabar_i = e fbar x n,
 //   etabar = nbar / (|eta| + 1e-8) - eta ((eta + 1e-8) . nbar) / ((|eta| + 1e-8)^2 |eta|),
 // and per entry, with D = p_j - p_i + 1e-8, u = omega_j - omega_i, l = |u|:
 //   omegabar_j += (sum_a etabar_a / D_a) u / l (omegabar_i the opposite),
 //   pbar_j,a -= etabar_a l / D_a^2 (pbar_i,a the opposite).
-// Two walks of the frame's list (the anchors' cells at the final positions): eta, then the
-// terms.  Own terms: pbar into gx, omegabar into gom; partners' terms to scat_om and scat_p.
-struct AdjEtaVisit {   // eta_i, as the forward sums it
-    struct Contrib { int dummy; };
-    using Extra = float4;   // omega_j
-    const float4* __restrict__ om;
-    float4 pi, oi;
-    float ex = 0.f, ey = 0.f, ez = 0.f;
-    __device__ __forceinline__ void end_contacts(uint32_t) {}
-    __device__ static Contrib zero() { return Contrib{0}; }
-    __device__ static bool effective(const Contrib&) { return false; }
-    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
-    __device__ __forceinline__ float4 fetch(uint32_t j) const { return __ldg(om + j); }
-    __device__ __forceinline__ Contrib contrib(uint32_t, const float4& pj, const float4& oj, bool) {
-        const float dx = oj.x - oi.x, dy = oj.y - oi.y, dz = oj.z - oi.z;
-        const float ol = sqrtf(dist2(dx, dy, dz));
-        ex += __fdividef(ol, (pj.x - pi.x) + 0.00000001f);
-        ey += __fdividef(ol, (pj.y - pi.y) + 0.00000001f);
-        ez += __fdividef(ol, (pj.z - pi.z) + 0.00000001f);
-        return zero();
-    }
-    __device__ __forceinline__ void add(const Contrib&, bool) {}
-};
 struct AdjVortVisit {   // the entries' terms for etabar
     struct Contrib { int dummy; };
     using Extra = float4;   // omega_j
@@ -262,34 +217,80 @@ struct AdjVortVisit {   // the entries' terms for etabar
     __device__ __forceinline__ void add(const Contrib&, bool) {}
 };
 
+// Both per-entry visitors in one walk, each with its own neighbour data.
+template <class A, class B>
+struct BothVisit {
+    struct Contrib { int dummy; };
+    struct Extra { typename ExtraOf<A>::type a; typename ExtraOf<B>::type b; };
+    A& va;
+    B& vb;
+    __device__ __forceinline__ void end_contacts(uint32_t n) { va.end_contacts(n); vb.end_contacts(n); }
+    __device__ static Contrib zero() { return Contrib{0}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ Extra fetch(uint32_t j) const { return Extra{fetch_extra(va, j), fetch_extra(vb, j)}; }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, const Extra& ex, bool contact) {
+        contrib_of(va, j, pj, ex.a, contact);
+        contrib_of(vb, j, pj, ex.b, contact);
+        return zero();
+    }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
+};
+
+// The reverse of the passes after updatePositions, the viscosity's and the vorticity force's
+// terms in one walk of the frame's list (the anchors' cells at the final positions):
+//   gx = dL/dx' + their own dL/dp terms, gv_u = dL/dv before the viscosity (own terms),
+//   gom = each particle's own dL/domega (vorticity);
+// the partners' terms go to scat_p, scat_v and scat_om.  omega's own reverse runs after it.
 __global__ void __launch_bounds__(128)
-adj_vort_kernel(DevParams P, const float4* __restrict__ pf, const float4* __restrict__ pa, const float4* __restrict__ om,
-                const float4* __restrict__ gv_out, const float* __restrict__ w, float4* __restrict__ gx,
-                float4* __restrict__ gom, unsigned long long* __restrict__ scat_om, unsigned long long* __restrict__ scat_p,
-                const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax) {
+adj_visc_vort_kernel(DevParams P, const float4* __restrict__ pf, const float4* __restrict__ pa,
+                     const float4* __restrict__ vu, const float4* __restrict__ om, const float4* __restrict__ eta,
+                     const float4* __restrict__ gx_out, const float4* __restrict__ gv_out, const float* __restrict__ w,
+                     float4* __restrict__ gx, float4* __restrict__ gv_u, float4* __restrict__ gom,
+                     unsigned long long* __restrict__ scat_p, unsigned long long* __restrict__ scat_v,
+                     unsigned long long* __restrict__ scat_om, const uint32_t* __restrict__ cs,
+                     const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax, int do_visc, int do_vort) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
-    const float4 g = gv_out[i];
-    const float k = (w && w[i] == 0.0f) ? 0.0f : P.dt;   // solids take no force
-    const float3 fb = make_float3(g.x * k, g.y * k, g.z * k);
-    if (fb.x == 0.0f && fb.y == 0.0f && fb.z == 0.0f) { gom[i] = make_float4(0.f, 0.f, 0.f, 0.f); return; }
     const SceneCtx S = scene_ctx(P, i);
-    const float4 oi = om[i], pi = pf[i], ai = pa[i];
+    const float fix = fix_scale(gmax).sc;
+    const float4 g = gv_out[i], x0 = gx_out[i], pi = pf[i];
+    // viscosity: v'' = v' + c w_i sum_j (v'_j - v'_i) W_ij
+    const float ci = w ? w[i] * P.c_visc : P.c_visc;   // a solid's coefficient is 0
+    AdjViscVisit vis{P, vu, pi, vu[i], make_float3(g.x, g.y, g.z), ci, scat_p, scat_v, fix, 0.f,
+                     make_float3(0.f, 0.f, 0.f)};
+    // vorticity: dL/df = dt dL/dv of the next frame (zero for the last frame and for solids)
+    const float k = (w && w[i] == 0.0f) ? 0.0f : P.dt;
+    const float3 fb = make_float3(g.x * k, g.y * k, g.z * k);
+    const bool vort = do_vort && (fb.x != 0.0f || fb.y != 0.0f || fb.z != 0.0f);
+    float3 ob = make_float3(0.f, 0.f, 0.f), eb = ob;
+    float4 oi = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (vort) {
+        oi = om[i];
+        const float4 et = eta[i];
+        const float e = P.e_vort, EPS = 0.00000001f;
+        const float gl = sqrtf(et.x * et.x + et.y * et.y + et.z * et.z), ge = gl + EPS;
+        const float3 nv = make_float3((et.x + EPS) / ge, (et.y + EPS) / ge, (et.z + EPS) / ge);
+        const float3 nb = make_float3(e * (oi.y * fb.z - oi.z * fb.y), e * (oi.z * fb.x - oi.x * fb.z),
+                                      e * (oi.x * fb.y - oi.y * fb.x));
+        ob = make_float3(e * (fb.y * nv.z - fb.z * nv.y), e * (fb.z * nv.x - fb.x * nv.z), e * (fb.x * nv.y - fb.y * nv.x));
+        const float c2 = gl > 0.0f ? ((et.x + EPS) * nb.x + (et.y + EPS) * nb.y + (et.z + EPS) * nb.z) / (ge * ge * gl) : 0.0f;
+        eb = make_float3(nb.x / ge - et.x * c2, nb.y / ge - et.y * c2, nb.z / ge - et.z * c2);
+    }
+    AdjVortVisit vv{om, pi, oi, eb, scat_om, scat_p, fix};
     bool deferred = false;
-    AdjEtaVisit ev{om, pi, oi};
-    walk_seq(P, S, i, ai, pf, cs, ce, ev, false, &deferred);
-    const float e = P.e_vort, EPS = 0.00000001f;
-    const float gl = sqrtf(ev.ex * ev.ex + ev.ey * ev.ey + ev.ez * ev.ez), ge = gl + EPS;
-    const float3 nv = make_float3((ev.ex + EPS) / ge, (ev.ey + EPS) / ge, (ev.ez + EPS) / ge);
-    const float3 nb = make_float3(e * (oi.y * fb.z - oi.z * fb.y), e * (oi.z * fb.x - oi.x * fb.z), e * (oi.x * fb.y - oi.y * fb.x));
-    const float3 ob = make_float3(e * (fb.y * nv.z - fb.z * nv.y), e * (fb.z * nv.x - fb.x * nv.z), e * (fb.x * nv.y - fb.y * nv.x));
-    const float c2 = gl > 0.0f ? ((ev.ex + EPS) * nb.x + (ev.ey + EPS) * nb.y + (ev.ez + EPS) * nb.z) / (ge * ge * gl) : 0.0f;
-    const float3 eb = make_float3(nb.x / ge - ev.ex * c2, nb.y / ge - ev.ey * c2, nb.z / ge - ev.ez * c2);
-    AdjVortVisit vv{om, pi, oi, eb, scat_om, scat_p, fix_scale(gmax).sc};
-    walk_seq(P, S, i, ai, pf, cs, ce, vv, false, &deferred);
-    gom[i] = make_float4(ob.x + vv.obi.x, ob.y + vv.obi.y, ob.z + vv.obi.z, 0.f);
-    const float4 x0 = gx[i];
-    gx[i] = make_float4(x0.x + vv.pbi.x, x0.y + vv.pbi.y, x0.z + vv.pbi.z, 0.f);
+    if (do_visc && vort) {
+        BothVisit<AdjViscVisit, AdjVortVisit> both{vis, vv};
+        walk_seq(P, S, i, pa[i], pf, cs, ce, both, false, &deferred);
+    } else if (do_visc) {
+        walk_seq(P, S, i, pa[i], pf, cs, ce, vis, false, &deferred);
+    } else if (vort) {
+        walk_seq(P, S, i, pa[i], pf, cs, ce, vv, false, &deferred);
+    }
+    gx[i] = make_float4(x0.x + vis.gpi.x + vv.pbi.x, x0.y + vis.gpi.y + vv.pbi.y, x0.z + vis.gpi.z + vv.pbi.z, 0.f);
+    const float kv = do_visc ? 1.0f - ci * vis.sumw : 1.0f;
+    gv_u[i] = make_float4(g.x * kv, g.y * kv, g.z * kv, 0.f);
+    if (do_vort) gom[i] = make_float4(ob.x + vv.obi.x, ob.y + vv.obi.y, ob.z + vv.obi.z, 0.f);
 }
 
 // computeOmega backward (Density.h:232-269): omega_i = sum_j (v_j - v_i) x G_ij, G = g(|r|) rhat,

@@ -60,6 +60,9 @@ struct DevParams {
     const SceneParams* scenes;
     uint32_t* scene_of;
     uint32_t* scene_range;
+    // an adjoint's taped frame: the vorticity pass also stores each particle's eta (its
+    // sum_j |omega_j - omega_i| / (p_j - p_i + 1e-8)) here; null in every other frame
+    float4* eta_tape;
 };
 
 // The scene a particle belongs to, as the walk and the per-scene constants see it.

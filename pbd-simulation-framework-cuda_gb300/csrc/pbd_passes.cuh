@@ -1197,6 +1197,7 @@ __device__ __forceinline__ void vort_visc_finish(const DevParams& P, uint32_t i,
                                                  float4* __restrict__ vout, float4* __restrict__ fext,
                                                  const float* __restrict__ w, float4* __restrict__ vhost = nullptr) {
     if (vo.vort) {
+        if (P.eta_tape) P.eta_tape[i] = make_float4(vo.gx, vo.gy, vo.gz, 0.f);
         const float EPS = 0.00000001f;
         const float gl = sqrtf(__fmaf_rn(vo.gz, vo.gz, __fmaf_rn(vo.gy, vo.gy, __fmul_rn(vo.gx, vo.gx))));
         const float inv = 1.0f / __fadd_rn(gl, EPS);

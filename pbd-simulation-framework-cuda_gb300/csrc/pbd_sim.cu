@@ -91,8 +91,9 @@ struct Tape {
     float4* p_fin;                 // with viscosity: the frame's final positions and the
     float4* v_u;                   // velocities before the viscosity pass (sorted order)
     float* w;                      // with solids: the inverse masses (sorted order)
-    float4* omega;                 // with vorticity: the frame's omega (sorted order) and the
-    float4* fext;                  // external force its applyForces took (pre-sort order)
+    float4* omega;                 // with vorticity: the frame's omega and eta (sorted order) and
+    float4* eta;
+    float4* fext;                  // the external force its applyForces took (pre-sort order)
 };
 
 struct pbd_sim {
@@ -281,6 +282,7 @@ DevParams make_dev_params(const pbd_sim* s) {
     P.scenes = s->d_scenes;
     P.scene_of = s->scene_of;
     P.scene_range = s->scene_range;
+    P.eta_tape = nullptr;
     const float c = std::max(P.hp, std::max(P.hs, P.d));
     P.cut2 = c * c * 1.0001f;
     return P;
@@ -364,7 +366,8 @@ static void launch_delta_list(uint32_t gn, int tn, cudaStream_t st, const DevPar
 // paths copy them at the end of the frame).
 cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only, uint32_t& nl,
                           Profiler* prof = nullptr, const Tape* tape = nullptr, bool readback = false) {
-    const DevParams P = make_dev_params(s);
+    DevParams P = make_dev_params(s);
+    if (tape) P.eta_tape = tape->eta;   // a taped frame keeps the vorticity pass's eta
     const pbd_params& prm = s->prm;
     const uint32_t N = s->N;
     const int np = sort_passes(s);
@@ -1590,8 +1593,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     const bool visc = (s->prm.active & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     const bool solids = s->mass_used != 0;
     const bool vort = (s->prm.active & PBD_ACTIVE_COMPUTE_VORTICITY) != 0;
-    const size_t per_tape = N * (16 + 16 + 4 + 4 + ((visc || vort) ? 32 : 0) + (solids ? 4 : 0) + (vort ? 32 : 0)) +
-                            (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 1280;
+    const size_t per_tape = N * (16 + 16 + 4 + 4 + ((visc || vort) ? 32 : 0) + (solids ? 4 : 0) + (vort ? 48 : 0)) +
+                            (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 1536;
     const size_t acc_bytes = 16 * (size_t)div_up((uint32_t)N, 128);   // two doubles per reverse block
     const size_t w_bytes = solids ? ((size_t)nck + 1) * N * 4 + 512 : 0;   // checkpoints + final
     const size_t vort_bytes = vort ? N * 48 + ((size_t)nck + 1) * N * 16 + 1024 : 0;   // scat3, gom, force checkpoints
@@ -1637,6 +1640,7 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
         T.v_u = (visc || vort) ? (float4*)take(N * 16) : nullptr;
         T.w = solids ? (float*)take(N * 4) : nullptr;
         T.omega = vort ? (float4*)take(N * 16) : nullptr;
+        T.eta = vort ? (float4*)take(N * 16) : nullptr;
         T.fext = vort ? (float4*)take(N * 16) : nullptr;
     }
     for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
@@ -1725,20 +1729,15 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
         adj_gmax_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, s->adj_gmax);
         if (T.p_fin) {
             // the passes after updatePositions, last first, into gx (dL/dp final) and gp2 (dL/dv
-            // before the viscosity): the viscosity's own terms, then vorticity's and omega's
-            if (visc_on) {
-                adj_visc_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, gx_out, gv_out, gx, gp2, s->adj_scat,
-                                                    s->adj_scat2, s->cell_start, s->cell_end, s->adj_gmax, T.w);
-            } else {
-                cudaMemcpyAsync(gx, gx_out, (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
-                cudaMemcpyAsync(gp2, gv_out, (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
-            }
-            if (T.omega) {   // dL/df of this frame's force is in gv_out (the next frame's dL/dv)
-                adj_vort_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.omega, gv_out, T.w, gx, s->adj_gom,
-                                                    s->adj_scat3, s->adj_scat, s->cell_start, s->cell_end, s->adj_gmax);
+            // before the viscosity): the viscosity's and the vorticity force's terms in one walk,
+            // then omega's (dL/df of this frame's force is in gv_out, the next frame's dL/dv)
+            adj_visc_vort_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, T.omega, T.eta, gx_out, gv_out, T.w, gx,
+                                                     gp2, s->adj_gom, s->adj_scat, s->adj_scat2, s->adj_scat3,
+                                                     s->cell_start, s->cell_end, s->adj_gmax, visc_on ? 1 : 0,
+                                                     T.omega ? 1 : 0);
+            if (T.omega)
                 adj_omega_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, s->adj_gom, s->adj_scat3, gx, gp2,
                                                      s->adj_scat2, s->adj_scat, s->cell_start, s->cell_end, s->adj_gmax);
-            }
             adj_update_visc_kernel<<<ge, 256, 0, st>>>(P, gx, gp2, gp, s->adj_scat, s->adj_scat2, s->adj_gmax);
         } else {
             adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
