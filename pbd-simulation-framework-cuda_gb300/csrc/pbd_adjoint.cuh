@@ -217,6 +217,21 @@ struct AdjVortVisit {   // the entries' terms for etabar
     __device__ __forceinline__ void add(const Contrib&, bool) {}
 };
 
+// Particle i's entries of the frame's list: from the full list the taped forward recorded (meta
+// fm), or from the anchors' cells when it has none for i (a list longer than its slots, a walk
+// that met a long cell range, or no list recorded).  The same entries either way.
+template <class V>
+__device__ __forceinline__ void walk_frame_list(const DevParams& P, const SceneCtx& S, uint32_t i, float4 anchor,
+                                                const float4* __restrict__ p, const uint32_t* __restrict__ cs,
+                                                const uint32_t* __restrict__ ce, const NbList& F, uint32_t fm, V& vis) {
+    if (fm != kListOff) {
+        walk_list(F, i, fm, p, vis);
+    } else {
+        bool deferred = false;
+        walk_seq(P, S, i, anchor, p, cs, ce, vis, false, &deferred);
+    }
+}
+
 // Both per-entry visitors in one walk, each with its own neighbour data.
 template <class A, class B>
 struct BothVisit {
@@ -249,7 +264,8 @@ adj_visc_vort_kernel(DevParams P, const float4* __restrict__ pf, const float4* _
                      float4* __restrict__ gx, float4* __restrict__ gv_u, float4* __restrict__ gom,
                      unsigned long long* __restrict__ scat_p, unsigned long long* __restrict__ scat_v,
                      unsigned long long* __restrict__ scat_om, const uint32_t* __restrict__ cs,
-                     const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax, int do_visc, int do_vort) {
+                     const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax, int do_visc, int do_vort,
+                     NbList Ft) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const SceneCtx S = scene_ctx(P, i);
@@ -278,14 +294,14 @@ adj_visc_vort_kernel(DevParams P, const float4* __restrict__ pf, const float4* _
         eb = make_float3(nb.x / ge - et.x * c2, nb.y / ge - et.y * c2, nb.z / ge - et.z * c2);
     }
     AdjVortVisit vv{om, pi, oi, eb, scat_om, scat_p, fix};
-    bool deferred = false;
+    const uint32_t fm = Ft.list ? Ft.meta[i] : kListOff;   // the taped full list, else the cells
     if (do_visc && vort) {
         BothVisit<AdjViscVisit, AdjVortVisit> both{vis, vv};
-        walk_seq(P, S, i, pa[i], pf, cs, ce, both, false, &deferred);
+        walk_frame_list(P, S, i, pa[i], pf, cs, ce, Ft, fm, both);
     } else if (do_visc) {
-        walk_seq(P, S, i, pa[i], pf, cs, ce, vis, false, &deferred);
+        walk_frame_list(P, S, i, pa[i], pf, cs, ce, Ft, fm, vis);
     } else if (vort) {
-        walk_seq(P, S, i, pa[i], pf, cs, ce, vv, false, &deferred);
+        walk_frame_list(P, S, i, pa[i], pf, cs, ce, Ft, fm, vv);
     }
     gx[i] = make_float4(x0.x + vis.gpi.x + vv.pbi.x, x0.y + vis.gpi.y + vv.pbi.y, x0.z + vis.gpi.z + vv.pbi.z, 0.f);
     const float kv = do_visc ? 1.0f - ci * vis.sumw : 1.0f;
@@ -341,7 +357,8 @@ __global__ void __launch_bounds__(128)
 adj_omega_kernel(DevParams P, const float4* __restrict__ pf, const float4* __restrict__ pa, const float4* __restrict__ vu,
                  const float4* __restrict__ gom, unsigned long long* __restrict__ scat_om, float4* __restrict__ gx,
                  float4* __restrict__ gv_u, unsigned long long* __restrict__ scat_v, unsigned long long* __restrict__ scat_p,
-                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax) {
+                 const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, const uint32_t* __restrict__ gmax,
+                 NbList Ft) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P.N) return;
     const FixScale fs = fix_scale(gmax);
@@ -350,8 +367,7 @@ adj_omega_kernel(DevParams P, const float4* __restrict__ pf, const float4* __res
     if (ob.x == 0.0f && ob.y == 0.0f && ob.z == 0.0f) return;
     const SceneCtx S = scene_ctx(P, i);
     AdjOmegaVisit vis{P, vu, pf[i], vu[i], ob, scat_v, scat_p, fs.sc};
-    bool deferred = false;
-    walk_seq(P, S, i, pa[i], pf, cs, ce, vis, false, &deferred);
+    walk_frame_list(P, S, i, pa[i], pf, cs, ce, Ft, Ft.list ? Ft.meta[i] : kListOff, vis);
     const float4 a = gx[i], b = gv_u[i];
     gx[i] = make_float4(a.x + vis.pbi.x, a.y + vis.pbi.y, a.z + vis.pbi.z, 0.f);
     gv_u[i] = make_float4(b.x + vis.vbi.x, b.y + vis.vbi.y, b.z + vis.vbi.z, 0.f);

@@ -94,6 +94,8 @@ struct Tape {
     float4* omega;                 // with vorticity: the frame's omega and eta (sorted order) and
     float4* eta;
     float4* fext;                  // the external force its applyForces took (pre-sort order)
+    uint32_t* full;                // with viscosity or vorticity: the frame's full list (recorded
+    uint32_t* full_meta;           // here instead of the simulation's buffer; stride N)
 };
 
 struct pbd_sim {
@@ -309,6 +311,13 @@ struct Profiler {
 #define PROF_BEGIN(name) do { if (prof) prof->begin(name); } while (0)
 #define PROF_END() do { if (prof) prof->end(); } while (0)
 
+// The frame's first lambda pass stores the full list (its walk of the anchor cells) for the
+// passes after it.
+static bool use_full_list(const pbd_sim* s) {
+    return !(s->prm.flags & PBD_FLAG_FULL_WALK) && (s->prm.active & PBD_ACTIVE_COMPUTE_LAMBDA) &&
+           s->prm.solver_iterations > 0;
+}
+
 // Near lists need kernels that vanish beyond the cut (far_pairs_zero), and they pay only when the
 // cut keeps a small part of the list: the cut's sphere against the cube of cells the list covers.
 // With kernel widths of a few cells (config.txt's 4.1 and 6.1 with kernelWidthNeighbours 2) the
@@ -445,8 +454,10 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
     const NbList L = Lf;
     const NbList L0{nullptr, nullptr, 0u, 0u};
     // full lists: stored by the first lambda pass of the frame (its walk of the anchor cells)
-    const bool use_full = !(prm.flags & PBD_FLAG_FULL_WALK) && (act & PBD_ACTIVE_COMPUTE_LAMBDA) && I > 0;
-    const NbList F = use_full ? NbList{s->fl_list, s->fl_meta, s->cap, s->fl_slots} : L0;
+    const bool use_full = use_full_list(s);
+    const NbList F = !use_full ? L0
+                     : (tape && tape->full) ? NbList{tape->full, tape->full_meta, N, s->fl_slots}
+                                            : NbList{s->fl_list, s->fl_meta, s->cap, s->fl_slots};
     // PBD_FLAG_STAGED_PASSES: the later lambda passes and the delta passes stage each block's
     // neighbourhood in shared memory (the full list stays the fallback); inverse masses are not
     // staged, so simulations with solids read the lists
@@ -1593,8 +1604,10 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     const bool visc = (s->prm.active & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
     const bool solids = s->mass_used != 0;
     const bool vort = (s->prm.active & PBD_ACTIVE_COMPUTE_VORTICITY) != 0;
+    const bool tape_full = visc || vort;   // the reverse passes after updatePositions read the frame's full list
     const size_t per_tape = N * (16 + 16 + 4 + 4 + ((visc || vort) ? 32 : 0) + (solids ? 4 : 0) + (vort ? 48 : 0)) +
-                            (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 1536;
+                            (tape_full ? N * (4 * (size_t)s->fl_slots + 4) : 0) +
+                            (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 2048;
     const size_t acc_bytes = 16 * (size_t)div_up((uint32_t)N, 128);   // two doubles per reverse block
     const size_t w_bytes = solids ? ((size_t)nck + 1) * N * 4 + 512 : 0;   // checkpoints + final
     const size_t vort_bytes = vort ? N * 48 + ((size_t)nck + 1) * N * 16 + 1024 : 0;   // scat3, gom, force checkpoints
@@ -1641,6 +1654,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
         T.w = solids ? (float*)take(N * 4) : nullptr;
         T.omega = vort ? (float4*)take(N * 16) : nullptr;
         T.eta = vort ? (float4*)take(N * 16) : nullptr;
+        T.full = tape_full ? (uint32_t*)take(N * 4 * (size_t)s->fl_slots) : nullptr;
+        T.full_meta = tape_full ? (uint32_t*)take(N * 4) : nullptr;
         T.fext = vort ? (float4*)take(N * 16) : nullptr;
     }
     for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
@@ -1731,13 +1746,17 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
             // the passes after updatePositions, last first, into gx (dL/dp final) and gp2 (dL/dv
             // before the viscosity): the viscosity's and the vorticity force's terms in one walk,
             // then omega's (dL/df of this frame's force is in gv_out, the next frame's dL/dv)
+            // the frame's full list as the forward recorded it into the tape (unset when the
+            // forward walked the cells: then the reverse walks them too)
+            const NbList Ft = (T.full && use_full_list(s)) ? NbList{T.full, T.full_meta, N, s->fl_slots}
+                                                           : NbList{nullptr, nullptr, 0u, 0u};
             adj_visc_vort_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, T.omega, T.eta, gx_out, gv_out, T.w, gx,
                                                      gp2, s->adj_gom, s->adj_scat, s->adj_scat2, s->adj_scat3,
                                                      s->cell_start, s->cell_end, s->adj_gmax, visc_on ? 1 : 0,
-                                                     T.omega ? 1 : 0);
+                                                     T.omega ? 1 : 0, Ft);
             if (T.omega)
                 adj_omega_kernel<<<gn, 128, 0, st>>>(P, T.p_fin, T.p_it[0], T.v_u, s->adj_gom, s->adj_scat3, gx, gp2,
-                                                     s->adj_scat2, s->adj_scat, s->cell_start, s->cell_end, s->adj_gmax);
+                                                     s->adj_scat2, s->adj_scat, s->cell_start, s->cell_end, s->adj_gmax, Ft);
             adj_update_visc_kernel<<<ge, 256, 0, st>>>(P, gx, gp2, gp, s->adj_scat, s->adj_scat2, s->adj_gmax);
         } else {
             adj_update_kernel<<<ge, 256, 0, st>>>(P, gx_out, gv_out, gp, gx);
