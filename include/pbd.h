@@ -146,7 +146,9 @@ int pbd_capacity(const pbd_sim* sim, uint32_t* cap);
 /* ---- particle injection (kernel/Communication.h:22-67, 626-660) ------------------- */
 /* addParticlesCallback: append n particles at index N from host arrays of n float4
  * (col may be NULL).  Rejected with PBD_ERR_CAPACITY when N + n > capacity (the reference
- * returns silently).  Synchronous with respect to the host arrays. */
+ * returns silently).  Synchronous with respect to the host arrays, except when they are the
+ * arrays pbd_step_readback returned (with col NULL): that copy is queued, and the library's
+ * next write into those arrays comes after it. */
 int pbd_add_particles(pbd_sim* sim, uint32_t n, const float* pos4, const float* vel4,
                       const float* col4);
 /* Same, with a per-particle inverse mass (unified solids).  The reference forces mass 1

@@ -986,7 +986,13 @@ static int add_common(pbd_sim* s, uint32_t n, const float* pos4, const float* ve
 int pbd_add_particles(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4) {
     clear_error();
     if (int rc = check_sim(s, "pbd_add_particles")) return rc;
-    return add_common(s, n, pos4, vel4, col4, nullptr, cudaMemcpyHostToDevice, s->last_stream, true);
+    // The library's own readback buffers (a host loop feeding pbd_step_readback's output back
+    // in): the next write into them is a later frame's readback, queued behind this copy on the
+    // same stream (pbd_step and pbd_step_readback first wait for the last stream when they run on
+    // another one), so the host need not wait for the copy here.
+    const bool own = s->rb_host && pos4 == reinterpret_cast<const float*>(s->rb_host) &&
+                     vel4 == reinterpret_cast<const float*>(s->rb_host + s->cap) && !col4;
+    return add_common(s, n, pos4, vel4, col4, nullptr, cudaMemcpyHostToDevice, s->last_stream, !own);
 }
 
 int pbd_add_particles_mass(pbd_sim* s, uint32_t n, const float* pos4, const float* vel4, const float* col4,
@@ -1042,6 +1048,7 @@ int pbd_step(pbd_sim* s, int nsteps, void* stream) {
     if (nsteps < 0) { set_error("pbd_step: nsteps < 0"); return PBD_ERR_INVALID_ARG; }
     if (s->N == 0 || nsteps == 0) return PBD_OK;   // Fluid.cu:19
     cudaStream_t st = (cudaStream_t)stream;
+    if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));   // work queued on another stream
     if (s->dirty || s->graph_n != s->N || s->table_passes != sort_passes(s)) {
         if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));
         if (int rc = settle_tables(s, st)) return rc;
@@ -1082,6 +1089,7 @@ int pbd_step_readback(pbd_sim* s, int nsteps, void* stream, const float** pos4, 
     }
     cudaStream_t st = (cudaStream_t)stream;
     if (s->N > 0) {
+        if (s->last_stream != st) CK(cudaStreamSynchronize(s->last_stream));   // work queued on another stream
         if (nsteps > 1)
             if (int rc = pbd_step(s, nsteps - 1, stream)) return rc;
         ++s->gen;

@@ -178,3 +178,32 @@ def test_step_readback_matches_step_and_get_state(need_gpu, pbd, scenes, vort, v
         assert np.array_equal(xa, sb["x"]) and np.array_equal(va, sb["v"])
     _same(a.state(), b.state())
     a.close(); b.close()
+
+
+def test_readback_arrays_fed_back_in(need_gpu, pbd, scenes):
+    """A host loop that feeds pbd_step_readback's own arrays back through pbd_clear +
+    pbd_add_particles (the copy is queued, not waited for) gives, frame by frame, the bits of a
+    loop that restarts from host copies of the same state with the synchronous path"""
+    params = scenes.workload_params(pbd, 32, 1000.0, vorticity=0.0005, viscosity=0.01)
+    params.lambda_epsilon = 0.1
+    pos, vel = scenes.lattice(20, 16, 20, spacing=0.9, seed=13)
+    n = len(pos)
+    a = pbd.Sim(params, n); a.add_particles(pos, vel)
+    b = pbd.Sim(params, n); b.add_particles(pos, vel)
+    L = pbd.lib()
+    rx, rv = pbd.C.POINTER(pbd.C.c_float)(), pbd.C.POINTER(pbd.C.c_float)()
+    pbd.check(L.pbd_step_readback(a.h, 1, None, pbd.C.byref(rx), pbd.C.byref(rv)))
+    b.step(1)
+    for _ in range(4):
+        pbd.check(L.pbd_clear(a.h))
+        pbd.check(L.pbd_add_particles(a.h, n, rx, rv, None))
+        pbd.check(L.pbd_step_readback(a.h, 1, None, pbd.C.byref(rx), pbd.C.byref(rv)))
+        sb = b.state()
+        b.clear()
+        b.add_particles(sb["x"], sb["v"])
+        b.step(1)
+        sb = b.state()
+        xa = np.ctypeslib.as_array(rx, shape=(n, 4))
+        va = np.ctypeslib.as_array(rv, shape=(n, 4))
+        assert np.array_equal(xa, sb["x"]) and np.array_equal(va, sb["v"])
+    a.close(); b.close()
