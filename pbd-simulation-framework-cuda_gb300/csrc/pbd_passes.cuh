@@ -775,7 +775,7 @@ lambda_coop_kernel(DevParams P, const float4* __restrict__ p, const float4* __re
 // The particles without a full list (the set C) are walked by the leading blocks; the ones left
 // without a near list are noted in DN for the delta pass.  Kept apart from lambda_kernel so that
 // its register budget is the list walk's alone.
-__global__ void __launch_bounds__(256, 6)
+__global__ void __launch_bounds__(256, 5)
 lambda_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
                    const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float* __restrict__ lambda,
                    CoopSet C, DeferList DN, float4* __restrict__ aux, NbList L, NbList F) {
@@ -962,8 +962,10 @@ __device__ __noinline__ void coop_delta(const DevParams& P, uint32_t mode, const
 // any delta pass over the frame's full list when there are no near lists (kB = kListBatch); the
 // particles without one (the set C) walk the cells.  kMode != 0: the pass
 // mode fixed at compile time (the two passes of a fluid frame), kMode = 0: `mode` at run time.
+// Blocks per SM by the list it walks (measured on GB300): 6 over the near lists (fluid_1m: 2%
+// faster than 5), 5 over the full lists of the density-active workload (6 was 15% slower).
 template <uint32_t kMode, uint32_t kB = kNearBatch>
-__global__ void __launch_bounds__(256, 5)
+__global__ void __launch_bounds__(256, kB == kNearBatch ? 6 : 5)
 delta_list_kernel(DevParams P, uint32_t mode_rt, const float4* __restrict__ pin, const float4* __restrict__ pa,
                   float4* __restrict__ pout, float4* __restrict__ x, float4* __restrict__ v,
                   const float* __restrict__ lambda, const float* __restrict__ w, float4* __restrict__ delta,
@@ -1267,7 +1269,11 @@ __device__ __noinline__ void coop_vort_visc(const DevParams& P, const float4* __
 // terms and the omega pass's near list Ln at hand, vorticity runs over the full list and
 // viscosity over the near list (its entries beyond the cut add exact zeros): the two sums keep
 // their own order.
-__global__ void __launch_bounds__(256, 5)
+// kNear: viscosity over omega's near list (the fluid workloads: 6 blocks per SM, 6.6% faster
+// than 5 on fluid_1m); else both terms over the full list (the density-active workload's ~125
+// entries: 5 blocks per SM, 6 was 36% slower).
+template <bool kNear>
+__global__ void __launch_bounds__(256, kNear ? 6 : 5)
 vort_visc_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
                       const float4* __restrict__ vin, float4* __restrict__ vout, const float4* __restrict__ omega,
                       float4* __restrict__ fext, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,

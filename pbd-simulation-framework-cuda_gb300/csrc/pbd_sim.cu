@@ -656,7 +656,12 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         PROF_BEGIN(Lv.list ? "vort_visc_list" : "vort_visc");
         if (Lv.list) {
             float4* const vh = (readback && visc) ? s->rb_dev + s->cap : nullptr;
-            vort_visc_list_kernel<<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
+            if (Ln.list)
+                vort_visc_list_kernel<true><<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
+                                                                   s->fext, s->cell_start, s->cell_end, vort, visc, wf,
+                                                                   vfull ? CF : CN, Lv, Ln, vh);
+            else
+                vort_visc_list_kernel<false><<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->v[cur.v ^ 1], s->omega,
                                                                    s->fext, s->cell_start, s->cell_end, vort, visc, wf,
                                                                    vfull ? CF : CN, Lv, Ln, vh);
             v_read = v_read || vh != nullptr;
