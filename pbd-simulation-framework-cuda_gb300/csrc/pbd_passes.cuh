@@ -1090,7 +1090,11 @@ __device__ __noinline__ void coop_omega(const DevParams& P, const float4* __rest
 // omega over the full list (recording the near list when L.list, and noting the particles left
 // without one in DN when DN is given); the particles without a full list (the set C) are walked
 // by the leading blocks.
-__global__ void __launch_bounds__(256, 6)
+// kNear: the pass filters the full list into omega's near list (the fluid workloads: 5 blocks
+// per SM, 2.5% faster than 6 on fluid_1m); else it walks the full list (the density-active
+// workload: 6, 5 was 3.8% slower).
+template <bool kNear>
+__global__ void __launch_bounds__(256, kNear ? 5 : 6)
 omega_list_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa, const float4* __restrict__ v,
                   const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, float4* __restrict__ omega,
                   CoopSet C, DeferList DN, NbList L, NbList F) {

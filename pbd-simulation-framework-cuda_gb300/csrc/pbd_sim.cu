@@ -636,7 +636,11 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
         // viscosity alone walks them: the particles left without one go to its cooperative blocks
         const DeferList DNo = (Lo.list && !vort) ? DN : DX;
         if (use_full) {
-            omega_list_kernel<<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end,
+            if (Lo.list)
+                omega_list_kernel<true><<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end,
+                                                               s->omega, CF, DNo, Lo, F);
+            else
+                omega_list_kernel<false><<<gn + kCoopBlocks, tn, 0, st>>>(P, s->p[cur.p], pa, s->v[cur.v], s->cell_start, s->cell_end,
                                                                s->omega, CF, DNo, Lo, F);
             nl += 1;
         } else {
