@@ -2,7 +2,7 @@
 
 Only tests/ and bench.py's checks import this module; the shipped library never does.  It
 restates, for the adjoint's supported configuration (applyForces, the density solve with
-stabilizationIterations = 1, solveCollisions, updatePositions, XSPH viscosity; no vorticity,
+stabilizationIterations S, solveCollisions, updatePositions, XSPH viscosity, vorticity,
 enclosurePositionDamping = 0, unit cell width, the cell-end quirk off), the frame that
 Fluid::compute runs (src/app/simulation/Fluid.cu:14-97):
 
@@ -54,7 +54,10 @@ class Consts:
         self.bmax = np.array([prm.bounds_max[a] for a in range(3)], np.float64)
         self.iters = int(prm.solver_iterations)
         self.M = int(prm.max_neighbours_per_particle)
-        self.collide = prm.collision_type == 0
+        # solveCollisions runs S times per iteration (Fluid.cu:60-65), each on the positions the
+        # pass before left; the density correction is applied after the last
+        self.stab = int(prm.stabilization_iterations)
+        self.collide = prm.collision_type == 0 and self.stab > 0
         self.poly_inv_den = 1.0 / (0.001 + 64.0 * PI * self.hp ** 9)
         self.spiky_k = 15.0 / (PI * self.hs ** 6)
         q = self.hs * float(prm.q_scorr)
@@ -207,13 +210,19 @@ def frame(C, x, v, f=None, tape=None):
         delta = _sum(I, (coef * q["g"])[:, None] * rh, n) / C.rho0
         if C.w is not None:
             delta = C.w[:, None] * delta
-        c = np.zeros_like(p)
-        if C.collide:
+        if tape is not None:
+            tape[-1].setdefault("ps", []).append([])
+        for k in range(C.stab if C.collide else 0):
+            if k > 0:   # a later pass: the contacts at the positions the pass before left
+                if tape is not None:
+                    tape[-1]["ps"][-1].append(p.copy())
+                I, J, r, L, rh = _pair_geometry(C, p, I0, J0)
             ov = C.d - L
             cm = (ov > 0.0) & (L > 0.00001)
             c = _sum(I[cm], (C.share(I[cm], J[cm]) * ov[cm])[:, None] * rh[cm], n)
-        p = p + c - delta
-        x = x + c
+            p = p + c
+            x = x + c
+        p = p - delta
     v = (p - x) / C.dt
     if tape is not None and (C.cvisc or C.evort):
         tape[-1]["pf"], tape[-1]["vu"] = p.copy(), v.copy()
@@ -293,6 +302,18 @@ def frame_backward(C, rec, gxo, gvo, acc, gf=None):
     gp = gxo + gvo / C.dt
     gx = -gvo / C.dt
     for it in range(C.iters - 1, -1, -1):
+        # the contact passes after the first, last first: gc = dL/dp entering each (the density
+        # correction, applied after the last pass, keeps the iteration's final gradient gp)
+        gc = gp
+        for pk in reversed(rec["ps"][it] if C.collide else []):
+            I, J, r, L, rh = _pair_geometry(C, pk, I0, J0)
+            cbar = (gc + gx)[I]
+            ov = C.d - L
+            cm = ((ov > 0.0) & (L > 0.00001)).astype(np.float64)
+            rc = np.einsum("ij,ij->i", rh, cbar)
+            ol = ov / L
+            rb = (C.share(I, J) * cm)[:, None] * (-rc[:, None] * rh + ol[:, None] * (cbar - rc[:, None] * rh))
+            gc = gc + _sum(I, rb, n) - _sum(J, rb, n)
         p = rec["p"][it]
         I, J, r, L, rh = _pair_geometry(C, p, I0, J0)
         lam, q = _lambda(C, n, I, L, rh)
@@ -308,7 +329,7 @@ def frame_backward(C, rec, gxo, gvo, acc, gf=None):
         glam = _sum(I, gd, n) + _sum(J, gd, n)
         rbar = coef[:, None] * _hess_mul(g, dg, L, rh, a[I]) + (gd * dsc)[:, None] * rh
         if C.collide:
-            cbar = (gp + gx)[I]
+            cbar = (gc + gx)[I]
             ov = C.d - L
             cm = ((ov > 0.0) & (L > 0.00001)).astype(np.float64)
             rc = np.einsum("ij,ij->i", rh, cbar)
@@ -317,7 +338,7 @@ def frame_backward(C, rec, gxo, gvo, acc, gf=None):
         sdelta = _sum(I, coef[:, None] * G, n)
         wgp = gp if C.w is None else C.w[:, None] * gp
         acc[0] += float(np.sum(wgp * sdelta)) / (C.rho0 * C.rho0)
-        gnew = gp + _sum(I, rbar, n) - _sum(J, rbar, n)
+        gnew = gc + _sum(I, rbar, n) - _sum(J, rbar, n)
         # lambda
         Cbar = -glam / q["D"]
         Dbar = glam * q["C"] / q["D"] ** 2

@@ -479,7 +479,8 @@ adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
                  const float4* __restrict__ gp_in, const float4* __restrict__ gx, float4* __restrict__ gp_out,
                  float* __restrict__ glam, unsigned long long* __restrict__ scat, unsigned long long* __restrict__ scat_in,
                  const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce, double* acc, bool collide,
-                 NbList Lt, const uint32_t* __restrict__ gmax, const float* __restrict__ w) {
+                 NbList Lt, const uint32_t* __restrict__ gmax, const float* __restrict__ w,
+                 const float4* __restrict__ gfin) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     double drho = 0.0;
     if (i < P.N) {
@@ -487,10 +488,13 @@ adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
         const FixScale fs = fix_scale(gmax);
         const float4 g0 = gp_in[i], t = take_scattered(scat_in, i, fs.inv), gxi = gx[i];   // + the pass after's partners
         const float4 gpin = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
+        // the density correction is applied after the iteration's last contact pass: its terms take
+        // the iteration's final gradient (gfin, with later contact passes), else this pass's
+        const float4 gd = gfin ? gfin[i] : gpin;
         const float wi = w ? w[i] : 1.0f;
         const float inv = 1.0f / S.rho0, winv = wi * inv;
         AdjDeltaVisit vis{P, lambda, w, wi, p[i], lambda[i],
-                          make_float3(-gpin.x * winv, -gpin.y * winv, -gpin.z * winv),
+                          make_float3(-gd.x * winv, -gd.y * winv, -gd.z * winv),
                           make_float3(gpin.x + gxi.x, gpin.y + gxi.y, gpin.z + gxi.z), scat, fs.sc,
                           make_float3(0.f, 0.f, 0.f), make_float3(0.f, 0.f, 0.f), 0.f, collide};
         // the forward's near list of this iteration (the pairs within the cut), else the cells
@@ -502,10 +506,73 @@ adj_delta_kernel(DevParams P, const float4* __restrict__ p, const float4* __rest
         gp_out[i] = make_float4(gpin.x + vis.gpi.x, gpin.y + vis.gpi.y, gpin.z + vis.gpi.z, 0.f);
         glam[i] = vis.glami;
         // Delta_i = sdelta / rho0 (applied as w_i Delta_i): d/drho0 = -w_i sdelta / rho0^2, Delta-bar = -w_i gp_in
-        drho = (double)(gpin.x * vis.sdelta.x + gpin.y * vis.sdelta.y + gpin.z * vis.sdelta.z) * (double)(inv * inv) *
+        drho = (double)(gd.x * vis.sdelta.x + gd.y * vis.sdelta.y + gd.z * vis.sdelta.z) * (double)(inv * inv) *
                (double)wi;
     }
     block_add2(drho, 0.0, acc);
+}
+
+// A contact pass after the iteration's first (stabilizationIterations > 1; Collision.h:171-242 run
+// again on the positions the pass before left): p' = p + c(p), x' = x + c(p).  gp_out = gp_in
+// (own + the pass after's partners) + the contacts' own J^T terms, the partners' to scat;
+// gd_out, when given, keeps the complete gp_in (the iteration's final gradient).
+struct AdjCollideVisit {
+    struct Contrib { int dummy; };
+    const DevParams& P;
+    const float* __restrict__ w;
+    float wi;
+    float4 pi;
+    float3 cbar;       // dL/dc_i = gp_in + gx
+    unsigned long long* scat;
+    float fix;
+    float3 gpi = make_float3(0.f, 0.f, 0.f);
+    __device__ __forceinline__ void end_contacts(uint32_t) {}
+    __device__ static Contrib zero() { return Contrib{0}; }
+    __device__ static bool effective(const Contrib&) { return false; }
+    __device__ static Contrib shfl(const Contrib& c, int) { return c; }
+    __device__ __forceinline__ Contrib contrib(uint32_t j, const float4& pj, bool contact) {
+        if (!contact) return zero();
+        const float rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        const float r2 = dist2(rx, ry, rz);
+        if (r2 >= P.cut2 || r2 <= 0.0f) return zero();
+        const float L = sqrtf(r2);
+        const float overlap = P.d - L;
+        float share = 0.5f;
+        if (w) {
+            const float wj = __ldg(w + j);
+            share = (wi + wj) > 0.0f ? wi / (wi + wj) : 0.0f;
+        }
+        if (!(overlap > 0.0f && L > 0.00001f && share != 0.0f)) return zero();
+        const float3 rh = make_float3(rx / L, ry / L, rz / L);
+        const float ac = share * P.one_minus_stiffness;
+        const float rc = rh.x * cbar.x + rh.y * cbar.y + rh.z * cbar.z;
+        const float ol = overlap / L;
+        const float3 rb = make_float3(ac * (-rc * rh.x + ol * (cbar.x - rc * rh.x)), ac * (-rc * rh.y + ol * (cbar.y - rc * rh.y)),
+                                      ac * (-rc * rh.z + ol * (cbar.z - rc * rh.z)));
+        gpi.x += rb.x; gpi.y += rb.y; gpi.z += rb.z;
+        scatter_sub3(scat + 4 * (size_t)j, rb, fix);
+        return zero();
+    }
+    __device__ __forceinline__ void add(const Contrib&, bool) {}
+};
+
+__global__ void __launch_bounds__(128)
+adj_collide_kernel(DevParams P, const float4* __restrict__ p, const float4* __restrict__ pa,
+                   const float4* __restrict__ gp_in, const float4* __restrict__ gx, float4* __restrict__ gp_out,
+                   unsigned long long* __restrict__ scat_in, unsigned long long* __restrict__ scat,
+                   float4* __restrict__ gd_out, const uint32_t* __restrict__ cs, const uint32_t* __restrict__ ce,
+                   const uint32_t* __restrict__ gmax, const float* __restrict__ w) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P.N) return;
+    const SceneCtx S = scene_ctx(P, i);
+    const FixScale fs = fix_scale(gmax);
+    const float4 g0 = gp_in[i], t = take_scattered(scat_in, i, fs.inv), gxi = gx[i];
+    const float4 g = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
+    if (gd_out) gd_out[i] = g;
+    AdjCollideVisit vis{P, w, w ? w[i] : 1.0f, p[i], make_float3(g.x + gxi.x, g.y + gxi.y, g.z + gxi.z), scat, fs.sc};
+    bool deferred = false;
+    walk_seq(P, S, i, pa[i], p, cs, ce, vis, false, &deferred);
+    gp_out[i] = make_float4(g.x + vis.gpi.x, g.y + vis.gpi.y, g.z + vis.gpi.z, 0.f);
 }
 
 // lambda backward for one iteration: glam complete; adds J^T terms to gp_out, d/drho0, d/deps.

@@ -78,12 +78,14 @@ inline uint32_t div_up(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) /
 
 // What the adjoint keeps of one frame (device buffers of N entries each).
 constexpr int kMaxTapeIters = 16;
+constexpr int kMaxTapeStab = 8;   // stabilizationIterations the adjoint takes
 struct Tape {
     float4* x_in;                  // state before applyForces (pre-sort order)
     float4* v_in;
     uint32_t* perm;                // sort permutation of the frame
     uint32_t* keys;                // sorted keys (rebuild the frame's cell tables)
     float4* p_it[kMaxTapeIters];   // p* entering each solver iteration (sorted order)
+    float4* p_s[kMaxTapeIters][kMaxTapeStab];   // p* entering the iteration's contact passes 1..S-1
     float* lam[kMaxTapeIters];     // lambda of each iteration
     float4* aux[kMaxTapeIters];    // the lambda pass's sums (2N float4: rho, B, S)
     uint32_t* near[kMaxTapeIters];       // each iteration's near lists (kListMax x N, slot-major)
@@ -126,7 +128,7 @@ struct pbd_sim {
     float *adj_ck_w = nullptr, *adj_fin_w = nullptr;   // with solids: the inverse masses (permuted with the state)
     float4 *adj_ck_f = nullptr, *adj_fin_f = nullptr;  // with vorticity: the force the next frame applies
     std::vector<Tape> adj_tape;
-    float4 *adj_g[5]{};            // gradient buffers
+    float4 *adj_g[6]{};            // gradient buffers
     float* adj_glam = nullptr;
     unsigned long long* adj_scat3 = nullptr;  // with vorticity: partners' dL/domega terms, fixed point
     float4* adj_gom = nullptr;                // with vorticity: each particle's own dL/domega
@@ -577,6 +579,9 @@ cudaError_t enqueue_frame(pbd_sim* s, cudaStream_t st, Cur& cur, bool front_only
             }
             if ((mode & kDoDelta) && (!last || !do_apply)) mode |= kStoreDelta;
             if (mode == 0) continue;
+            // a taped frame keeps the positions a later contact pass starts from
+            if (taped && k >= 1 && k < (uint32_t)kMaxTapeStab && tape->p_s[it][k - 1])
+                cudaMemcpyAsync(tape->p_s[it][k - 1], s->p[cur.p], (size_t)N * 16, cudaMemcpyDeviceToDevice, st);
             const bool final_pass = last && (it + 1 == I);
             if (final_pass && do_update) mode |= kDoUpdate;
             const bool recorded = (act & PBD_ACTIVE_COMPUTE_LAMBDA) && (act & PBD_ACTIVE_COMPUTE_DELTA_POSITIONS);
@@ -1596,7 +1601,11 @@ static int adjoint_supported(const pbd_sim* s) {
         set_error("adjoint: vorticity needs computeOmegas (it would read a stale omega)");
         return PBD_ERR_UNSUPPORTED;
     }
-    if (p.stabilization_iterations != 1 || p.solver_iterations == 0 || p.solver_iterations > (uint32_t)kMaxTapeIters) { set_error("adjoint: stabilizationIterations must be 1 and solverIterations 1..16"); return PBD_ERR_UNSUPPORTED; }
+    if (p.stabilization_iterations > (uint32_t)kMaxTapeStab || p.solver_iterations == 0 ||
+        p.solver_iterations > (uint32_t)kMaxTapeIters) {
+        set_error("adjoint: stabilizationIterations must be 0..8 and solverIterations 1..16");
+        return PBD_ERR_UNSUPPORTED;
+    }
     if (p.enclosure_position_damping != 0.0f) { set_error("adjoint: enclosurePositionDamping must be 0"); return PBD_ERR_UNSUPPORTED; }
     if (s->batched) { set_error("adjoint: batches have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
     if (p.collision_type != 0) { set_error("adjoint: collisionType 1 has no reverse pass"); return PBD_ERR_UNSUPPORTED; }
@@ -1622,13 +1631,17 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
     const bool solids = s->mass_used != 0;
     const bool vort = (s->prm.active & PBD_ACTIVE_COMPUTE_VORTICITY) != 0;
     const bool tape_full = visc || vort;   // the reverse passes after updatePositions read the frame's full list
+    const uint32_t S = s->prm.stabilization_iterations;
+    const bool stab_tape = s->prm.collision_type == 0 && S > 1;   // contact passes after the first
     const size_t per_tape = N * (16 + 16 + 4 + 4 + ((visc || vort) ? 32 : 0) + (solids ? 4 : 0) + (vort ? 48 : 0)) +
                             (tape_full ? N * (4 * (size_t)s->fl_slots + 4) : 0) +
-                            (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) + 2048;
+                            (size_t)I * N * (16 + 4 + 32 + 4 * kListMax + 4) +
+                            (stab_tape ? (size_t)I * (S - 1) * (N * 16 + 256) : 0) + 2048;
     const size_t acc_bytes = 16 * (size_t)div_up((uint32_t)N, 128);   // two doubles per reverse block
     const size_t w_bytes = solids ? ((size_t)nck + 1) * N * 4 + 512 : 0;   // checkpoints + final
-    const size_t vort_bytes = vort ? N * 48 + ((size_t)nck + 1) * N * 16 + 1024 : 0;   // scat3, gom, force checkpoints
-    const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 5 * N * 16 + N * 4 + acc_bytes + w_bytes + vort_bytes +
+    const size_t vort_bytes = (vort ? N * 48 + ((size_t)nck + 1) * N * 16 + 1024 : 0) +
+                              (stab_tape ? N * 32 + 256 : 0);   // scat3, gom, force checkpoints
+    const size_t need = (size_t)nck * N * 32 + N * 64 + N * 8 + (size_t)k * per_tape + 6 * N * 16 + N * 4 + acc_bytes + w_bytes + vort_bytes +
                         N * 64 + (size_t)(19 + (4 + 5 * I) * k) * 256;
     if (need > s->adj_bytes) {
         if (s->adj_arena) CK(cudaStreamSynchronize(st));
@@ -1660,6 +1673,8 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
         T.perm = (uint32_t*)take(N * 4);
         T.keys = (uint32_t*)take(N * 4);
         for (uint32_t it = 0; it < I; ++it) {
+            for (uint32_t k = 0; k + 1 < (uint32_t)kMaxTapeStab; ++k)
+                T.p_s[it][k] = (stab_tape && k + 1 < S) ? (float4*)take(N * 16) : nullptr;
             T.p_it[it] = (float4*)take(N * 16);
             T.lam[it] = (float*)take(N * 4);
             T.aux[it] = (float4*)take(N * 32);
@@ -1675,13 +1690,13 @@ int pbd_adjoint_forward(pbd_sim* s, int nsteps, int ckpt_every, void* stream) {
         T.full_meta = tape_full ? (uint32_t*)take(N * 4) : nullptr;
         T.fext = vort ? (float4*)take(N * 16) : nullptr;
     }
-    for (int g = 0; g < 5; ++g) s->adj_g[g] = (float4*)take(N * 16);
+    for (int g = 0; g < 6; ++g) s->adj_g[g] = (float4*)take(N * 16);
     s->adj_glam = (float*)take(N * 4);
     s->adj_acc = (double*)take(acc_bytes);
     s->adj_gmax = (uint32_t*)take(4);
     s->adj_scat = (unsigned long long*)take((size_t)N * 32);
     s->adj_scat2 = (unsigned long long*)take((size_t)N * 32);
-    s->adj_scat3 = vort ? (unsigned long long*)take((size_t)N * 32) : nullptr;
+    s->adj_scat3 = (vort || stab_tape) ? (unsigned long long*)take((size_t)N * 32) : nullptr;
     s->adj_gom = vort ? (float4*)take((size_t)N * 16) : nullptr;
     s->adj_steps = nsteps;
     s->adj_every = k;
@@ -1742,6 +1757,7 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
     const bool collide = s->prm.collision_type == 0;
     const uint32_t gn = div_up(N, 128), ge = div_up(N, 256);
     const bool visc_on = (s->prm.active & PBD_ACTIVE_COMPUTE_VISCOSITY) != 0;
+    const uint32_t nstab = collide ? s->prm.stabilization_iterations : 0u;   // contact passes per iteration
     float4 *gx_out = s->adj_g[0], *gv_out = s->adj_g[1], *gx = s->adj_g[2];
     if (recompute) {
         for (int t = 0; t < nf; ++t) {
@@ -1785,9 +1801,23 @@ static cudaError_t enqueue_segment(pbd_sim* s, cudaStream_t st, Cur& cur, int nf
             // each pass writes every particle's own terms and scatters the partners' in fixed point;
             // the next kernel adds a particle's scattered terms in one place: the same bits
             // whatever order the atomics landed in
+            // the contact passes after the first (stabilizationIterations > 1), last first, each at the
+            // positions it started from; the first of them also keeps the iteration's complete final
+            // gradient for the density correction's terms, applied after the last pass
+            unsigned long long* sin = s->adj_scat2;
+            const float4* gD = nullptr;
+            for (int k = (int)nstab - 1; k >= 1; --k) {
+                unsigned long long* sout = (sin == s->adj_scat2) ? s->adj_scat3 : s->adj_scat2;
+                float4* gd_out = (k == (int)nstab - 1) ? s->adj_g[5] : nullptr;
+                adj_collide_kernel<<<gn, 128, 0, st>>>(P, T.p_s[it][k - 1], pa, gp, gx, gp2, sin, sout, gd_out,
+                                                       s->cell_start, s->cell_end, s->adj_gmax, T.w);
+                std::swap(gp, gp2);
+                sin = sout;
+                if (gd_out) gD = gd_out;
+            }
             adj_delta_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.lam[it], gp, gx, gp2, s->adj_glam, s->adj_scat,
-                                                 s->adj_scat2, s->cell_start, s->cell_end, s->adj_acc, collide, Lt,
-                                                 s->adj_gmax, T.w);
+                                                 sin, s->cell_start, s->cell_end, s->adj_acc, collide && nstab > 0, Lt,
+                                                 s->adj_gmax, T.w, gD);
             adj_lambda_kernel<<<gn, 128, 0, st>>>(P, p, pa, T.aux[it], s->adj_glam, gp2, s->adj_scat2, s->adj_scat,
                                                   s->cell_start, s->cell_end, s->adj_acc, Lt, s->adj_gmax);
             std::swap(gp, gp2);

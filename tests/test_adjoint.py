@@ -397,3 +397,75 @@ def test_gpu_adjoint_segments_agree(need_gpu, pbd, scenes, solids):
     for gv, gx, gr, ge in runs[1:]:
         assert np.array_equal(gv, gv0) and np.array_equal(gx, gx0)
         assert gr == gr0 and ge == ge0
+
+
+@pytest.mark.parametrize("stab,frames", [(0, 4), (2, FRAMES), (3, FRAMES)])
+def test_restatement_stabilization_passes(pbd, scenes, oracle_mod, adj, stab, frames):
+    """stabilizationIterations S: solveCollisions S times per iteration, each on the positions the
+    pass before left, the density correction applied after the last (S = 0: no contacts).  The
+    FP64 restatement follows the C oracle's FP64 trajectory and its reverse pass matches central
+    differences (without contacts the dam break's particles pass through one another and the
+    gradients grow fast, hence 4 frames there)."""
+    prm, pos, vel, w = adjoint_scene(pbd, scenes, viscosity=0.01)
+    prm.stabilization_iterations = stab
+    C = adj.Consts(prm)
+    o = oracle_mod.Oracle(prm, len(pos), "f64")
+    o.add_particles(pos, vel)
+    x0, v0 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+    x, v, f = x0, v0, None
+    for _ in range(frames):
+        o.step(1)
+        x, v, f = adj.frame(C, x, v, f)
+    s = o.state()
+    order = np.argsort(s["ids"])
+    assert maxdiff(s["x"][order, :3], x) < 1e-8 and maxdiff(s["v"][order, :3], v) < 1e-6
+    gv, gx, gr, ge = adj.backward(C, x0, v0, frames, w)
+    loss = lambda c, xx, vv: float(np.sum(w * adj.rollout(c, xx, vv, frames)[0]))
+    dirn = np.random.default_rng(11).normal(size=x0.shape)
+    h = 1e-7
+    fd_v = (loss(C, x0, v0 + h * dirn) - loss(C, x0, v0 - h * dirn)) / (2 * h)
+    fd_x = (loss(C, x0 + h * dirn, v0) - loss(C, x0 - h * dirn, v0)) / (2 * h)
+    assert abs(fd_v - np.sum(gv * dirn)) <= 1e-4 * abs(fd_v), (fd_v, np.sum(gv * dirn))
+    assert abs(fd_x - np.sum(gx * dirn)) <= 1e-4 * abs(fd_x), (fd_x, np.sum(gx * dirn))
+    for attr, g in (("rho0", gr), ("eps", ge)):
+        base = getattr(C, attr)
+        hh = 1e-7 * base
+        cp, cm = copy.copy(C), copy.copy(C)
+        setattr(cp, attr, base + hh)
+        setattr(cm, attr, base - hh)
+        fd = (loss(cp, x0, v0) - loss(cm, x0, v0)) / (2 * hh)
+        assert abs(fd - g) <= 1e-4 * abs(fd), (attr, fd, g)
+
+
+def calm_scene(pbd, scenes, stab):
+    """A tight lattice (spacing 0.9, jitter 0.01) with slow random velocities (sigma 0.1): every
+    touching pair overlaps by ~0.1 and no pair comes near the contact distance within a few
+    frames, so no contact switches on or off between the FP32 and FP64 trajectories.  With the
+    wider jitter and faster particles of adjoint_scene, the FP64 gradients themselves move by
+    1e-3 to 2e-1 when the initial positions move by 1e-5 once there are several contact passes;
+    here by at most 7e-4 over 2 frames."""
+    prm = scenes.workload_params(pbd, 20, 1000.0, iterations=4, viscosity=0.01)
+    prm.lambda_epsilon = 0.1
+    prm.flags &= ~pbd.FLAG_CELL_END_QUIRK
+    prm.flags |= pbd.FLAG_TRACK_IDS
+    prm.stabilization_iterations = stab
+    pos, vel = scenes.lattice(12, 10, 12, spacing=0.9, jitter=0.01, seed=7)
+    rng = np.random.default_rng(7)
+    vel[:, :3] = rng.normal(0, 0.1, size=(len(vel), 3)).astype(np.float32)
+    return prm, pos, vel, rng.normal(size=(len(pos), 3))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("stab,frames", [(2, 1), (2, 2), (3, 2), (0, 2)])
+def test_gpu_adjoint_stabilization_passes(need_gpu, pbd, scenes, adj, stab, frames):
+    """stabilizationIterations 0, 2 and 3 (the positions each later contact pass starts from are
+    taped; the density correction's terms take the iteration's final gradient) against the FP64
+    reverse pass on a well-conditioned scene, within 2e-3"""
+    prm, pos, vel, w = calm_scene(pbd, scenes, stab)
+    C = adj.Consts(prm)
+    rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), frames, w)
+    _, fin, after, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, frames, 1)
+    assert _close_l2(gv, rv, 2e-3) and _close_l2(gx, rx, 2e-3)
+    assert abs(gr - rr) <= 2e-3 * abs(rr) and abs(ge - re) <= 2e-3 * abs(re), (gr, rr, ge, re)
+    for k in ("x", "v", "p", "ids"):
+        assert np.array_equal(fin[k], after[k]), k
