@@ -318,8 +318,8 @@ int pbd_render_sprites(pbd_sim* sim, const pbd_camera* camera, uint8_t* rgba, fl
  * and leaves the simulation as the forward left it; it may be called again for another loss on
  * the same forward.  Supported: the density solve, contacts, walls, integration, omega +
  * vorticity confinement (its force reaches the next frame), XSPH viscosity and unified solids
- * (pbd_add_particles_mass), stabilizationIterations 0..8; batches, collisionType 1, vorticity
- * without computeOmegas and enclosurePositionDamping != 0 return PBD_ERR_UNSUPPORTED. */
+ * (pbd_add_particles_mass), stabilizationIterations 0..8, enclosurePositionDamping; batches,
+ * collisionType 1 and vorticity without computeOmegas return PBD_ERR_UNSUPPORTED. */
 int pbd_adjoint_forward(pbd_sim* sim, int nsteps, int ckpt_every, void* stream);
 int pbd_adjoint_backward(pbd_sim* sim, const float* dL_dx_final, float* dL_dv0, float* dL_dx0,
                          double* dL_drest_density, double* dL_deps, void* stream);

@@ -52,6 +52,7 @@ class Consts:
         self.ac = 0.5 * (1.0 - float(prm.stiffness))
         self.bmin = np.array([prm.bounds_min[a] for a in range(3)], np.float64)
         self.bmax = np.array([prm.bounds_max[a] for a in range(3)], np.float64)
+        self.pd = float(prm.enclosure_position_damping)
         self.iters = int(prm.solver_iterations)
         self.M = int(prm.max_neighbours_per_particle)
         # solveCollisions runs S times per iteration (Fluid.cu:60-65), each on the positions the
@@ -166,6 +167,15 @@ def _predict(C, x, v, f=None):
     return p, ~(lo | hi)
 
 
+def _damp(C, x, p, mask):
+    """enclosurePositionDamping (Forces.h:56-58): a particle clamped on some axis has x moved
+    toward its clamped p by that fraction, on every axis; returns (x', any clamp)."""
+    anyc = ~np.all(mask, axis=1)
+    if not C.pd:
+        return x, anyc
+    return np.where(anyc[:, None], x + C.pd * (p - x), x), anyc
+
+
 def _omega(C, pf, vu, I0, J0):
     """omega_i = sum_j (v_j - v_i) x G_ij over the pairs within the cut (spiky is 0 beyond)."""
     n = len(pf)
@@ -195,11 +205,11 @@ def frame(C, x, v, f=None, tape=None):
     frame before (None: none); returns (x', v', f') with f' the vorticity force for the next
     frame (zeros without vorticity)."""
     n = len(x)
-    p, _ = _predict(C, x, v, f)
+    p, mask = _predict(C, x, v, f)
     I0, J0 = candidate_pairs(p, C.M)
     if tape is not None:
         tape.append(dict(x=x.copy(), v=v.copy(), f=None if f is None else f.copy(), I=I0, J=J0, p=[]))
-    x = x.copy()
+    x, _ = _damp(C, x.copy(), p, mask)
     for _ in range(C.iters):
         if tape is not None:
             tape[-1]["p"].append(p.copy())
@@ -348,9 +358,13 @@ def frame_backward(C, rec, gxo, gvo, acc, gf=None):
         rbar2 = (Cbar[I] / C.rho0 * dW)[:, None] * rh + (2.0 * Dbar[I] / C.rho0)[:, None] * _hess_mul(g, dg, L, rh, G + S[I])
         gnew += _sum(I, rbar2, n) - _sum(J, rbar2, n)
         gp = gnew
-    _, mask = _predict(C, rec["x"], rec["v"], rec["f"])
-    gx_in = gx + mask * gp
-    gv_in = mask * gp * C.dt
+    p0, mask = _predict(C, rec["x"], rec["v"], rec["f"])
+    _, anyc = _damp(C, rec["x"], p0, mask)
+    # p = clamp(x + v* dt); x' = x + pd any (p - x): dx'/dx = 1 - pd any + pd any mask,
+    # dx'/dv* = pd any mask dt (per axis; gx is dL/dx')
+    k = C.pd * anyc.astype(np.float64)[:, None]
+    gx_in = mask * gp + gx * (1.0 - k + k * mask)
+    gv_in = mask * (gp + k * gx) * C.dt
     moves = np.ones(n) if C.w is None else (C.w != 0.0).astype(np.float64)
     return gx_in, gv_in, gv_in * (C.dt * moves)[:, None]     # v* = v + dt (g + f): dL/df = dt dL/dv*
 

@@ -654,7 +654,7 @@ adj_lambda_kernel(DevParams P, const float4* __restrict__ p, const float4* __res
 }
 
 // re-order + applyForces backward, fused: sorted slot i came from pre-sort slot o = perm[i];
-// x_pred = x (no positional damping), p = x + v* dt unless the wall clamp fired on that axis.
+// p = x + v* dt unless the wall clamp fired on that axis, and x is damped toward p when it did.
 __global__ void adj_predict_kernel(DevParams P, const uint32_t* __restrict__ perm, const float4* __restrict__ x_in,
                                    const float4* __restrict__ v_in, const float4* __restrict__ fext,
                                    const float4* __restrict__ gp, const float4* __restrict__ gxp,
@@ -676,8 +676,13 @@ __global__ void adj_predict_kernel(DevParams P, const uint32_t* __restrict__ per
     const float mz = (pz < P.bmin[2] || pz > P.bmax[2]) ? 0.f : 1.f;
     const float4 g0 = gp[i], t = take_scattered(scat_in, i, fix_scale(gmax).inv), gx = gxp[i];   // + the last lambda pass's partners
     const float4 g = make_float4(g0.x + t.x, g0.y + t.y, g0.z + t.z, 0.f);
-    gx_out[o] = make_float4(gx.x + mx * g.x, gx.y + my * g.y, gx.z + mz * g.z, 0.f);
-    gv_out[o] = make_float4(mx * g.x * dt, my * g.y * dt, mz * g.z * dt, 0.f);
+    // enclosurePositionDamping (Forces.h:56-58): a particle clamped on some axis takes
+    // x' = x + pd (p - x) on every axis, so dx'/dx = 1 - k + k m and dx'/dv* = k m dt per axis
+    // (k = pd when clamped, m the axis's clamp mask; gx is dL/dx')
+    const float k = (mx == 0.f || my == 0.f || mz == 0.f) ? P.pos_damp : 0.f;
+    gx_out[o] = make_float4(mx * g.x + gx.x * (1.f - k + k * mx), my * g.y + gx.y * (1.f - k + k * my),
+                            mz * g.z + gx.z * (1.f - k + k * mz), 0.f);
+    gv_out[o] = make_float4(mx * (g.x + k * gx.x) * dt, my * (g.y + k * gx.y) * dt, mz * (g.z + k * gx.z) * dt, 0.f);
 }
 
 // Rebuild the cell tables of a taped frame from its sorted keys (computeCellInfo,

@@ -1606,7 +1606,6 @@ static int adjoint_supported(const pbd_sim* s) {
         set_error("adjoint: stabilizationIterations must be 0..8 and solverIterations 1..16");
         return PBD_ERR_UNSUPPORTED;
     }
-    if (p.enclosure_position_damping != 0.0f) { set_error("adjoint: enclosurePositionDamping must be 0"); return PBD_ERR_UNSUPPORTED; }
     if (s->batched) { set_error("adjoint: batches have no reverse pass"); return PBD_ERR_UNSUPPORTED; }
     if (p.collision_type != 0) { set_error("adjoint: collisionType 1 has no reverse pass"); return PBD_ERR_UNSUPPORTED; }
     return PBD_OK;

@@ -469,3 +469,58 @@ def test_gpu_adjoint_stabilization_passes(need_gpu, pbd, scenes, adj, stab, fram
     assert abs(gr - rr) <= 2e-3 * abs(rr) and abs(ge - re) <= 2e-3 * abs(re), (gr, rr, ge, re)
     for k in ("x", "v", "p", "ids"):
         assert np.array_equal(fin[k], after[k]), k
+
+
+def walled_scene(pbd, scenes, damping=0.5):
+    """The adjoint scene started against the low walls (origin 1.6, walls at 1.5) with
+    enclosurePositionDamping: particles are clamped on some axis in most frames, and a clamped
+    particle's x is pulled toward its clamped position (Forces.h:56-58)."""
+    prm = scenes.workload_params(pbd, 14, 1000.0, iterations=3, viscosity=0.01)
+    prm.lambda_epsilon = 0.1
+    prm.flags &= ~pbd.FLAG_CELL_END_QUIRK
+    prm.flags |= pbd.FLAG_TRACK_IDS
+    prm.enclosure_position_damping = damping
+    pos, vel = scenes.lattice(7, 7, 7, spacing=0.75, origin=(1.6, 1.6, 1.6), seed=5)
+    rng = np.random.default_rng(5)
+    vel[:, :3] = rng.normal(0, 1.0, size=(len(vel), 3)).astype(np.float32)
+    return prm, pos, vel, rng.normal(size=(len(pos), 3))
+
+
+def test_restatement_position_damping(pbd, scenes, oracle_mod, adj):
+    """enclosurePositionDamping 0.5 with particles at the walls: the FP64 restatement follows the
+    C oracle's FP64 trajectory and its reverse pass matches central differences"""
+    prm, pos, vel, w = walled_scene(pbd, scenes)
+    C = adj.Consts(prm)
+    o = oracle_mod.Oracle(prm, len(pos), "f64")
+    o.add_particles(pos, vel)
+    x0, v0 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+    x, v, f = x0, v0, None
+    clamped = 0
+    for _ in range(FRAMES):
+        clamped += int((~np.all(adj._predict(C, x, v, f)[1], axis=1)).sum())
+        o.step(1)
+        x, v, f = adj.frame(C, x, v, f)
+    assert clamped > 100
+    s = o.state()
+    order = np.argsort(s["ids"])
+    assert maxdiff(s["x"][order, :3], x) < 1e-8 and maxdiff(s["v"][order, :3], v) < 1e-6
+    gv, gx, gr, ge = adj.backward(C, x0, v0, FRAMES, w)
+    dirn = np.random.default_rng(11).normal(size=x0.shape)
+    h = 1e-7
+    fd_v = (_loss(adj, C, x0, v0 + h * dirn, w) - _loss(adj, C, x0, v0 - h * dirn, w)) / (2 * h)
+    fd_x = (_loss(adj, C, x0 + h * dirn, v0, w) - _loss(adj, C, x0 - h * dirn, v0, w)) / (2 * h)
+    assert abs(fd_v - np.sum(gv * dirn)) <= 1e-5 * abs(fd_v)
+    assert abs(fd_x - np.sum(gx * dirn)) <= 1e-5 * abs(fd_x)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("frames,tol,tol_scalar", [(1, 1e-4, 3e-4), (4, 0.02, 0.02)])
+def test_gpu_adjoint_position_damping(need_gpu, pbd, scenes, adj, frames, tol, tol_scalar):
+    """against the FP64 reverse pass (one frame: the scalars' sums over the wall particles, whose
+    clamped coordinate bmin + 0.001 rounds differently in FP32, agree to 1.3e-4)"""
+    prm, pos, vel, w = walled_scene(pbd, scenes)
+    C = adj.Consts(prm)
+    rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), frames, w)
+    _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, frames, 2)
+    assert _close_l2(gv, rv, tol) and _close_l2(gx, rx, tol)
+    assert abs(gr - rr) <= tol_scalar * abs(rr) and abs(ge - re) <= tol_scalar * abs(re), (gr, rr, ge, re)
