@@ -40,7 +40,7 @@ extern "C" {
 #define PBD_ERR_CUDA          3  /* a CUDA runtime call failed (text in pbd_last_error) */
 #define PBD_ERR_CONFIG        4  /* config.txt could not be read or parsed */
 #define PBD_ERR_TIMEOUT       5  /* a bounded device-side wait gave up (no hang, no trap) */
-#define PBD_ERR_UNSUPPORTED   6  /* a valid reference option this build does not implement */
+#define PBD_ERR_UNSUPPORTED   6  /* a valid reference option this library does not implement */
 #define PBD_ERR_ALLOC         7  /* device or host allocation failed */
 #define PBD_ERR_RANGE         8  /* a parameter is outside the range the reference's setters accept */
 

@@ -1,7 +1,7 @@
 /*
  * pbd_oracle.c -- CPU restatement of the reference PBD step.  TEST INFRASTRUCTURE ONLY.
  *
- * This file is the checker, never the product: only tests/, __graft_entry__.smoke() and
+ * This file is the oracle, never the product: only tests/, __graft_entry__.smoke() and
  * bench.py's CPU-baseline / reference arm load it.  The shipped library never links it.
  *
  * It restates niklasandersson/PBD-Simulation-Framework-CUDA's Fluid::compute()

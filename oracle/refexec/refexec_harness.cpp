@@ -1,5 +1,5 @@
 /* refexec_harness.cpp -- drives the reference's own kernel code on the CPU.  TEST
- * INFRASTRUCTURE ONLY (the checker that pins the oracle; never shipped).
+ * INFRASTRUCTURE ONLY (it pins the oracle to the reference's own kernels; never shipped).
  *
  * build_refexec.py compiles this file after the reference's kernel headers, in one translation
  * unit, with refexec_shim.h in front.  The harness restates only the host glue the reference
