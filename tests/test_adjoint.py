@@ -524,3 +524,61 @@ def test_gpu_adjoint_position_damping(need_gpu, pbd, scenes, adj, frames, tol, t
     _, _, _, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, frames, 2)
     assert _close_l2(gv, rv, tol) and _close_l2(gx, rx, tol)
     assert abs(gr - rr) <= tol_scalar * abs(rr) and abs(ge - re) <= tol_scalar * abs(re), (gr, rr, ge, re)
+
+
+def test_restatement_everything_at_once(pbd, scenes, oracle_mod, adj):
+    """Solids, vorticity, XSPH viscosity, two stabilization passes and wall damping together
+    (particles started against the walls): the FP64 restatement follows the C oracle and its
+    reverse pass matches central differences for v0, x0, the rest density and eps"""
+    prm, pos, vel, w = walled_scene(pbd, scenes)
+    prm.e_vorticity = 0.01
+    prm.active |= pbd.ACTIVE["computeOmegas"] | pbd.ACTIVE["computeVorticity"]
+    prm.stabilization_iterations = 2
+    vel, m = with_solids(pos, vel)
+    C = adj.Consts(prm, m)
+    o = oracle_mod.Oracle(prm, len(pos), "f64")
+    o.add_particles_mass(pos, vel, m)
+    frames = 4
+    x0, v0 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+    x, v, f = x0, v0, None
+    for _ in range(frames):
+        o.step(1)
+        x, v, f = adj.frame(C, x, v, f)
+    s = o.state()
+    order = np.argsort(s["ids"])
+    assert maxdiff(s["x"][order, :3], x) < 1e-8 and maxdiff(s["v"][order, :3], v) < 1e-6
+    gv, gx, gr, ge = adj.backward(C, x0, v0, frames, w)
+    loss = lambda c, xx, vv: float(np.sum(w * adj.rollout(c, xx, vv, frames)[0]))
+    dirn = np.random.default_rng(11).normal(size=x0.shape)
+    h = 1e-7
+    fd_v = (loss(C, x0, v0 + h * dirn) - loss(C, x0, v0 - h * dirn)) / (2 * h)
+    fd_x = (loss(C, x0 + h * dirn, v0) - loss(C, x0 - h * dirn, v0)) / (2 * h)
+    assert abs(fd_v - np.sum(gv * dirn)) <= 1e-4 * abs(fd_v), (fd_v, np.sum(gv * dirn))
+    assert abs(fd_x - np.sum(gx * dirn)) <= 1e-4 * abs(fd_x), (fd_x, np.sum(gx * dirn))
+    for attr, g in (("rho0", gr), ("eps", ge)):
+        base = getattr(C, attr)
+        hh = 1e-7 * base
+        cp, cm = copy.copy(C), copy.copy(C)
+        setattr(cp, attr, base + hh)
+        setattr(cm, attr, base - hh)
+        fd = (loss(cp, x0, v0) - loss(cm, x0, v0)) / (2 * hh)
+        assert abs(fd - g) <= 1e-4 * abs(fd), (attr, fd, g)
+
+
+@pytest.mark.gpu
+def test_gpu_adjoint_everything_at_once(need_gpu, pbd, scenes, adj):
+    """Solids, vorticity, XSPH viscosity and two stabilization passes together over two frames
+    (the vorticity force acts in the second) against the FP64 reverse pass, on the calm scene
+    (there the FP64 gradients move by at most 4e-3 when the initial positions move by 1e-5)"""
+    prm, pos, vel, w = calm_scene(pbd, scenes, 2)
+    prm.enclosure_position_damping = 0.5
+    prm.e_vorticity = 0.01
+    prm.active |= pbd.ACTIVE["computeOmegas"] | pbd.ACTIVE["computeVorticity"]
+    vel, m = with_solids(pos, vel)
+    C = adj.Consts(prm, m)
+    rv, rx, rr, re = adj.backward(C, pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64), 2, w)
+    _, fin, after, gv, gx, gr, ge = _gpu_grads(pbd, prm, pos, vel, w, 2, 1, m)
+    assert _close_l2(gv, rv, 1e-2) and _close_l2(gx, rx, 1e-2)
+    assert abs(gr - rr) <= 1e-2 * abs(rr) and abs(ge - re) <= 1e-2 * abs(re), (gr, rr, ge, re)
+    for k in ("x", "v", "p", "ids"):
+        assert np.array_equal(fin[k], after[k]), k
