@@ -170,8 +170,9 @@ int pbd_clear(pbd_sim* sim);
 /* ---- the step -------------------------------------------------------------------- */
 /* Run `nsteps` frames of Fluid::compute() (Fluid.cu:14-97) on `stream` (a cudaStream_t,
  * NULL = legacy default stream).  The whole frame is one CUDA graph launch; nothing is
- * synchronised.  Simulation::step's cudaDeviceSynchronize (Simulation.cu:16-19) is
- * pbd_sync(). */
+ * synchronised, except that when the sim's previous call queued work on another stream the host
+ * first waits for that stream.  Simulation::step's cudaDeviceSynchronize (Simulation.cu:16-19)
+ * is pbd_sync(). */
 int pbd_step(pbd_sim* sim, int nsteps, void* stream);
 /* Wait for the sim's queued work and report device-side error words
  * (PBD_ERR_TIMEOUT if a bounded wait gave up). */
