@@ -18,6 +18,9 @@
  *  - A pbd_sim handle is externally synchronised: one host thread at a time.  Separate
  *    handles are independent.  All GPU work of a call is queued on the stream passed to
  *    it (NULL = the legacy default stream) and is asynchronous unless stated otherwise.
+ *    A handle remembers the stream of its last call and, when the next call comes on
+ *    another stream, first waits for that one: keep a stream alive until the handle's
+ *    next call (or pbd_sync) after the last use of it.
  *  - Particles are kept in Morton-sorted order, exactly as the reference re-orders its
  *    textures every frame (kernel/SortReorder.h:86-129); pbd_get_state returns that order.
  */
